@@ -1,0 +1,315 @@
+#!/usr/bin/env python3
+"""Benchmark: FP64 cell-stage updates per second of the multi-material
+finite-volume step (3D shock-bubble, 256^3 cells, RK2) on GB300.
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference] [--size 256]
+
+`value`: whole-job cell-stage updates/s with the state resident in HBM,
+device-timed with CUDA events on the library stream over K steps (the step
+loop runs as a replayed CUDA graph; dt never leaves the device).
+`e2e`: the same metric through the C ABI with host buffers -- every step
+uploads {V, ID, phi} from pinned host memory, computes dt, advances one step
+and downloads the new state.
+`--impl reference`: the reference arm -- the oracle's CPU restatement of the
+reference numerics (the reference itself needs MPI and PETSc, absent on the
+box) on a bounded sample of the workload with every host thread.
+N > 1 (torchrun): replicas only -- every rank advances its own copy of the
+workload; no data-path collective (the reference's halo exchange has no
+counterpart on one GPU per replica); value = all ranks' cell-stages / max time.
+"""
+import argparse
+import ctypes as C
+import json
+import os
+import shutil
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+import numpy as np
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "FP64 cell-stage updates/s (1 GB300) + Newton iters/interface, MLP vs cold start @1e-10"
+UNIT = "cell-stage/s"
+MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
+# FP64 fused multiply-add rate measured on this machine's GB300 with a dependent-chain
+# microbenchmark (1.91 DFMA/clk/SM at 2070 MHz, 152 SMs): 601.6e9 DFMA/s.
+FP64_DFMA_PER_S = 601.6e9
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    ap.add_argument("--size", type=int, default=256)
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--cpu-size", type=int, default=96)
+    ap.add_argument("--cpu-steps", type=int, default=2)
+    ap.add_argument("--no-cpu", action="store_true")
+    return ap.parse_args()
+
+
+def dist_info():
+    return int(os.environ.get("RANK", 0)), int(os.environ.get("WORLD_SIZE", 1)), int(os.environ.get("LOCAL_RANK", 0))
+
+
+class Clocks:
+    """nvidia-smi sampling of SM clocks and throttle reasons during the timed region."""
+
+    def __init__(self, gpu_index):
+        self.proc = None
+        self.path = None
+        smi = shutil.which("nvidia-smi")
+        if not smi:
+            return
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        self.proc = subprocess.Popen([smi, "-i", str(gpu_index), f"--query-gpu={q}", "--format=csv,noheader,nounits",
+                                      "-lms", "200"], stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+
+    def stop(self):
+        if not self.proc:
+            return None
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                smax = float(f[2])
+            except ValueError:
+                continue
+            for n, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(n)
+        os.unlink(self.path)
+        if not sm:
+            return None
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": smax, "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def peaks():
+    try:
+        return json.load(open(MEASURED_PEAKS)), "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def cpu_port_rate(size, steps, threads=None):
+    """Oracle restatement on the host cores, shock-bubble sample of `size`^3 cells."""
+    from m2c_gb300 import problems
+    from oracle import binding as ob
+    lib = ob.lib()
+    if threads:
+        lib.orc_set_threads(threads)
+    used = lib.orc_max_threads()
+    cfg, V, ID, phi = problems.shock_bubble(n=size)
+    sim = ob.OracleSim(cfg)
+    sim.upload(V, ID, phi)
+    sim.run(1)
+    t0 = time.perf_counter()
+    sim.run(steps)
+    t = time.perf_counter() - t0
+    cells = size ** 3
+    return cells * 2 * steps / t, used, t
+
+
+def run_reference(args):
+    rank, world, _ = dist_info()
+    if rank != 0:
+        return 0
+    # each step: one RK2 step of the oracle on a bounded sample of the workload
+    threads = os.cpu_count()
+    from oracle import binding as ob
+    from m2c_gb300 import problems
+    ob.lib().orc_set_threads(threads)
+    size = args.cpu_size
+    cfg, V, ID, phi = problems.shock_bubble(n=size)
+    sim = ob.OracleSim(cfg)
+    sim.upload(V, ID, phi)
+    for _ in range(args.warmup):
+        sim.run(1)
+    t0 = time.perf_counter()
+    sim.run(args.steps)
+    t = time.perf_counter() - t0
+    cells = size ** 3
+    value = cells * 2 * args.steps / t
+    c = sim.counters()
+    sample = (f"shock-bubble {size}^3 cells (same physics, IC and numerics as the {args.size}^3 workload), "
+              f"{args.steps} RK2 steps after {args.warmup} warm-up")
+    out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"shock-bubble {args.size}^3, SG/SG, MUSCL-van Albada, HLLC, exact interface "
+                                  f"Riemann @1e-10, RK2, CFL 0.4", "cells": cells, "sample": sample,
+                      "parallelism": "replicas" if args.gpus > 1 else "single"},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+           "riemann": {"mean_iters_per_solve": c["riemann_iterations"] / max(c["riemann_solves"], 1),
+                       "solves": c["riemann_solves"]},
+           "note": "CPU restatement of the reference numerics (oracle/), OpenMP on all host threads; "
+                   "the m2c binary needs MPI + PETSc, absent on the box"}
+    print(json.dumps(out))
+    return 0
+
+
+def run_gb300(args):
+    rank, world, local = dist_info()
+    pg = None
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+        pg = dist
+    from m2c_gb300 import abi, problems
+    from m2c_gb300.solver import FluidState, Solver
+    lib = abi.load()
+    cfg, V, ID, phi = problems.shock_bubble(n=args.size)
+    cells = cfg.nx * cfg.ny * cfg.nz
+    stages = 2
+    s = Solver(cfg, FluidState(V, ID, phi))
+    ctx = s.ctx
+
+    def barrier():
+        if pg:
+            pg.barrier()
+
+    # warm-up (the first run captures the step into a CUDA graph)
+    s.run(args.warmup)
+    c0 = s.counters()
+    l0 = lib.m2cg_kernel_launches(ctx)
+    barrier()
+    lib.m2cg_sync(ctx)
+    clocks = Clocks(local)
+    lib.m2cg_event_record(ctx, 0)
+    s.run(args.steps)
+    lib.m2cg_event_record(ctx, 1)
+    lib.m2cg_sync(ctx)
+    barrier()
+    ms = C.c_float()
+    abi.check(lib, lib.m2cg_event_elapsed(ctx, 0, 1, C.byref(ms)), "elapsed")
+    launches = lib.m2cg_kernel_launches(ctx) - l0
+    c1 = s.counters()
+    clk = clocks.stop()
+    t_ms = ms.value
+    if pg:
+        import torch
+        t = torch.tensor([t_ms], dtype=torch.float64, device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        t_ms = float(t.item())
+    value = world * cells * stages * args.steps / (t_ms * 1e-3)
+    solves = c1["riemann_solves"] - c0["riemann_solves"]
+    iters = c1["riemann_iterations"] - c0["riemann_iterations"]
+
+    # per-phase device times (CUDA events around every kernel, same stream)
+    ph = np.zeros(8)
+    nph = 2
+    abi.check(lib, lib.m2cg_phase_times(ctx, nph, abi.dptr(ph)), "phase_times")
+    names = ["dt", "compact", "reconstruct", "face_flux", "riemann", "update", "bc", "end_of_step"]
+    phase = {n: float(v) / nph for n, v in zip(names, ph)}
+    dom = max(("reconstruct", "face_flux", "update"), key=lambda n: phase[n])
+    # algorithmic bytes per cell-stage for each stage kernel (binary64 state, int32 IDs)
+    #   reconstruct: read V (40) + ID (4), write 6 face states (240)            = 284
+    #   face_flux:   read 2 face states per face (3 faces: 240) + IDs (8), write 3 fluxes (120) = 368
+    #   update:      read 6 face fluxes (3 own + 3 neighbour faces, 240) + Un/Us (80) + ID (4) +
+    #                phi (8) + V own (40); write V (40) + phi (8) + U (40)       = 460
+    alg_bytes = {"reconstruct": 284, "face_flux": 368, "update": 460}
+    pk, pk_kind = peaks()
+    per_launch_ms = phase[dom] / stages
+    achieved_gbs = alg_bytes[dom] * cells / (per_launch_ms * 1e-3) / 1e9
+    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+            "frac": achieved_gbs / pk["hbm_gbs"], "traffic": None, "peak_source": pk_kind,
+            "alg_bytes_per_cell": alg_bytes[dom], "launch_ms": per_launch_ms}
+
+    # e2e through the C ABI with host buffers
+    e2e_steps = args.e2e_steps or max(2, min(args.steps, 5))
+    nb_v, nb_i, nb_p = cells * 5 * 8, cells * 4, cells * 8
+    hv = lib.m2cg_host_alloc(nb_v)
+    hi = lib.m2cg_host_alloc(nb_i)
+    hp = lib.m2cg_host_alloc(nb_p)
+    Vh = np.ctypeslib.as_array(C.cast(hv, C.POINTER(C.c_double)), shape=(cells * 5,))
+    Ih = np.ctypeslib.as_array(C.cast(hi, C.POINTER(C.c_int32)), shape=(cells,))
+    Ph = np.ctypeslib.as_array(C.cast(hp, C.POINTER(C.c_double)), shape=(cells,))
+    abi.check(lib, lib.m2cg_download_state(ctx, abi.dptr(Vh), abi.iptr(Ih), abi.dptr(Ph)), "download")
+    dt, cfl = C.c_double(), C.c_double()
+
+    def e2e_step():
+        abi.check(lib, lib.m2cg_upload_state(ctx, abi.dptr(Vh), abi.iptr(Ih), abi.dptr(Ph)), "upload")
+        abi.check(lib, lib.m2cg_compute_dt(ctx, C.byref(dt), C.byref(cfl)), "dt")
+        abi.check(lib, lib.m2cg_advance(ctx, dt.value), "advance")
+        abi.check(lib, lib.m2cg_download_state(ctx, abi.dptr(Vh), abi.iptr(Ih), abi.dptr(Ph)), "download")
+
+    e2e_step()
+    barrier()
+    t0 = time.perf_counter()
+    for _ in range(e2e_steps):
+        e2e_step()
+    te = time.perf_counter() - t0
+    barrier()
+    if pg:
+        import torch
+        t = torch.tensor([te], dtype=torch.float64, device="cuda")
+        pg.all_reduce(t, op=pg.ReduceOp.MAX)
+        te = float(t.item())
+    e2e_value = world * cells * stages * e2e_steps / te
+    for p in (hv, hi, hp):
+        lib.m2cg_host_free(p)
+
+    if rank != 0:
+        return 0
+    cpu = None
+    if not args.no_cpu:
+        rate, used, tcpu = cpu_port_rate(args.cpu_size, args.cpu_steps)
+        cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port",
+               "sample": f"oracle CPU restatement, shock-bubble {args.cpu_size}^3, {args.cpu_steps} RK2 steps "
+                         f"({tcpu:.1f} s)"}
+    # FP64 pipe view of the whole stage (from the fp64 op counts in profiles/)
+    out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
+           "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
+           "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+           "config": {"workload": f"shock-bubble {args.size}^3, SG/SG, MUSCL-van Albada, HLLC, exact interface "
+                                  f"Riemann @1e-10, RK2, CFL 0.4", "cells": cells, "stages_per_step": stages,
+                      "l2": "inputs larger than L2 (state 52 B/cell x 16.8M cells = 0.87 GB per copy)",
+                      "parallelism": "replicas" if world > 1 else "single"},
+           "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nb_v + nb_i + nb_p,
+                   "d2h_bytes_per_step": nb_v + nb_i + nb_p, "steps": e2e_steps},
+           "roofline": roof,
+           "cpu_baseline": cpu,
+           "gpu_launches": int(launches),
+           "clocks": clk,
+           "riemann": {"solves": solves, "mean_iters_per_solve": iters / max(solves, 1),
+                       "interface_faces_per_stage": (c1["interface_faces"] - c0["interface_faces"]) /
+                                                     max(stages * args.steps, 1),
+                       "errors": c1["riemann_errors"] - c0["riemann_errors"], "warm_start": "cold"},
+           "phase_ms_per_step": phase,
+           "counters": {k: c1[k] for k in ("clipped_cells", "nonphysical", "swept_cells", "unresolved_cells")}}
+    print(json.dumps(out))
+    return 0
+
+
+def main():
+    args = parse()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_gb300(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,235 @@
+/*
+ * m2cg.h -- C ABI of the GB300 multi-material finite-volume step (libm2cg.so).
+ *
+ * The library computes M2C's explicit multi-material finite-volume time step on
+ * one GPU: MUSCL reconstruction, HLLC / local Lax-Friedrichs / generalized Roe
+ * fluxes, stiffened-gas / Noble-Abel stiffened-gas / Mie-Gruneisen equations of
+ * state, the exact two-material Riemann solver at material interfaces, the
+ * level-set advection residual, the SSP Runge-Kutta stage update and the CFL
+ * time-step reduction.
+ *
+ * Every entry point takes plain pointers and sizes.  Host pointers are copied;
+ * the context owns all device memory.  Integer enum values follow the
+ * reference's IoData enums so a reference config maps field-for-field.
+ *
+ * Threading: one context per host thread; every call is issued on the
+ * context's own CUDA stream.  Calls that return host data synchronize that
+ * stream.  No entry point aborts the process: failures come back as an
+ * m2cg_status and per-step counters.
+ */
+#ifndef M2CG_H
+#define M2CG_H
+
+#include <stdint.h>
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define M2CG_ABI_VERSION 1
+#define M2CG_MAX_MATERIALS 8
+
+typedef enum {
+  M2CG_OK = 0,
+  M2CG_ERR_INVALID_ARG = 1,    /* null pointer, bad size, unsupported option */
+  M2CG_ERR_CUDA = 2,           /* a CUDA runtime call failed (message via m2cg_last_error) */
+  M2CG_ERR_NONPHYSICAL = 3,    /* a state failed CheckState; the reference calls exit(-1) here */
+  M2CG_ERR_UNRESOLVED = 4,     /* swept cell with no usable Riemann solution and no reinitializer */
+  M2CG_ERR_NO_DEVICE = 5,      /* no CUDA device visible */
+  M2CG_ERR_CAPACITY = 6        /* a fixed-size buffer would overflow */
+} m2cg_status;
+
+/* Equation of state (VarFcnBase::Type, VarFcnBase.h:40-42). */
+enum { M2CG_EOS_SG = 0, M2CG_EOS_NASG = 1, M2CG_EOS_MG = 2 };
+/* Boundary conditions (MeshData::BcType, IoData.h:283-284). */
+enum { M2CG_BC_INLET = 1, M2CG_BC_INLET2 = 2, M2CG_BC_SLIPWALL = 3, M2CG_BC_STICKWALL = 4,
+       M2CG_BC_SYMMETRY = 5, M2CG_BC_OUTLET = 7 };
+/* Level-set boundary conditions (LevelSetSchemeData::BcType, IoData.h:814). */
+enum { M2CG_LSBC_ZERO_NEUMANN = 1, M2CG_LSBC_LINEAR_EXTRAPOLATION = 2, M2CG_LSBC_NON_NEGATIVE = 3 };
+/* Numerical flux (SchemeData::Flux, IoData.h:710). */
+enum { M2CG_FLUX_ROE = 0, M2CG_FLUX_LLF = 1, M2CG_FLUX_HLLC = 2 };
+/* Reconstruction (ReconstructionData, IoData.h:660-671). */
+enum { M2CG_REC_CONSTANT = 0, M2CG_REC_LINEAR = 1 };
+enum { M2CG_LIM_NONE = 0, M2CG_LIM_GENERALIZED_MINMOD = 1, M2CG_LIM_VANALBADA = 2 };
+enum { M2CG_SLOPE_ZERO = 0, M2CG_SLOPE_NONZERO = 1 };
+enum { M2CG_VAR_PRIMITIVE = 0 };
+/* Multiphase (MultiPhaseData, IoData.h:893-903). */
+enum { M2CG_MPFLUX_EXACT = 0, M2CG_MPFLUX_NUMERICAL = 1, M2CG_MPFLUX_LLF = 2 };
+enum { M2CG_MPREC_CONSTANT = 0, M2CG_MPREC_LINEAR = 1 };
+enum { M2CG_PHASECHANGE_RIEMANN = 0, M2CG_PHASECHANGE_EXTRAPOLATION = 1 };
+enum { M2CG_PCDIR_ALL = 0, M2CG_PCDIR_UPWIND = 1 };
+/* Time integrator (ExplicitData::Type, IoData.h:931). */
+enum { M2CG_TS_FORWARD_EULER = 0, M2CG_TS_RK2 = 1, M2CG_TS_RK3 = 2 };
+
+/* One material: Equations.Material[i] (MaterialModelData, IoData.cpp:1044-1055;
+ * StiffenedGasModel / NobleAbelStiffenedGasModel / MieGruneisenModel). */
+typedef struct {
+  int32_t eos;                 /* M2CG_EOS_* */
+  int32_t pad_;
+  double gamma;                /* SG, NASG: SpecificHeatRatio */
+  double pc;                   /* SG, NASG: PressureConstant */
+  double b;                    /* NASG: VolumeConstant */
+  double q;                    /* NASG: EnergyConstant */
+  double rho0, c0, Gamma0, s, e0; /* MG: ReferenceDensity, BulkSpeedOfSound, GruneisenParameter,
+                                     HugoniotSlope, ReferenceSpecificInternalEnergy */
+  double rhomin, pmin, rhomax, pmax; /* DensityCutOff, PressureCutOff and the upper clips */
+  double failsafe_density;
+} m2cg_material;
+
+/* The subset of IoData the hot path reads, with the reference keys noted. */
+typedef struct {
+  /* Mesh: uniform Cartesian (MeshGenerator::ComputeMesh1DUniform, MeshGenerator.cpp:160-171) */
+  int32_t nx, ny, nz;
+  int32_t pad0_;
+  double x0, xmax, y0, ymax, z0, zmax;
+  int32_t bc[6];               /* BoundaryConditionX0, Xmax, Y0, Ymax, Z0, Zmax: M2CG_BC_* */
+  double inlet[5];             /* BoundaryConditions.Inlet  {Density, VelocityX/Y/Z, Pressure} */
+  double inlet2[5];            /* BoundaryConditions.Inlet2 */
+  /* Equations */
+  int32_t n_materials;         /* 1..M2CG_MAX_MATERIALS */
+  int32_t pad1_;
+  m2cg_material mat[M2CG_MAX_MATERIALS];
+  /* Space.NavierStokes */
+  int32_t flux;                /* Flux: M2CG_FLUX_* (default HLLC) */
+  int32_t rec_type;            /* Reconstruction.Type (default Linear) */
+  int32_t limiter;             /* Reconstruction.Limiter (default GeneralizedMinMod) */
+  int32_t rec_var;             /* Reconstruction.VariableType (Primitive only) */
+  int32_t slope_near_interface;/* Reconstruction.SlopeNearInterface (default NonZero) */
+  int32_t pad2_;
+  double minmod_coeff;         /* GeneralizedMinModCoefficient (1.2) */
+  double roe_delta;            /* EntropyFixCoefficient (0.2) */
+  /* MultiPhase */
+  int32_t mp_flux;             /* Flux (default Numerical) */
+  int32_t mp_recon;            /* ReconstructionAtInterface (default Constant) */
+  int32_t mp_phasechange;      /* PhaseChange (default RiemannSolution) */
+  int32_t mp_phasechange_dir;  /* PhaseChangeDirection (default Upwind) */
+  /* ExactRiemannSolution (ExactRiemannSolverData, IoData.cpp:1622-1637) */
+  int32_t maxits_main, maxits_bracket, maxits_shock, numsteps_rarefaction;
+  double tol_main, tol_shock, tol_rarefaction;
+  double min_pressure, failure_threshold, pressure_at_failure;
+  /* Space.LevelSet[0] (one level set; finite-difference solver) */
+  int32_t n_levelsets;         /* 0 or 1 */
+  int32_t ls_matid;            /* LevelSet[0].MaterialID */
+  int32_t ls_bc[6];            /* BoundaryConditionX0..Zmax: M2CG_LSBC_* */
+  /* Time */
+  int32_t ts_type;             /* Explicit.Type: M2CG_TS_* */
+  int32_t max_its;             /* MaxIts */
+  double cfl;                  /* CFL (0.5) */
+  double timestep;             /* TimeStep (<=0: CFL-driven) */
+  double max_time;             /* MaxTime */
+  /* Learned warm start for the interface Riemann solve (no reference counterpart) */
+  int32_t warm_start;          /* 0 = cold start (reference), 1 = MLP warm start */
+  int32_t pad3_;
+} m2cg_config;
+
+/* Per-step counters (the reference prints these as warnings; SpaceOperator.cpp:681-683,
+ * 2031-2034, 2557-2559). */
+typedef struct {
+  int64_t interface_faces;     /* faces whose two cells carry different material IDs */
+  int64_t riemann_errors;      /* ComputeRiemannSolution returned non-zero */
+  int64_t riemann_iterations;  /* secant iterations + bracketing evaluations, summed */
+  int64_t riemann_solves;      /* exact solves performed (faces x stages) */
+  int64_t clipped_cells;       /* ClipDensityAndPressure hits in stage updates */
+  int64_t clipped_faces;       /* clipped reconstructed face states */
+  int64_t nonphysical;         /* CheckState failures (reference: exit(-1)) */
+  int64_t swept_cells;         /* cells whose material ID changed this step */
+  int64_t unresolved_cells;    /* swept cells with no Riemann solution / extrapolation */
+  int64_t steps;               /* time steps taken on this context */
+  double time;                 /* simulated time */
+  double dt;                   /* last time step */
+  double cfl;                  /* last CFL number */
+} m2cg_counters;
+
+typedef struct m2cg_ctx m2cg_ctx;
+
+/* ---- library ---------------------------------------------------------- */
+int32_t     m2cg_abi_version(void);
+/* sizeof(m2cg_config) and sizeof(m2cg_counters), for bindings that mirror the structs. */
+size_t      m2cg_config_size(void);
+size_t      m2cg_counters_size(void);
+const char* m2cg_last_error(void);
+/* IoData defaults (IoData.cpp:1044-1055, 1262-1272, 1368-1374, 1508-1530, 1618-1637,
+ * 1690-1710, 1838-1850). */
+m2cg_status m2cg_config_default(m2cg_config* cfg);
+
+/* ---- context ---------------------------------------------------------- */
+/* Replaces the construction in Main.cpp:88-222 and 475-491 (VarFcn, FluxFcn,
+ * ExactRiemannSolverBase, SpaceOperator, LevelSetOperator, TimeIntegrator). */
+m2cg_status m2cg_create(const m2cg_config* cfg, m2cg_ctx** out);
+void        m2cg_destroy(m2cg_ctx* ctx);
+
+/* State upload / download over the real cells, k-major then j then i.
+ * V: N x 5 doubles, dof-interleaved like SpaceVariable3D (rho, u, v, w, p).
+ * id: N material IDs.  phi: N doubles (ignored when n_levelsets == 0).
+ * Ghost cells are filled by the boundary conditions. */
+m2cg_status m2cg_upload_state(m2cg_ctx* ctx, const double* V, const int32_t* id, const double* phi);
+m2cg_status m2cg_download_state(m2cg_ctx* ctx, double* V, int32_t* id, double* phi);
+
+/* SpaceOperator::ComputeTimeStepSize (SpaceOperator.cpp:1298-1330). */
+m2cg_status m2cg_compute_dt(m2cg_ctx* ctx, double* dt, double* cfl);
+
+/* SpaceOperator::ComputeResidual on the current state with the stored
+ * Riemann solutions refreshed (SpaceOperator.cpp:2573-2641, first RK stage).
+ * R: N x 5 doubles (real cells), may be NULL to keep the residual on device. */
+m2cg_status m2cg_compute_residual(m2cg_ctx* ctx, double* R);
+
+/* LevelSetOperator::ComputeResidual, finite-difference solver
+ * (LevelSetOperator.cpp:768-870). Rphi: N doubles. */
+m2cg_status m2cg_levelset_residual(m2cg_ctx* ctx, double* Rphi);
+
+/* TimeIntegratorBase::AdvanceOneTimeStep with a given dt, including the
+ * end-of-step material-ID and interface-state update (TimeIntegrator.cpp:319-455,
+ * 527-715, 720-843). */
+m2cg_status m2cg_advance(m2cg_ctx* ctx, double dt);
+
+/* The step loop of Main.cpp:653-771: n_steps x (ComputeTimeStepSize, clamp to
+ * MaxTime, AdvanceOneTimeStep).  dt stays on the device; nothing is copied to
+ * the host until the call returns.  Counters are summed over the steps. */
+m2cg_status m2cg_run(m2cg_ctx* ctx, int32_t n_steps, m2cg_counters* counters);
+
+m2cg_status m2cg_get_counters(m2cg_ctx* ctx, m2cg_counters* counters);
+
+/* Conserved totals sum(U * vol) over real cells: mass, momentum x/y/z, energy. */
+m2cg_status m2cg_conserved_totals(m2cg_ctx* ctx, double totals[5]);
+
+/* ---- batched device kernels (unit-level parity surface) ---------------- */
+/* ExactRiemannSolverBase::ComputeRiemannSolution (ExactRiemannSolverBase.cpp:59-347)
+ * for n independent problems, host arrays:
+ *   Vm, Vp: n x 5; idm, idp: n; dir: n x 3 (unit normals)
+ *   Vs, Vsm, Vsp: n x 5 outputs; id: n; iters: n (secant + bracketing evaluations);
+ *   err: n (the reference's return code: 0 ok, 1 failed). */
+m2cg_status m2cg_riemann_batch(m2cg_ctx* ctx, int64_t n,
+                               const double* Vm, const int32_t* idm,
+                               const double* Vp, const int32_t* idp, const double* dir,
+                               double* Vs, int32_t* id, double* Vsm, double* Vsp,
+                               int32_t* iters, int32_t* err);
+
+/* FluxFcn*::ComputeNumericalFluxAtCellInterface (FluxFcnHLLC.h:196-245,
+ * FluxFcnLLF.h:80-111, FluxFcnGenRoe.h:183-213) with the context's flux type,
+ * host arrays: dir n; Vm, Vp n x 5; id n; F n x 5 output. */
+m2cg_status m2cg_flux_batch(m2cg_ctx* ctx, int64_t n, const int32_t* dir,
+                            const double* Vm, const double* Vp, const int32_t* id, double* F);
+
+/* ---- timing on the context stream -------------------------------------- */
+m2cg_status m2cg_sync(m2cg_ctx* ctx);
+/* Records CUDA event `slot` (0..15) on the context stream. */
+m2cg_status m2cg_event_record(m2cg_ctx* ctx, int32_t slot);
+/* Milliseconds between two recorded events (synchronizes on the second). */
+m2cg_status m2cg_event_elapsed(m2cg_ctx* ctx, int32_t slot0, int32_t slot1, float* ms);
+/* Runs n_steps CFL-driven steps launch by launch with a CUDA event pair around
+ * every kernel and returns the summed device milliseconds per phase:
+ * [0] dt reduction, [1] interface compaction, [2] reconstruction, [3] face fluxes,
+ * [4] interface Riemann solves, [5] residual gather + stage update, [6] boundary
+ * conditions, [7] end-of-step material update. */
+m2cg_status m2cg_phase_times(m2cg_ctx* ctx, int32_t n_steps, double ms[8]);
+/* Kernel launches issued on this context since creation (all kernels are this library's). */
+int64_t     m2cg_kernel_launches(m2cg_ctx* ctx);
+/* Page-locked host memory for fast upload / download (NULL on failure). */
+void*       m2cg_host_alloc(size_t bytes);
+void        m2cg_host_free(void* ptr);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* M2CG_H */

@@ -1,0 +1,693 @@
+// Host side of libm2cg: the context that owns device memory and the stream,
+// the step orchestration (captured once into a CUDA graph and replayed), and
+// the extern "C" entry points declared in include/m2cg.h.
+#include <cstdio>
+#include <cstring>
+#include <cstdarg>
+#include <vector>
+#include <string>
+#include <algorithm>
+#include "m2cg_internal.h"
+
+namespace m2cg {
+void launch_reconstruct(cudaStream_t, const Params&, const StateSet&, const int32_t*, double* const*, unsigned long long*);
+void launch_face_flux(cudaStream_t, const Params&, const int32_t*, double* const*, double* const*, unsigned long long*);
+void launch_update(cudaStream_t, const Params&, const StageArgs&, const int32_t*, int32_t*, double* const*,
+                   const IfaceList&, const DevScalars*, int64_t*, unsigned long long*, int64_t, unsigned long long*);
+void launch_ls_residual(cudaStream_t, const Params&, const StateSet&, double*);
+void launch_bc(cudaStream_t, const Params&, const StateSet&, int, int, int32_t*, const DevScalars*);
+void launch_dt(cudaStream_t, const Params&, const StateSet&, const int32_t*, DevScalars*, int, double);
+void launch_compact(cudaStream_t, const Params&, const int32_t*, const IfaceList&, unsigned long long*,
+                    const DevScalars*);
+void launch_end_of_step(cudaStream_t, const Params&, const StateSet&, int32_t*, int32_t*, const IfaceList&,
+                        const int64_t*, const unsigned long long*, int64_t, int32_t*, unsigned long long*,
+                        const DevScalars*, int);
+void launch_conserved(cudaStream_t, const Params&, const StateSet&, const int32_t*, double*, int*);
+void launch_unpack(cudaStream_t, const Params&, const double*, const int32_t*, const double*, const StateSet&, int32_t*,
+                   unsigned long long*);
+void launch_pack(cudaStream_t, const Params&, const StateSet&, const int32_t*, double*, int32_t*, double*,
+                 double* const*, double*, const double*, double*);
+void launch_riemann_interfaces(cudaStream_t, const Params&, const Mats*, const StateSet&, const int32_t*,
+                               double* const*, const IfaceList&, int, double*, int, int, int, const float*,
+                               unsigned long long*, const DevScalars*);
+void launch_riemann_batch(cudaStream_t, const Params&, const Mats*, int64_t, const double*, const int32_t*,
+                          const double*, const int32_t*, const double*, double*, int32_t*, double*, double*, int32_t*,
+                          int32_t*, double*, int, int, int, const double*);
+void launch_flux_batch(cudaStream_t, const Params&, int64_t, const int32_t*, const double*, const double*,
+                       const int32_t*, double*);
+}  // namespace m2cg
+
+using namespace m2cg;
+
+static thread_local std::string g_err;
+static void set_err(const char* fmt, ...) {
+  char buf[512];
+  va_list a;
+  va_start(a, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, a);
+  va_end(a);
+  g_err = buf;
+}
+
+#define CK(call)                                                                          \
+  do {                                                                                    \
+    cudaError_t e_ = (call);                                                              \
+    if (e_ != cudaSuccess) {                                                              \
+      set_err("%s failed: %s (%s:%d)", #call, cudaGetErrorString(e_), __FILE__, __LINE__); \
+      return M2CG_ERR_CUDA;                                                               \
+    }                                                                                     \
+  } while (0)
+
+struct m2cg_ctx {
+  m2cg_config cfg;
+  Params P;
+  cudaStream_t stream = nullptr;
+  int nsm = 0;
+  std::vector<void*> allocs;
+  Mats* d_mats = nullptr;
+  StateSet S[3];
+  double* Un[5];
+  double* Us[5];
+  int32_t* id = nullptr;
+  int32_t* id_new = nullptr;
+  double** d_fs = nullptr;
+  double** d_F = nullptr;
+  double* R[5];
+  double** d_R = nullptr;
+  double* rphi = nullptr;
+  IfaceList L;
+  int64_t* swept = nullptr;
+  unsigned long long* swept_count = nullptr;
+  int64_t swept_cap = 0;
+  int32_t* cand = nullptr;
+  DevScalars* sc = nullptr;
+  unsigned long long* cnt = nullptr;
+  double* scratch = nullptr;
+  // Integration-path cache entries per wave.  The reference keeps an unbounded
+  // std::vector; 1024 entries covers the longest paths seen on random two-material
+  // problems (767); a solve that would exceed it is counted in CNT_PATH_CAPPED.
+  int path_cap = 1024;
+  int rblocks = 0, rthreads = 128;
+  double* partial = nullptr;
+  double* stage_V = nullptr;
+  int32_t* stage_id = nullptr;
+  double* stage_phi = nullptr;
+  cudaEvent_t ev[16];
+  int64_t launches = 0;
+  int64_t launches_per_step = 0;
+  cudaGraphExec_t graph_exec = nullptr;
+  // batch buffers
+  std::vector<void*> batch;
+  int64_t batch_n = 0;
+  double* batch_scratch = nullptr;
+  int64_t batch_threads = 0;
+
+  template <class T>
+  cudaError_t alloc(T** p, size_t count) {
+    void* q = nullptr;
+    cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) return e;
+    allocs.push_back(q);
+    *p = (T*)q;
+    return cudaMemsetAsync(q, 0, std::max<size_t>(count, 1) * sizeof(T), stream);
+  }
+};
+
+static m2cg_status fill_params(const m2cg_config& c, Params& P) {
+  if (c.nx < 1 || c.ny < 1 || c.nz < 1) { set_err("mesh dimensions must be >= 1"); return M2CG_ERR_INVALID_ARG; }
+  if (c.n_materials < 1 || c.n_materials > M2CG_MAX_MATERIALS) { set_err("n_materials out of range"); return M2CG_ERR_INVALID_ARG; }
+  if (c.rec_var != M2CG_VAR_PRIMITIVE) { set_err("only primitive-variable reconstruction is supported"); return M2CG_ERR_INVALID_ARG; }
+  if (c.n_levelsets < 0 || c.n_levelsets > 1) { set_err("at most one level set is supported"); return M2CG_ERR_INVALID_ARG; }
+  if (c.n_levelsets == 1 && (c.ls_matid < 0 || c.ls_matid >= c.n_materials)) { set_err("ls_matid out of range"); return M2CG_ERR_INVALID_ARG; }
+  if (c.ts_type < 0 || c.ts_type > 2) { set_err("bad ts_type"); return M2CG_ERR_INVALID_ARG; }
+  memset(&P, 0, sizeof(P));
+  Grid& g = P.g;
+  g.nx = c.nx; g.ny = c.ny; g.nz = c.nz;
+  g.px = c.nx + 2; g.py = c.ny + 2; g.pz = c.nz + 2;
+  g.sy = g.px; g.sz = (int64_t)g.px * g.py; g.ntot = g.sz * g.pz;
+  g.dx = (c.xmax - c.x0) / c.nx; g.dy = (c.ymax - c.y0) / c.ny; g.dz = (c.zmax - c.z0) / c.nz;
+  P.n_mat = c.n_materials;
+  for (int m = 0; m < c.n_materials; m++) {
+    const m2cg_material& s = c.mat[m];
+    DevMat& d = P.mats.m[m];
+    d.type = s.eos;
+    if (s.eos < 0 || s.eos > 2) { set_err("material %d: unsupported EOS %d", m, s.eos); return M2CG_ERR_INVALID_ARG; }
+    d.gam = s.gamma; d.gam1 = s.gamma - 1.0; d.Pstiff = s.pc; d.gamPs = s.gamma * s.pc;
+    d.invgam1 = 1.0 / (s.gamma - 1.0);
+    d.b = s.b; d.q = s.q;
+    d.rho0 = s.rho0; d.s = s.s; d.e0 = s.e0; d.rho0_c0_c0 = s.rho0 * s.c0 * s.c0;
+    d.G0_half = 0.5 * s.Gamma0; d.G0_rho0 = s.Gamma0 * s.rho0;
+    d.rhomin = s.rhomin; d.pmin = s.pmin; d.rhomax = s.rhomax; d.pmax = s.pmax;
+  }
+  P.flux = c.flux; P.rec_type = c.rec_type; P.limiter = c.limiter; P.slope_zero = (c.slope_near_interface == M2CG_SLOPE_ZERO);
+  P.mp_flux = c.mp_flux; P.mp_recon = c.mp_recon; P.mp_phasechange = c.mp_phasechange; P.mp_pcdir = c.mp_phasechange_dir;
+  P.minmod_coeff = c.minmod_coeff; P.roe_delta = c.roe_delta;
+  for (int s = 0; s < 6; s++) { P.bc[s] = c.bc[s]; P.ls_bc[s] = c.ls_bc[s]; }
+  for (int p = 0; p < 5; p++) { P.inlet[p] = c.inlet[p]; P.inlet2[p] = c.inlet2[p]; }
+  P.n_ls = c.n_levelsets; P.ls_matid = c.ls_matid;
+  RiemannPrm& r = P.rp;
+  r.maxIts_main = c.maxits_main; r.maxIts_bracket = c.maxits_bracket; r.maxIts_shock = c.maxits_shock;
+  r.numSteps = c.numsteps_rarefaction; r.tol_main = c.tol_main; r.tol_shock = c.tol_shock; r.tol_rare = c.tol_rarefaction;
+  r.min_pressure = c.min_pressure; r.failure_threshold = c.failure_threshold; r.pressure_at_failure = c.pressure_at_failure;
+  P.area[0] = g.dy * g.dz; P.area[1] = g.dx * g.dz; P.area[2] = g.dx * g.dy;
+  double vol = g.dx * g.dy * g.dz;
+  P.inv_negvol = 1.0 / (-vol);
+  // FD3 coefficients on a uniform mesh: the solution of the Taylor system of
+  // GradientCalculatorFD3.cpp:455-470 for offsets (-2h,-h,0,h) and (-h,0,h,2h).
+  const double h[3] = {g.dx, g.dy, g.dz};
+  for (int d = 0; d < 3; d++) {
+    double s6 = 1.0 / (6.0 * h[d]);
+    P.fd3l[d][0] = 1.0 * s6; P.fd3l[d][1] = -6.0 * s6; P.fd3l[d][2] = 3.0 * s6; P.fd3l[d][3] = 2.0 * s6;
+    P.fd3r[d][0] = -2.0 * s6; P.fd3r[d][1] = -3.0 * s6; P.fd3r[d][2] = 6.0 * s6; P.fd3r[d][3] = -1.0 * s6;
+  }
+  P.cfl = c.cfl; P.timestep = c.timestep; P.max_time = c.max_time; P.ts_type = c.ts_type;
+  return M2CG_OK;
+}
+
+static m2cg_status ctx_alloc(m2cg_ctx* x) {
+  const int64_t N = x->P.g.ntot;
+  for (int s = 0; s < 3; s++)
+    for (int q = 0; q < 6; q++) CK(x->alloc(&x->S[s].q[q], N));
+  for (int p = 0; p < 5; p++) { CK(x->alloc(&x->Un[p], N)); CK(x->alloc(&x->Us[p], N)); CK(x->alloc(&x->R[p], N)); }
+  CK(x->alloc(&x->rphi, N));
+  CK(x->alloc(&x->id, N));
+  CK(x->alloc(&x->id_new, N));
+  std::vector<double*> h_fs(30), h_F(15);
+  for (int f = 0; f < 30; f++) CK(x->alloc(&h_fs[f], N));
+  for (int f = 0; f < 15; f++) CK(x->alloc(&h_F[f], N));
+  CK(x->alloc(&x->d_fs, 30));
+  CK(x->alloc(&x->d_F, 15));
+  CK(x->alloc(&x->d_R, 5));
+  CK(cudaMemcpyAsync(x->d_fs, h_fs.data(), 30 * sizeof(double*), cudaMemcpyHostToDevice, x->stream));
+  CK(cudaMemcpyAsync(x->d_F, h_F.data(), 15 * sizeof(double*), cudaMemcpyHostToDevice, x->stream));
+  CK(cudaMemcpyAsync(x->d_R, x->R, 5 * sizeof(double*), cudaMemcpyHostToDevice, x->stream));
+  // interface list: capacity for N/16 + 64k faces
+  IfaceList& L = x->L;
+  L.cap = std::min<int64_t>(N / 16 + 65536, (int64_t)1 << 30);
+  CK(x->alloc(&L.face, L.cap));
+  for (int p = 0; p < 5; p++) {
+    CK(x->alloc(&L.lf1[p], L.cap)); CK(x->alloc(&L.lf2[p], L.cap));
+    CK(x->alloc(&L.vsm[p], L.cap)); CK(x->alloc(&L.vsp[p], L.cap));
+  }
+  CK(x->alloc(&L.err, L.cap));
+  CK(x->alloc(&L.iters, L.cap));
+  for (int d = 0; d < 3; d++) CK(x->alloc(&L.slot[d], N));
+  CK(x->alloc(&L.count, 1));
+  x->swept_cap = std::max<int64_t>(65536, N / 64);
+  CK(x->alloc(&x->swept, x->swept_cap));
+  CK(x->alloc(&x->cand, x->swept_cap));
+  CK(x->alloc(&x->swept_count, 1));
+  CK(x->alloc(&x->sc, 1));
+  CK(x->alloc(&x->cnt, CNT_N));
+  CK(x->alloc(&x->d_mats, 1));
+  CK(cudaMemcpyAsync(x->d_mats, &x->P.mats, sizeof(Mats), cudaMemcpyHostToDevice, x->stream));
+  x->rblocks = x->nsm * 2;
+  x->rthreads = 128;
+  CK(x->alloc(&x->scratch, (size_t)6 * x->path_cap * x->rblocks * x->rthreads));
+  int64_t nreal = (int64_t)x->P.g.nx * x->P.g.ny * x->P.g.nz;
+  CK(x->alloc(&x->partial, (size_t)((nreal + 255) / 256) * 5));
+  DevScalars s0;
+  memset(&s0, 0, sizeof(s0));
+  s0.min_dx_over_lambda = 0x7fefffffffffffffull;
+  s0.active = 1;
+  CK(cudaMemcpyAsync(x->sc, &s0, sizeof(s0), cudaMemcpyHostToDevice, x->stream));
+  for (int i = 0; i < 16; i++) CK(cudaEventCreate(&x->ev[i]));
+  CK(cudaStreamSynchronize(x->stream));
+  return M2CG_OK;
+}
+
+// Optional per-phase CUDA-event timing of a step (m2cg_phase_times).
+enum { PH_DT = 0, PH_COMPACT, PH_RECON, PH_FLUX, PH_RIEMANN, PH_UPDATE, PH_BC, PH_POST, PH_N };
+struct PhaseTimer {
+  std::vector<cudaEvent_t> ev;
+  std::vector<int> cat;
+  size_t used = 0;
+  cudaStream_t s = nullptr;
+  void begin(int c) {
+    if (used + 2 > ev.size()) { cudaEvent_t a, b; cudaEventCreate(&a); cudaEventCreate(&b); ev.push_back(a); ev.push_back(b); cat.push_back(0); cat.push_back(0); }
+    cat[used] = c;
+    cudaEventRecord(ev[used], s);
+  }
+  void end() { cudaEventRecord(ev[used + 1], s); used += 2; }
+};
+static PhaseTimer* g_timer = nullptr;  // set only inside m2cg_phase_times (not captured in graphs)
+#define PHASE(c, stmt) do { if (g_timer) g_timer->begin(c); stmt; if (g_timer) g_timer->end(); } while (0)
+
+// Enqueue one Runge-Kutta stage.
+static int64_t enqueue_stage(m2cg_ctx* x, int stage, bool last, const StateSet& in, const StateSet& out) {
+  cudaStream_t s = x->stream;
+  const Params& P = x->P;
+  int64_t n = 0;
+  PHASE(PH_RECON, launch_reconstruct(s, P, in, x->id, x->d_fs, x->cnt)); n += 2;
+  PHASE(PH_FLUX, launch_face_flux(s, P, x->id, x->d_fs, x->d_F, x->cnt)); n++;
+  PHASE(PH_RIEMANN, launch_riemann_interfaces(s, P, x->d_mats, in, x->id, x->d_fs, x->L, stage == 0, x->scratch,
+                                              x->path_cap, x->rblocks, x->rthreads, nullptr, x->cnt, x->sc)); n++;
+  StageArgs A;
+  memset(&A, 0, sizeof(A));
+  A.in = in;
+  A.out = out;
+  A.stage = stage;
+  A.last = last;
+  A.phi_lsin = in.q[5];
+  A.phi_own = in.q[5];
+  A.phi_tmp = x->S[0].q[5];
+  for (int p = 0; p < 5; p++) { A.Un[p] = x->Un[p]; A.Us[p] = x->Us[p]; }
+  const int ts = x->cfg.ts_type;
+  if (stage == 0) { A.store_un = (ts != M2CG_TS_FORWARD_EULER); }
+  if (ts == M2CG_TS_FORWARD_EULER) A.ls_use_updated_v = 1;
+  if (ts == M2CG_TS_RK2 && stage == 1) { A.a_own = 0.5; A.b_un = 0.5; A.c_dt = 0.5; A.la = 0.5; A.lb = 0.5; A.lc = 0.5; }
+  if (ts == M2CG_TS_RK3 && stage == 1) { A.a_own = 0.25; A.b_un = 0.75; A.c_dt = 0.25; A.la = 0.25; A.lb = 0.75; A.lc = 0.25; }
+  if (ts == M2CG_TS_RK3 && stage == 2) {
+    A.a_own = 2.0 / 3.0; A.b_un = 1.0 / 3.0; A.c_dt = 2.0 / 3.0; A.la = 2.0 / 3.0; A.lb = 1.0 / 3.0; A.lc = 2.0 / 3.0;
+  }
+  PHASE(PH_UPDATE, launch_update(s, P, A, x->id, x->id_new, x->d_F, x->L, x->sc, x->swept, x->swept_count,
+                                  x->swept_cap, x->cnt)); n++;
+  if (!last) { PHASE(PH_BC, launch_bc(s, P, out, 1, 1, nullptr, x->sc)); n++; }
+  return n;
+}
+
+// One time step (dt mode: 1 = CFL with MaxTime clamp, 2 = fixed dt).
+static int64_t enqueue_step(m2cg_ctx* x, int mode, double fixed_dt) {
+  cudaStream_t s = x->stream;
+  int64_t n = 0;
+  PHASE(PH_DT, launch_dt(s, x->P, x->S[0], x->id, x->sc, mode, fixed_dt)); n += 2;
+  cudaMemsetAsync(x->L.count, 0, sizeof(unsigned long long), s);
+  cudaMemsetAsync(x->swept_count, 0, sizeof(unsigned long long), s);
+  PHASE(PH_COMPACT, launch_compact(s, x->P, x->id, x->L, x->cnt, x->sc)); n++;
+  const int ts = x->cfg.ts_type;
+  if (ts == M2CG_TS_FORWARD_EULER) {
+    StateSet out = x->S[0];
+    out.q[5] = x->S[1].q[5];
+    n += enqueue_stage(x, 0, true, x->S[0], out);
+    if (x->P.n_ls > 0)
+      cudaMemcpyAsync(x->S[0].q[5], x->S[1].q[5], x->P.g.ntot * sizeof(double), cudaMemcpyDeviceToDevice, s);
+  } else if (ts == M2CG_TS_RK2) {
+    n += enqueue_stage(x, 0, false, x->S[0], x->S[1]);
+    n += enqueue_stage(x, 1, true, x->S[1], x->S[0]);
+  } else {
+    n += enqueue_stage(x, 0, false, x->S[0], x->S[1]);
+    n += enqueue_stage(x, 1, false, x->S[1], x->S[2]);
+    n += enqueue_stage(x, 2, true, x->S[2], x->S[0]);
+  }
+  if (x->P.n_ls > 0) {
+    PHASE(PH_POST, launch_end_of_step(s, x->P, x->S[0], x->id, x->id_new, x->L, x->swept, x->swept_count,
+                                      x->swept_cap, x->cand, x->cnt, x->sc, x->nsm));
+    n += 3 * 2 + 3;
+  } else {
+    PHASE(PH_BC, launch_bc(s, x->P, x->S[0], 1, 1, nullptr, x->sc)); n++;
+  }
+  return n;
+}
+
+extern "C" {
+
+int32_t m2cg_abi_version(void) { return M2CG_ABI_VERSION; }
+size_t m2cg_config_size(void) { return sizeof(m2cg_config); }
+size_t m2cg_counters_size(void) { return sizeof(m2cg_counters); }
+const char* m2cg_last_error(void) { return g_err.c_str(); }
+
+m2cg_status m2cg_config_default(m2cg_config* c) {
+  if (!c) return M2CG_ERR_INVALID_ARG;
+  memset(c, 0, sizeof(*c));
+  c->nx = c->ny = c->nz = 1;
+  c->xmax = c->ymax = c->zmax = 1.0;
+  for (int s = 0; s < 6; s++) { c->bc[s] = M2CG_BC_OUTLET; c->ls_bc[s] = M2CG_LSBC_ZERO_NEUMANN; }
+  c->n_materials = 1;
+  for (int m = 0; m < M2CG_MAX_MATERIALS; m++) {
+    m2cg_material& t = c->mat[m];
+    t.eos = M2CG_EOS_SG; t.gamma = 1.4; t.pc = 0.0;
+    t.rho0 = 1.0; t.c0 = 1.0; t.Gamma0 = 1.0; t.s = 1.0;
+    t.rhomin = 0.0; t.pmin = -DBL_MAX; t.rhomax = DBL_MAX; t.pmax = DBL_MAX; t.failsafe_density = 1.0e-10;
+  }
+  c->flux = M2CG_FLUX_HLLC;
+  c->rec_type = M2CG_REC_LINEAR;
+  c->limiter = M2CG_LIM_GENERALIZED_MINMOD;
+  c->rec_var = M2CG_VAR_PRIMITIVE;
+  c->slope_near_interface = M2CG_SLOPE_NONZERO;
+  c->minmod_coeff = 1.2;
+  c->roe_delta = 0.2;
+  c->mp_flux = M2CG_MPFLUX_NUMERICAL;
+  c->mp_recon = M2CG_MPREC_CONSTANT;
+  c->mp_phasechange = M2CG_PHASECHANGE_RIEMANN;
+  c->mp_phasechange_dir = M2CG_PCDIR_UPWIND;
+  c->maxits_main = 200; c->maxits_bracket = 100; c->maxits_shock = 200; c->numsteps_rarefaction = 200;
+  c->tol_main = 1.0e-5; c->tol_shock = 1.0e-12; c->tol_rarefaction = 1.0e-8;
+  c->min_pressure = -1.0e8; c->failure_threshold = 0.2; c->pressure_at_failure = 1.0e-8;
+  c->n_levelsets = 0; c->ls_matid = 1;
+  c->ts_type = M2CG_TS_RK2; c->max_its = 0x7fffffff;
+  c->cfl = 0.5; c->timestep = -1.0; c->max_time = 1e10;
+  c->warm_start = 0;
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_create(const m2cg_config* cfg, m2cg_ctx** out) {
+  if (!cfg || !out) { set_err("null argument"); return M2CG_ERR_INVALID_ARG; }
+  *out = nullptr;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_err("no CUDA device"); return M2CG_ERR_NO_DEVICE; }
+  m2cg_ctx* x = new m2cg_ctx();
+  x->cfg = *cfg;
+  m2cg_status st = fill_params(*cfg, x->P);
+  if (st != M2CG_OK) { delete x; return st; }
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&x->nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess) {
+    set_err("cudaStreamCreate failed");
+    delete x;
+    return M2CG_ERR_CUDA;
+  }
+  st = ctx_alloc(x);
+  if (st != M2CG_OK) { m2cg_destroy(x); return st; }
+  *out = x;
+  return M2CG_OK;
+}
+
+void m2cg_destroy(m2cg_ctx* x) {
+  if (!x) return;
+  if (x->stream) cudaStreamSynchronize(x->stream);
+  if (x->graph_exec) cudaGraphExecDestroy(x->graph_exec);
+  for (void* p : x->allocs) cudaFree(p);
+  for (void* p : x->batch) cudaFree(p);
+  if (x->batch_scratch) cudaFree(x->batch_scratch);
+  for (int i = 0; i < 16; i++) if (x->ev[i]) cudaEventDestroy(x->ev[i]);
+  if (x->stream) cudaStreamDestroy(x->stream);
+  delete x;
+}
+
+m2cg_status m2cg_upload_state(m2cg_ctx* x, const double* V, const int32_t* id, const double* phi) {
+  if (!x || !V || !id) { set_err("null argument"); return M2CG_ERR_INVALID_ARG; }
+  int64_t n = (int64_t)x->P.g.nx * x->P.g.ny * x->P.g.nz;
+  cudaStream_t s = x->stream;
+  if (!x->stage_V) {   // staging buffers for the host layout, kept for later uploads / downloads
+    CK(x->alloc(&x->stage_V, (size_t)n * 5));
+    CK(x->alloc(&x->stage_id, (size_t)n));
+    CK(x->alloc(&x->stage_phi, (size_t)n));
+  }
+  CK(cudaMemsetAsync(&x->cnt[CNT_BADID], 0, sizeof(unsigned long long), s));
+  CK(cudaMemcpyAsync(x->stage_V, V, n * 5 * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(x->stage_id, id, n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  bool with_phi = phi && x->P.n_ls > 0;
+  if (with_phi) CK(cudaMemcpyAsync(x->stage_phi, phi, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  launch_unpack(s, x->P, x->stage_V, x->stage_id, with_phi ? x->stage_phi : nullptr, x->S[0], x->id, x->cnt);
+  launch_bc(s, x->P, x->S[0], 1, 1, x->id, nullptr);
+  x->launches += 2;
+  CK(cudaMemcpyAsync(x->id_new, x->id, x->P.g.ntot * sizeof(int32_t), cudaMemcpyDeviceToDevice, s));
+  unsigned long long bad = 0;
+  CK(cudaMemcpyAsync(&bad, &x->cnt[CNT_BADID], sizeof(bad), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  if (bad) { set_err("%llu material IDs outside [0, n_materials)", bad); return M2CG_ERR_INVALID_ARG; }
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_download_state(m2cg_ctx* x, double* V, int32_t* id, double* phi) {
+  if (!x) { set_err("null argument"); return M2CG_ERR_INVALID_ARG; }
+  int64_t n = (int64_t)x->P.g.nx * x->P.g.ny * x->P.g.nz;
+  cudaStream_t s = x->stream;
+  if (!x->stage_V) {
+    CK(x->alloc(&x->stage_V, (size_t)n * 5));
+    CK(x->alloc(&x->stage_id, (size_t)n));
+    CK(x->alloc(&x->stage_phi, (size_t)n));
+  }
+  launch_pack(s, x->P, x->S[0], x->id, V ? x->stage_V : nullptr, id ? x->stage_id : nullptr,
+              phi ? x->stage_phi : nullptr, nullptr, nullptr, nullptr, nullptr);
+  x->launches++;
+  if (V) CK(cudaMemcpyAsync(V, x->stage_V, n * 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (id) CK(cudaMemcpyAsync(id, x->stage_id, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  if (phi) CK(cudaMemcpyAsync(phi, x->stage_phi, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_compute_dt(m2cg_ctx* x, double* dt, double* cfl) {
+  if (!x || !dt || !cfl) return M2CG_ERR_INVALID_ARG;
+  launch_dt(x->stream, x->P, x->S[0], x->id, x->sc, 0, 0.0);
+  x->launches += 2;
+  DevScalars h;
+  CK(cudaMemcpyAsync(&h, x->sc, sizeof(h), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  CK(cudaGetLastError());
+  *dt = h.dt;
+  *cfl = h.cfl;
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_compute_residual(m2cg_ctx* x, double* R) {
+  if (!x) return M2CG_ERR_INVALID_ARG;
+  cudaStream_t s = x->stream;
+  CK(cudaMemsetAsync(x->L.count, 0, sizeof(unsigned long long), s));
+  launch_compact(s, x->P, x->id, x->L, x->cnt, nullptr);
+  launch_reconstruct(s, x->P, x->S[0], x->id, x->d_fs, x->cnt);
+  launch_face_flux(s, x->P, x->id, x->d_fs, x->d_F, x->cnt);
+  launch_riemann_interfaces(s, x->P, x->d_mats, x->S[0], x->id, x->d_fs, x->L, 1, x->scratch, x->path_cap, x->rblocks,
+                            x->rthreads, nullptr, x->cnt, nullptr);
+  StageArgs A;
+  memset(&A, 0, sizeof(A));
+  A.in = x->S[0];
+  A.residual_only = 1;
+  for (int p = 0; p < 5; p++) A.R[p] = x->R[p];
+  launch_update(s, x->P, A, x->id, x->id_new, x->d_F, x->L, x->sc, x->swept, x->swept_count, x->swept_cap, x->cnt);
+  x->launches += 6;
+  if (R) {
+    int64_t n = (int64_t)x->P.g.nx * x->P.g.ny * x->P.g.nz;
+    double* dR;
+    CK(cudaMallocAsync(&dR, n * 5 * sizeof(double), s));
+    launch_pack(s, x->P, x->S[0], x->id, nullptr, nullptr, nullptr, x->d_R, dR, nullptr, nullptr);
+    x->launches++;
+    CK(cudaMemcpyAsync(R, dR, n * 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+    CK(cudaFreeAsync(dR, s));
+  }
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_levelset_residual(m2cg_ctx* x, double* Rphi) {
+  if (!x || !Rphi) return M2CG_ERR_INVALID_ARG;
+  if (x->P.n_ls == 0) { set_err("no level set configured"); return M2CG_ERR_INVALID_ARG; }
+  cudaStream_t s = x->stream;
+  launch_ls_residual(s, x->P, x->S[0], x->rphi);
+  int64_t n = (int64_t)x->P.g.nx * x->P.g.ny * x->P.g.nz;
+  double* d;
+  CK(cudaMallocAsync(&d, n * sizeof(double), s));
+  launch_pack(s, x->P, x->S[0], x->id, nullptr, nullptr, nullptr, nullptr, nullptr, x->rphi, d);
+  x->launches += 2;
+  CK(cudaMemcpyAsync(Rphi, d, n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaFreeAsync(d, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_advance(m2cg_ctx* x, double dt) {
+  if (!x || !(dt > 0)) { set_err("bad argument"); return M2CG_ERR_INVALID_ARG; }
+  x->launches += enqueue_step(x, 2, dt);
+  CK(cudaStreamSynchronize(x->stream));
+  CK(cudaGetLastError());
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_get_counters(m2cg_ctx* x, m2cg_counters* c) {
+  if (!x || !c) return M2CG_ERR_INVALID_ARG;
+  unsigned long long h[CNT_N];
+  DevScalars s;
+  CK(cudaMemcpyAsync(h, x->cnt, sizeof(h), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaMemcpyAsync(&s, x->sc, sizeof(s), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  memset(c, 0, sizeof(*c));
+  c->interface_faces = (int64_t)h[CNT_IFACE];
+  c->riemann_errors = (int64_t)h[CNT_RERR];
+  c->riemann_iterations = (int64_t)h[CNT_RITER];
+  c->riemann_solves = (int64_t)h[CNT_RSOLVE];
+  c->clipped_cells = (int64_t)h[CNT_CLIPCELL];
+  c->clipped_faces = (int64_t)h[CNT_CLIPFACE];
+  c->nonphysical = (int64_t)h[CNT_BAD];
+  c->swept_cells = (int64_t)h[CNT_SWEPT];
+  c->unresolved_cells = (int64_t)h[CNT_UNRES];
+  c->steps = s.steps;
+  c->time = s.time;
+  c->dt = s.dt;
+  c->cfl = s.cfl;
+  if (h[CNT_IF_OVERFLOW] || h[CNT_SWEPT_OVERFLOW]) {
+    set_err("interface or swept-cell list overflow");
+    return M2CG_ERR_CAPACITY;
+  }
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_run(m2cg_ctx* x, int32_t n_steps, m2cg_counters* counters) {
+  if (!x || n_steps < 0) return M2CG_ERR_INVALID_ARG;
+  cudaStream_t s = x->stream;
+  if (!x->graph_exec) {
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    x->launches_per_step = enqueue_step(x, 1, 0.0);
+    CK(cudaStreamEndCapture(s, &g));
+    CK(cudaGraphInstantiate(&x->graph_exec, g, 0));
+    cudaGraphDestroy(g);
+  }
+  for (int i = 0; i < n_steps; i++) {
+    CK(cudaGraphLaunch(x->graph_exec, s));
+    x->launches += x->launches_per_step;
+  }
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  if (counters) return m2cg_get_counters(x, counters);
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_conserved_totals(m2cg_ctx* x, double totals[5]) {
+  if (!x || !totals) return M2CG_ERR_INVALID_ARG;
+  int nb = 0;
+  launch_conserved(x->stream, x->P, x->S[0], x->id, x->partial, &nb);
+  x->launches++;
+  std::vector<double> h((size_t)nb * 5);
+  CK(cudaMemcpyAsync(h.data(), x->partial, h.size() * sizeof(double), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  double vol = x->P.g.dx * x->P.g.dy * x->P.g.dz;
+  for (int p = 0; p < 5; p++) {
+    double t = 0.0;
+    for (int b = 0; b < nb; b++) t += h[(size_t)b * 5 + p];
+    totals[p] = t * vol;
+  }
+  return M2CG_OK;
+}
+
+static m2cg_status batch_reserve(m2cg_ctx* x, int64_t n) {
+  if (n <= x->batch_n) return M2CG_OK;
+  for (void* p : x->batch) cudaFree(p);
+  x->batch.clear();
+  // Vm Vp Vs Vsm Vsp (5 each), dir (3), warm (1) doubles; idm idp id iters err ints
+  size_t doubles = (size_t)n * (5 * 5 + 3 + 1);
+  void* d = nullptr;
+  CK(cudaMalloc(&d, doubles * sizeof(double)));
+  x->batch.push_back(d);
+  void* q = nullptr;
+  CK(cudaMalloc(&q, (size_t)n * 5 * sizeof(int32_t)));
+  x->batch.push_back(q);
+  x->batch_n = n;
+  if (!x->batch_scratch) {
+    x->batch_threads = (int64_t)x->nsm * 2 * 128;
+    CK(cudaMalloc(&x->batch_scratch, (size_t)6 * x->path_cap * x->batch_threads * sizeof(double)));
+  }
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_riemann_batch(m2cg_ctx* x, int64_t n, const double* Vm, const int32_t* idm, const double* Vp,
+                               const int32_t* idp, const double* dir, double* Vs, int32_t* id, double* Vsm,
+                               double* Vsp, int32_t* iters, int32_t* err) {
+  if (!x || n < 0 || !Vm || !idm || !Vp || !idp || !dir || !Vs || !id || !Vsm || !Vsp) {
+    set_err("null argument");
+    return M2CG_ERR_INVALID_ARG;
+  }
+  if (n == 0) return M2CG_OK;
+  for (int64_t q = 0; q < n; q++)
+    if (idm[q] < 0 || idm[q] >= x->P.n_mat || idp[q] < 0 || idp[q] >= x->P.n_mat) {
+      set_err("material id out of range at problem %lld", (long long)q);
+      return M2CG_ERR_INVALID_ARG;
+    }
+  m2cg_status st = batch_reserve(x, n);
+  if (st != M2CG_OK) return st;
+  double* D = (double*)x->batch[0];
+  int32_t* I = (int32_t*)x->batch[1];
+  int64_t cap = x->batch_n;
+  double *dVm = D, *dVp = D + 5 * cap, *dVs = D + 10 * cap, *dVsm = D + 15 * cap, *dVsp = D + 20 * cap,
+         *ddir = D + 25 * cap;
+  int32_t *didm = I, *didp = I + cap, *did = I + 2 * cap, *dit = I + 3 * cap, *derr = I + 4 * cap;
+  cudaStream_t s = x->stream;
+  CK(cudaMemcpyAsync(dVm, Vm, n * 5 * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dVp, Vp, n * 5 * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(ddir, dir, n * 3 * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(didm, idm, n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(didp, idp, n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  launch_riemann_batch(s, x->P, x->d_mats, n, dVm, didm, dVp, didp, ddir, dVs, did, dVsm, dVsp, dit, derr,
+                       x->batch_scratch, x->path_cap, (int)(x->batch_threads / 128), 128, nullptr);
+  x->launches++;
+  CK(cudaMemcpyAsync(Vs, dVs, n * 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(Vsm, dVsm, n * 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(Vsp, dVsp, n * 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaMemcpyAsync(id, did, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  if (iters) CK(cudaMemcpyAsync(iters, dit, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  if (err) CK(cudaMemcpyAsync(err, derr, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_flux_batch(m2cg_ctx* x, int64_t n, const int32_t* dir, const double* Vm, const double* Vp,
+                            const int32_t* id, double* F) {
+  if (!x || n < 0 || !dir || !Vm || !Vp || !id || !F) { set_err("null argument"); return M2CG_ERR_INVALID_ARG; }
+  if (n == 0) return M2CG_OK;
+  for (int64_t q = 0; q < n; q++)
+    if (id[q] < 0 || id[q] >= x->P.n_mat || dir[q] < 0 || dir[q] > 2) { set_err("bad id/dir at %lld", (long long)q); return M2CG_ERR_INVALID_ARG; }
+  m2cg_status st = batch_reserve(x, n);
+  if (st != M2CG_OK) return st;
+  double* D = (double*)x->batch[0];
+  int32_t* I = (int32_t*)x->batch[1];
+  int64_t cap = x->batch_n;
+  cudaStream_t s = x->stream;
+  CK(cudaMemcpyAsync(D, Vm, n * 5 * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(D + 5 * cap, Vp, n * 5 * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(I, dir, n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(I + cap, id, n * sizeof(int32_t), cudaMemcpyHostToDevice, s));
+  launch_flux_batch(s, x->P, n, I, D, D + 5 * cap, I + cap, D + 10 * cap);
+  x->launches++;
+  CK(cudaMemcpyAsync(F, D + 10 * cap, n * 5 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_phase_times(m2cg_ctx* x, int32_t n_steps, double ms[8]) {
+  if (!x || !ms || n_steps < 1) return M2CG_ERR_INVALID_ARG;
+  PhaseTimer t;
+  t.s = x->stream;
+  for (int p = 0; p < PH_N; p++) ms[p] = 0.0;
+  g_timer = &t;
+  for (int i = 0; i < n_steps; i++) {
+    t.used = 0;
+    x->launches += enqueue_step(x, 1, 0.0);
+    cudaError_t e = cudaStreamSynchronize(x->stream);
+    if (e != cudaSuccess) { g_timer = nullptr; set_err("%s", cudaGetErrorString(e)); return M2CG_ERR_CUDA; }
+    for (size_t k = 0; k < t.used; k += 2) {
+      float f = 0.f;
+      cudaEventElapsedTime(&f, t.ev[k], t.ev[k + 1]);
+      ms[t.cat[k]] += f;
+    }
+  }
+  g_timer = nullptr;
+  for (cudaEvent_t e : t.ev) cudaEventDestroy(e);
+  CK(cudaGetLastError());
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_sync(m2cg_ctx* x) {
+  if (!x) return M2CG_ERR_INVALID_ARG;
+  CK(cudaStreamSynchronize(x->stream));
+  return M2CG_OK;
+}
+m2cg_status m2cg_event_record(m2cg_ctx* x, int32_t slot) {
+  if (!x || slot < 0 || slot >= 16) return M2CG_ERR_INVALID_ARG;
+  CK(cudaEventRecord(x->ev[slot], x->stream));
+  return M2CG_OK;
+}
+m2cg_status m2cg_event_elapsed(m2cg_ctx* x, int32_t a, int32_t b, float* ms) {
+  if (!x || !ms || a < 0 || a >= 16 || b < 0 || b >= 16) return M2CG_ERR_INVALID_ARG;
+  CK(cudaEventSynchronize(x->ev[b]));
+  CK(cudaEventElapsedTime(ms, x->ev[a], x->ev[b]));
+  return M2CG_OK;
+}
+int64_t m2cg_kernel_launches(m2cg_ctx* x) { return x ? x->launches : 0; }
+
+void* m2cg_host_alloc(size_t bytes) {
+  void* p = nullptr;
+  if (cudaHostAlloc(&p, bytes, cudaHostAllocDefault) != cudaSuccess) { set_err("cudaHostAlloc failed"); return nullptr; }
+  return p;
+}
+void m2cg_host_free(void* p) {
+  if (p) cudaFreeHost(p);
+}
+
+}  // extern "C"

@@ -1,0 +1,275 @@
+// Device-side equations of state, numerical fluxes and slope limiters for the
+// GB300 finite-volume step.  All arithmetic is IEEE binary64.
+//
+// Reference formulas: VarFcnSG.h:64-68, VarFcnNASG.h:55-59, VarFcnMG.h:70-87,
+// VarFcnBase.h:120-298, FluxFcnBase.h:82-123, FluxFcnHLLC.h:51-245,
+// FluxFcnLLF.h:46-185, FluxFcnGenRoe.h:63-221, Reconstructor.h:96-111.
+#pragma once
+#include <cstdint>
+#include <cfloat>
+#include "../../include/m2cg.h"
+
+#define M2CG_DEV __device__ __forceinline__
+
+namespace m2cg {
+
+// Material constants precomputed on the host (one entry per material ID).
+struct DevMat {
+  int type;                      // M2CG_EOS_*
+  int pad;
+  double gam, gam1, Pstiff, gamPs, invgam1;   // SG / NASG (Pstiff = pc for NASG)
+  double b, q;                                // NASG
+  double rho0, s, e0, rho0_c0_c0, G0_half, G0_rho0;  // MG
+  double rhomin, pmin, rhomax, pmax;
+};
+
+struct Mats {
+  DevMat m[M2CG_MAX_MATERIALS];
+};
+
+// ---- equation of state ----------------------------------------------------
+M2CG_DEV double eos_p(const DevMat& M, double rho, double e) {
+  if (M.type == M2CG_EOS_SG) return M.gam1 * rho * e - M.gam * M.Pstiff;
+  if (M.type == M2CG_EOS_NASG) return M.gam1 * (e - M.q) / (1.0 / rho - M.b) - M.gamPs;
+  double eta = 1.0 - M.rho0 / rho;
+  return M.rho0_c0_c0 * eta * (1.0 - M.G0_half * eta) / ((1.0 - M.s * eta) * (1.0 - M.s * eta)) + M.G0_rho0 * (e - M.e0);
+}
+M2CG_DEV double eos_e(const DevMat& M, double rho, double p) {
+  if (M.type == M2CG_EOS_SG) return (p + M.gam * M.Pstiff) / (M.gam1 * rho);
+  if (M.type == M2CG_EOS_NASG) return M.invgam1 * (p + M.gamPs) * (1.0 / rho - M.b) + M.q;
+  double eta = 1.0 - M.rho0 / rho;
+  return (p - M.rho0_c0_c0 * eta * (1.0 - M.G0_half * eta) / ((1.0 - M.s * eta) * (1.0 - M.s * eta))) / M.G0_rho0 + M.e0;
+}
+M2CG_DEV double eos_dpdrho(const DevMat& M, double rho, double e) {
+  if (M.type == M2CG_EOS_SG) return M.gam1 * e;
+  if (M.type == M2CG_EOS_NASG) { double V = 1.0 / rho; return M.gam1 * V * V * (e - M.q) / ((V - M.b) * (V - M.b)); }
+  double eta = 1.0 - M.rho0 / rho;
+  double S = 1.0 - M.s * eta;
+  return M.rho0_c0_c0 * (1.0 + (M.s - 2.0 * M.G0_half) * eta) / (S * S * S) * M.rho0 / (rho * rho);
+}
+M2CG_DEV double eos_Gamma(const DevMat& M, double rho) {
+  if (M.type == M2CG_EOS_SG) return M.gam1;
+  if (M.type == M2CG_EOS_NASG) return M.gam1 / (1.0 - M.b * rho);
+  return M.G0_rho0 / rho;
+}
+// VarFcnBase.h:219-223
+M2CG_DEV double eos_c2(const DevMat& M, double rho, double e) {
+  return eos_dpdrho(M, rho, e) + eos_p(M, rho, e) / rho * eos_Gamma(M, rho);
+}
+// CheckState: true = nonphysical (VarFcnSG.h:96-108, VarFcnNASG.h:73-85, VarFcnBase.h:120-140)
+M2CG_DEV bool eos_bad(const DevMat& M, double rho, double p) {
+  if (!isfinite(rho) || !isfinite(p)) return true;
+  if (M.type == M2CG_EOS_SG || M.type == M2CG_EOS_NASG) return (rho <= 0.0 || p + M.Pstiff <= 0.0);
+  if (rho <= 0.0) return true;
+  double e = eos_e(M, rho, p);
+  return eos_dpdrho(M, rho, e) + p / rho * eos_Gamma(M, rho) <= 0.0;
+}
+M2CG_DEV bool eos_bad5(const DevMat& M, const double* V) {
+  if (!isfinite(V[1]) || !isfinite(V[2]) || !isfinite(V[3])) return true;
+  return eos_bad(M, V[0], V[4]);
+}
+// VarFcnBase.h:262-298 (returns whether it clipped)
+M2CG_DEV bool eos_clip(const DevMat& M, double* V) {
+  bool c = false;
+  if (V[0] < M.rhomin) { V[0] = M.rhomin; c = true; }
+  if (V[4] < M.pmin) { V[4] = M.pmin; c = true; }
+  if (V[0] > M.rhomax) { V[0] = M.rhomax; c = true; }
+  if (V[4] > M.pmax) { V[4] = M.pmax; c = true; }
+  return c;
+}
+// VarFcnBase.h:190-201
+M2CG_DEV void prim_to_cons(const DevMat& M, const double* V, double* U) {
+  U[0] = V[0];
+  U[1] = V[0] * V[1]; U[2] = V[0] * V[2]; U[3] = V[0] * V[3];
+  double e = eos_e(M, V[0], V[4]);
+  U[4] = V[0] * (e + 0.5 * (V[1] * V[1] + V[2] * V[2] + V[3] * V[3]));
+}
+// VarFcnBase.h:173-186
+M2CG_DEV void cons_to_prim(const DevMat& M, const double* U, double* V) {
+  V[0] = U[0];
+  double invRho = 1.0 / U[0];
+  V[1] = U[1] * invRho; V[2] = U[2] * invRho; V[3] = U[3] * invRho;
+  double e = (U[4] - 0.5 * V[0] * (V[1] * V[1] + V[2] * V[2] + V[3] * V[3])) * invRho;
+  V[4] = eos_p(M, V[0], e);
+}
+M2CG_DEV double total_enthalpy(const DevMat& M, const double* V) {
+  double e = eos_e(M, V[0], V[4]);
+  return e + 0.5 * (V[1] * V[1] + V[2] * V[2] + V[3] * V[3]) + V[4] / V[0];
+}
+
+// ---- physical flux (FluxFcnBase.h:82-123) ------------------------------------
+M2CG_DEV void phys_flux(const DevMat& M, int dir, const double* V, double* F) {
+  double H = total_enthalpy(M, V);
+  double vn = V[1 + dir];
+  double rhou = V[0] * vn;
+  F[0] = rhou;
+  F[1] = rhou * V[1]; F[2] = rhou * V[2]; F[3] = rhou * V[3];
+  F[1 + dir] = rhou * vn + V[4];
+  F[4] = rhou * H;
+}
+
+M2CG_DEV double avg(double w1, double f1, double w2, double f2) { return (w1 * f1 + w2 * f2) / (w1 + w2); }
+
+// Generalized Roe-averaged state of Hu et al. (FluxFcnHLLC.h:57-126)
+struct RoeHat {
+  double rho_hat, srm, srp, em, ep, e_hat, c_hat, c2_hat, dpdrho_hat, Gamma_hat, p_over_rho_hat;
+};
+M2CG_DEV void roe_hat(const DevMat& M, int dir, const double* Vm, const double* Vp, RoeHat& r) {
+  const double eps = 1e-10;
+  r.rho_hat = sqrt(Vm[0] * Vp[0]);
+  r.srm = sqrt(Vm[0]);
+  r.srp = sqrt(Vp[0]);
+  double drho = Vp[0] - Vm[0];
+  double dp = Vp[4] - Vm[4];
+  double diff = (Vp[1 + dir] - Vm[1 + dir]) / (r.srm + r.srp);
+  r.p_over_rho_hat = avg(r.srm, Vm[4] / Vm[0], r.srp, Vp[4] / Vp[0]) + 0.5 * diff * diff;
+  r.em = eos_e(M, Vm[0], Vm[4]);
+  r.ep = eos_e(M, Vp[0], Vp[4]);
+  double de = r.ep - r.em;
+  r.e_hat = avg(r.srm, r.em, r.srp, r.ep);
+  double w_rho = drho * drho / (r.rho_hat * r.rho_hat);
+  double w_e = de * de / (r.e_hat * r.e_hat);
+  double denom = w_rho + w_e + eps;
+  double dpdrho_avg = avg(r.srm, eos_dpdrho(M, Vm[0], r.em), r.srp, eos_dpdrho(M, Vp[0], r.ep));
+  double Gamma_avg = avg(r.srm, eos_Gamma(M, Vm[0]), r.srp, eos_Gamma(M, Vp[0]));
+  double t1 = (w_e + eps) * dpdrho_avg;
+  double t2 = (dp - Gamma_avg * r.rho_hat * de) * drho / (r.rho_hat * r.rho_hat);
+  r.dpdrho_hat = (t1 + t2) / denom;
+  double g1 = (w_rho + eps) * Gamma_avg;
+  double g2 = (dp - dpdrho_avg * drho) * de / (r.rho_hat * r.e_hat * r.e_hat);
+  r.Gamma_hat = (g1 + g2) / denom;
+  r.c2_hat = r.dpdrho_hat + r.Gamma_hat * r.p_over_rho_hat;
+  if (r.c2_hat <= 0) { r.c_hat = eps; r.c2_hat = eps * eps; }
+  else r.c_hat = sqrt(r.c2_hat);
+}
+
+// FluxFcnHLLC.h:158-192
+M2CG_DEV void hllc_fstar(const DevMat& M, int dir, const double* V, double S, double Sstar, double* F) {
+  double velo = V[1 + dir];
+  double rhostar = V[0] * (S - velo) / (S - Sstar);
+  double U[5];
+  prim_to_cons(M, V, U);
+  double Us[5];
+  Us[0] = 1.0; Us[1] = V[1]; Us[2] = V[2]; Us[3] = V[3];
+  Us[1 + dir] = Sstar;
+  Us[4] = U[4] / V[0] + (Sstar - velo) * (Sstar + V[4] / (V[0] * (S - velo)));
+  phys_flux(M, dir, V, F);
+#pragma unroll
+  for (int i = 0; i < 5; i++) F[i] += S * (Us[i] * rhostar - U[i]);
+}
+
+// FluxFcnHLLC.h:196-245.  Returns false if c^2 < 0 on either side.
+M2CG_DEV bool flux_hllc(const DevMat& M, int dir, const double* Vm, const double* Vp, double* F) {
+  RoeHat r;
+  roe_hat(M, dir, Vm, Vp, r);
+  double cm = eos_c2(M, Vm[0], r.em);
+  double cp = eos_c2(M, Vp[0], r.ep);
+  bool ok = !(cm < 0.0) && !(cp < 0.0);
+  cm = sqrt(fmax(cm, 0.0));
+  cp = sqrt(fmax(cp, 0.0));
+  double vm = Vm[1 + dir], vp = Vp[1 + dir];
+  double vh = avg(r.srm, vm, r.srp, vp);
+  double Sm = fmin(vm - cm, vh - r.c_hat);
+  double Sp = fmax(vp + cp, vh + r.c_hat);
+  if (0.0 <= Sm) phys_flux(M, dir, Vm, F);
+  else if (0.0 >= Sp) phys_flux(M, dir, Vp, F);
+  else {
+    double Sstar = (Vp[4] - Vm[4] + Vm[0] * vm * (Sm - vm) - Vp[0] * vp * (Sp - vp)) /
+                   (Vm[0] * (Sm - vm) - Vp[0] * (Sp - vp));
+    if (Sstar >= 0.0) hllc_fstar(M, dir, Vm, Sm, Sstar, F);
+    else hllc_fstar(M, dir, Vp, Sp, Sstar, F);
+  }
+  return ok;
+}
+
+// FluxFcnLLF.h:46-111 and 118-185 (two materials)
+M2CG_DEV bool flux_llf2(const DevMat& Mm, const DevMat& Mp, int dir, const double* Vm, const double* Vp, double* F) {
+  double em = eos_e(Mm, Vm[0], Vm[4]);
+  double ep = eos_e(Mp, Vp[0], Vp[4]);
+  double cm = eos_c2(Mm, Vm[0], em);
+  double cp = eos_c2(Mp, Vp[0], ep);
+  bool ok = !(cm < 0.0) && !(cp < 0.0);
+  cm = sqrt(fmax(cm, 0.0));
+  cp = sqrt(fmax(cp, 0.0));
+  double a = fmax(fabs(Vm[1 + dir]) + cm, fabs(Vp[1 + dir]) + cp);
+  double fm[5], fp[5], Um[5], Up[5];
+  phys_flux(Mm, dir, Vm, fm);
+  phys_flux(Mp, dir, Vp, fp);
+  prim_to_cons(Mm, Vm, Um);
+  prim_to_cons(Mp, Vp, Up);
+#pragma unroll
+  for (int i = 0; i < 5; i++) F[i] = 0.5 * ((fm[i] + fp[i]) - a * (Up[i] - Um[i]));
+  return ok;
+}
+
+// FluxFcnGenRoe.h:63-221 with the eigenvectors of FluxFcnBase.h:154-176 (F),
+// 203-225 (G), 252-274 (H).
+M2CG_DEV bool flux_genroe(const DevMat& M, int dir, const double* Vm, const double* Vp, double del, double* F) {
+  double srm = sqrt(Vm[0]), srp = sqrt(Vp[0]);
+  double rho_hat = sqrt(Vm[0] * Vp[0]);
+  double vel[3];
+#pragma unroll
+  for (int m = 0; m < 3; m++) vel[m] = avg(srm, Vm[1 + m], srp, Vp[1 + m]);
+  double H_hat = avg(srm, total_enthalpy(M, Vm), srp, total_enthalpy(M, Vp));
+  double dvel[3] = {Vp[1] - Vm[1], Vp[2] - Vm[2], Vp[3] - Vm[3]};
+  double dp = Vp[4] - Vm[4], drho = Vp[0] - Vm[0];
+  RoeHat r;
+  roe_hat(M, dir, Vm, Vp, r);
+  double c = r.c_hat, c2 = r.c2_hat;
+  double vn = vel[dir];
+  double vel2 = vel[0] * vel[0] + vel[1] * vel[1] + vel[2] * vel[2];
+  double e_term = r.e_hat + 0.5 * vel2 - r.dpdrho_hat / r.Gamma_hat;
+  double lam[5] = {vn - c, vn, vn, vn, vn + c};
+  double a[5];
+  a[0] = (dp - rho_hat * c * dvel[dir]) / (2 * c2);
+  a[4] = (dp + rho_hat * c * dvel[dir]) / (2 * c2);
+#pragma unroll
+  for (int p = 1; p <= 3; p++) a[p] = (p - 1 == dir) ? (-dp / c2 + drho) : rho_hat * dvel[p - 1];
+  double tol = lam[0];
+#pragma unroll
+  for (int i = 1; i < 5; i++) if (fabs(lam[i]) > tol) tol = fabs(lam[i]);
+  tol *= del;
+#pragma unroll
+  for (int i = 0; i < 5; i++) if (fabs(lam[i]) < tol) lam[i] = (lam[i] * lam[i] + tol * tol) / (2 * tol);
+  double fm[5], fp[5];
+  phys_flux(M, dir, Vm, fm);
+  phys_flux(M, dir, Vp, fp);
+#pragma unroll
+  for (int i = 0; i < 5; i++) F[i] = 0.5 * (fm[i] + fp[i]);
+  // subtract 0.5|lam_p| a_p r_p in the order p = 0..4 for every component
+#pragma unroll
+  for (int p = 0; p < 5; p++) {
+    double coef = 0.5 * fabs(lam[p]) * a[p];
+    double R[5] = {0, 0, 0, 0, 0};
+    if (p == 0 || p == 4) {
+      R[0] = 1; R[1] = vel[0]; R[2] = vel[1]; R[3] = vel[2];
+      R[1 + dir] = (p == 0) ? vn - c : vn + c;
+      R[4] = (p == 0) ? H_hat - vn * c : H_hat + vn * c;
+    } else if (p - 1 == dir) {
+      R[0] = 1; R[1] = vel[0]; R[2] = vel[1]; R[3] = vel[2]; R[4] = e_term;
+    } else {
+      R[p] = 1; R[4] = vel[p - 1];
+    }
+#pragma unroll
+    for (int i = 0; i < 5; i++) F[i] -= coef * R[i];
+  }
+  return true;
+}
+
+// ---- slope limiters (Reconstructor.h:96-111) ------------------------------------
+M2CG_DEV double gen_minmod(double alpha, double dq0, double dq1) {
+  // uniform mesh: A = B = 1, so B/(A+1) = 0.5
+  if (dq0 < 0.0 && dq1 < 0.0) return fmax(alpha * dq0, fmax(0.5 * (dq0 + dq1), alpha * dq1));
+  if (dq0 > 0.0 && dq1 > 0.0) return fmin(alpha * dq0, fmin(0.5 * (dq0 + dq1), alpha * dq1));
+  return 0.0;
+}
+// k = 2 on a uniform mesh (Reconstructor.cpp:103-121 with A = B = 1)
+M2CG_DEV double van_albada(double dq0, double dq1) {
+  double pr = dq0 * dq1;
+  if (pr <= 0.0) return 0.0;
+  if (fabs(pr) < 1e-16) return 0.0;
+  double a = dq0 * dq0, b = dq1 * dq1;
+  return (dq1 * a + dq0 * b) / (a + b);
+}
+
+}  // namespace m2cg

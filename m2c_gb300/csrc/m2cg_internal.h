@@ -1,0 +1,93 @@
+// Internal definitions shared by the kernels and the host API of libm2cg.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+#include "m2cg_device.cuh"
+#include "m2cg_riemann.cuh"
+
+namespace m2cg {
+
+// Ghosted grid: one ghost layer on every side (the reference's DMDA stencil
+// width for V, ID and phi; SpaceVariable.cpp:58-70).  Real cell (i,j,k) with
+// i in [0,nx) sits at linear index ((k+1)*py + (j+1))*px + (i+1).
+struct Grid {
+  int nx, ny, nz;
+  int px, py, pz;
+  int64_t sy, sz, ntot;  // sx = 1
+  double dx, dy, dz;
+  M2CG_DEV int64_t at(int i, int j, int k) const { return ((int64_t)(k + 1) * py + (j + 1)) * px + (i + 1); }
+};
+
+// Device counter slots (int64).
+enum {
+  CNT_IFACE = 0, CNT_RERR, CNT_RITER, CNT_RSOLVE, CNT_CLIPCELL, CNT_CLIPFACE, CNT_BAD, CNT_SWEPT, CNT_UNRES,
+  CNT_IF_OVERFLOW, CNT_PATH_CAPPED, CNT_SWEPT_OVERFLOW, CNT_BADID, CNT_N
+};
+
+// Scalars that live on the device for the whole run (no host round trip per step).
+struct DevScalars {
+  unsigned long long min_dx_over_lambda;  // bit pattern of a positive double (atomicMin)
+  double dt, cfl, time;
+  int active;       // 0 once MaxTime has been reached
+  int pad;
+  long long steps;
+};
+
+struct Params {
+  Grid g;
+  Mats mats;
+  int n_mat;
+  int flux, rec_type, limiter, slope_zero;
+  int mp_flux, mp_recon, mp_phasechange, mp_pcdir;
+  double minmod_coeff, roe_delta;
+  int bc[6];
+  double inlet[5], inlet2[5];
+  int n_ls, ls_matid;
+  int ls_bc[6];
+  RiemannPrm rp;
+  double area[3];
+  double inv_negvol;
+  double fd3l[3][4], fd3r[3][4];
+  double cfl, timestep, max_time;
+  int ts_type;
+};
+
+// A primitive state set: rho, u, v, w, p, phi (SoA, ghosted).
+struct StateSet {
+  double* q[6];
+};
+
+// Interface-face work list (compacted each step).
+struct IfaceList {
+  int64_t* face;       // plus-cell index * 4 + direction
+  double* lf1[5];      // flux contribution to the minus cell
+  double* lf2[5];      // flux contribution to the plus cell
+  double* vsm[5];      // stored star states (first stage only)
+  double* vsp[5];
+  int32_t* err;        // 0 ok / 1 failed: solution not stored (SpaceOperator.cpp:1661)
+  int32_t* iters;
+  int32_t* slot[3];    // per-cell slot of the face at the cell's minus side in each direction
+  unsigned long long* count;
+  int64_t cap;
+};
+
+struct StageArgs {
+  // residual input (neighbors) and own-cell inputs of the stage combination
+  StateSet in;          // V and phi of the stage input (residual evaluated here)
+  StateSet out;         // output V and phi
+  const double* phi_lsin;   // phi whose gradient drives the level-set residual (== in.q[5])
+  const double* phi_own;    // phi combined with the stage weights (own cell)
+  const double* phi_tmp;    // phi at t^n for the sign test (last stage only)
+  double* Un[5];        // conservative state at t^n
+  double* Us[5];        // conservative stage state (U1 / U2)
+  int stage;            // 0, 1, 2
+  int last;             // 1 on the final stage
+  int store_un;         // write Un (first stage)
+  double a_own, b_un, c_dt;   // U = a*Us + b*Un + c*dt*R  (first stage: a=0, b=1, c=1)
+  double la, lb, lc;          // phi = la*phi_own_other + lb*phi_n + lc*dt*R (see kernel)
+  int ls_use_updated_v;       // forward Euler: level set advected with the updated velocity
+  double* R[5];               // residual output (residual-only mode)
+  int residual_only;
+};
+
+}  // namespace m2cg

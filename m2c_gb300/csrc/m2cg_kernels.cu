@@ -1,0 +1,769 @@
+// Stage kernels of the GB300 finite-volume step: reconstruction, same-material
+// face fluxes, residual gather + Runge-Kutta stage update + level-set update,
+// boundary conditions, the CFL reduction and the end-of-step material update.
+//
+// One thread per cell (or per face-owning cell); every face flux is evaluated
+// exactly once.  All arithmetic is binary64; the FP64 pipe, not HBM, bounds
+// these kernels on GB300.
+#include "m2cg_internal.h"
+
+namespace m2cg {
+
+__device__ __forceinline__ void atomic_inc(unsigned long long* c, unsigned long long v = 1ull) {
+  atomicAdd(c, v);
+}
+
+// Linear index of a real cell from a flat thread id over nx*ny*nz.
+__device__ __forceinline__ bool real_cell(const Grid& g, int64_t t, int& i, int& j, int& k) {
+  int64_t n = (int64_t)g.nx * g.ny * g.nz;
+  if (t >= n) return false;
+  int64_t nxy = (int64_t)g.nx * g.ny;
+  k = (int)(t / nxy);
+  int64_t r = t - (int64_t)k * nxy;
+  j = (int)(r / g.nx);
+  i = (int)(r - (int64_t)j * g.nx);
+  return true;
+}
+
+// ---------------------------------------------------------------------------
+// K1: MUSCL reconstruction of the six face states of every real cell
+// (Reconstructor.cpp:426-782) followed by CheckReconstructedStates
+// (SpaceOperator.cpp:2446-2484).  fs[f*5+p]: f = vl, vr, vb, vt, vk, vf.
+__global__ void k_reconstruct(Params P, StateSet S, const int32_t* __restrict__ id, double* const* fs,
+                              unsigned long long* cnt) {
+  int i, j, k;
+  if (!real_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
+  const Grid& g = P.g;
+  int64_t c = g.at(i, j, k);
+  double q[5];
+#pragma unroll
+  for (int p = 0; p < 5; p++) q[p] = S.q[p][c];
+  double face[6][5];
+  if (P.rec_type == M2CG_REC_CONSTANT) {
+#pragma unroll
+    for (int f = 0; f < 6; f++)
+#pragma unroll
+      for (int p = 0; p < 5; p++) face[f][p] = q[p];
+  } else {
+    const int64_t st[3] = {1, g.sy, g.sz};
+    int myid = id[c];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      bool zero = P.slope_zero && (id[c - st[d]] != myid || id[c + st[d]] != myid);
+#pragma unroll
+      for (int p = 0; p < 5; p++) {
+        double dq0 = q[p] - S.q[p][c - st[d]];
+        double dq1 = S.q[p][c + st[d]] - q[p];
+        double s;
+        if (P.limiter == M2CG_LIM_VANALBADA) s = van_albada(dq0, dq1);
+        else if (P.limiter == M2CG_LIM_GENERALIZED_MINMOD) s = gen_minmod(P.minmod_coeff, dq0, dq1);
+        else s = 0.5 * (dq0 + dq1);
+        if (zero) s = 0.0;
+        face[2 * d][p] = q[p] - 0.5 * s;
+        face[2 * d + 1][p] = q[p] + 0.5 * s;
+      }
+    }
+    // Reconstructor.cpp:722-778: the first nonphysical face state reverts to the cell value
+    const DevMat& M = P.mats.m[myid];
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+      if (eos_bad5(M, face[f])) {
+#pragma unroll
+        for (int p = 0; p < 5; p++) face[f][p] = q[p];
+        break;
+      }
+    }
+  }
+  // CheckReconstructedStates: clip -> revert to the cell value
+  const DevMat& M = P.mats.m[id[c]];
+  int nclip = 0, nbad = 0;
+#pragma unroll
+  for (int f = 0; f < 6; f++) {
+    double t[5] = {face[f][0], face[f][1], face[f][2], face[f][3], face[f][4]};
+    if (eos_clip(M, t)) {
+#pragma unroll
+      for (int p = 0; p < 5; p++) face[f][p] = q[p];
+      nclip++;
+    }
+    nbad += eos_bad5(M, face[f]);
+  }
+  if (nclip) atomic_inc(&cnt[CNT_CLIPFACE], nclip);
+  if (nbad) atomic_inc(&cnt[CNT_BAD], nbad);
+#pragma unroll
+  for (int f = 0; f < 6; f++)
+#pragma unroll
+    for (int p = 0; p < 5; p++) fs[f * 5 + p][c] = face[f][p];
+}
+
+// Face-ghost cells: position and image (SpaceOperator.cpp:493-519).
+__device__ __forceinline__ bool ghost_face_cell(const Grid& g, int64_t t, int& side, int& i, int& j, int& k,
+                                                int& ii, int& jj, int& kk) {
+  int64_t nyz = (int64_t)g.ny * g.nz, nxz = (int64_t)g.nx * g.nz, nxy = (int64_t)g.nx * g.ny;
+  if (t < 2 * nyz) {
+    side = (int)(t / nyz); int64_t r = t % nyz;
+    k = (int)(r / g.ny); j = (int)(r % g.ny);
+    i = side == 0 ? -1 : g.nx;
+    ii = side == 0 ? 0 : g.nx - 1; jj = j; kk = k;
+    return true;
+  }
+  t -= 2 * nyz;
+  if (t < 2 * nxz) {
+    side = 2 + (int)(t / nxz); int64_t r = t % nxz;
+    k = (int)(r / g.nx); i = (int)(r % g.nx);
+    j = side == 2 ? -1 : g.ny;
+    jj = side == 2 ? 0 : g.ny - 1; ii = i; kk = k;
+    return true;
+  }
+  t -= 2 * nxz;
+  if (t < 2 * nxy) {
+    side = 4 + (int)(t / nxy); int64_t r = t % nxy;
+    j = (int)(r / g.nx); i = (int)(r % g.nx);
+    k = side == 4 ? -1 : g.nz;
+    kk = side == 4 ? 0 : g.nz - 1; ii = i; jj = j;
+    return true;
+  }
+  return false;
+}
+
+// K1b: face states of the face-ghost cells by boundary condition
+// (Reconstructor.cpp:807-889), then the boundary branch of
+// CheckReconstructedStates (SpaceOperator.cpp:2486-2535).
+__global__ void k_reconstruct_ghosts(Params P, StateSet S, const int32_t* __restrict__ id, double* const* fs,
+                                     unsigned long long* cnt) {
+  int side, i, j, k, ii, jj, kk;
+  if (!ghost_face_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, side, i, j, k, ii, jj, kk)) return;
+  const Grid& g = P.g;
+  int64_t c = g.at(i, j, k), im = g.at(ii, jj, kk);
+  int inward = side ^ 1, src = side;
+  int bc = P.bc[side];
+  double t[5];
+  if (bc == M2CG_BC_INLET || bc == M2CG_BC_INLET2) {
+#pragma unroll
+    for (int p = 0; p < 5; p++) t[p] = S.q[p][c];
+  } else {
+#pragma unroll
+    for (int p = 0; p < 5; p++) t[p] = fs[src * 5 + p][im];
+    if (bc == M2CG_BC_SYMMETRY || bc == M2CG_BC_SLIPWALL) t[1 + side / 2] *= -1.0;
+    else if (bc == M2CG_BC_STICKWALL) { t[1] *= -1.0; t[2] *= -1.0; t[3] *= -1.0; }
+  }
+  const DevMat& M = P.mats.m[id[c]];
+  double u[5] = {t[0], t[1], t[2], t[3], t[4]};
+  if (eos_clip(M, u)) {
+#pragma unroll
+    for (int p = 0; p < 5; p++) t[p] = S.q[p][c];
+    atomic_inc(&cnt[CNT_CLIPFACE]);
+  }
+  if (eos_bad5(M, t)) atomic_inc(&cnt[CNT_BAD]);
+#pragma unroll
+  for (int p = 0; p < 5; p++) fs[inward * 5 + p][c] = t[p];
+}
+
+__device__ __forceinline__ bool num_flux(const Params& P, int dir, const double* Vm, const double* Vp, int id, double* F) {
+  const DevMat& M = P.mats.m[id];
+  if (P.flux == M2CG_FLUX_HLLC) return flux_hllc(M, dir, Vm, Vp, F);
+  if (P.flux == M2CG_FLUX_LLF) return flux_llf2(M, M, dir, Vm, Vp, F);
+  return flux_genroe(M, dir, Vm, Vp, P.roe_delta, F);
+}
+
+// ---------------------------------------------------------------------------
+// K2: numerical flux of every same-material face (SpaceOperator.cpp:1692-1701,
+// 1852-1861, 2011-2020).  The thread of cell c owns the faces at its minus side.
+__global__ void k_face_flux(Params P, const int32_t* __restrict__ id, double* const* fs, double* const* F,
+                            unsigned long long* cnt) {
+  const Grid& g = P.g;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t ex = g.nx + 1, ey = g.ny + 1;
+  int64_t n = ex * ey * (g.nz + 1);
+  if (t >= n) return;
+  int k = (int)(t / (ex * ey));
+  int64_t r = t - (int64_t)k * ex * ey;
+  int j = (int)(r / ex), i = (int)(r - (int64_t)j * ex);
+  int64_t c = g.at(i, j, k);
+  const int64_t st[3] = {1, g.sy, g.sz};
+  bool has[3] = {j < g.ny && k < g.nz, i < g.nx && k < g.nz, i < g.nx && j < g.ny};
+  int myid = id[c];
+  int bad = 0;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    if (!has[d]) continue;
+    int64_t m = c - st[d];
+    if (id[m] != myid) continue;  // material interface: exact Riemann kernel
+    double Vm[5], Vp[5], Fl[5];
+#pragma unroll
+    for (int p = 0; p < 5; p++) { Vm[p] = fs[(2 * d + 1) * 5 + p][m]; Vp[p] = fs[(2 * d) * 5 + p][c]; }
+    bad += !num_flux(P, d, Vm, Vp, myid, Fl);
+#pragma unroll
+    for (int p = 0; p < 5; p++) F[d * 5 + p][c] = Fl[p];
+  }
+  if (bad) atomic_inc(&cnt[CNT_BAD], bad);
+}
+
+// ---------------------------------------------------------------------------
+// Level-set residual at one cell: LevelSetOperator.cpp:834-852 with the FD3
+// coefficients of GradientCalculatorFD3.cpp:300-453 (uniform mesh).
+__device__ __forceinline__ double ls_residual(const Params& P, const double* __restrict__ phi, int64_t c, int i, int j,
+                                              int k, const double vel[3]) {
+  const Grid& g = P.g;
+  const int64_t st[3] = {1, g.sy, g.sz};
+  const int pos[3] = {i, j, k};
+  const int n[3] = {g.nx, g.ny, g.nz};
+  const double h[3] = {g.dx, g.dy, g.dz};
+  double term[3];
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    int64_t s = st[d];
+    double gr;
+    if (vel[d] >= 0) {
+      if (pos[d] - 2 >= -1)
+        gr = P.fd3l[d][0] * phi[c - 2 * s] + P.fd3l[d][1] * phi[c - s] + P.fd3l[d][2] * phi[c] + P.fd3l[d][3] * phi[c + s];
+      else
+        gr = (phi[c] - phi[c - s]) / h[d];
+    } else {
+      if (pos[d] + 2 <= n[d]) {
+        // the reference's right-biased y coefficients are 3rd order only when
+        // i < NY-1 (GradientCalculatorFD3.cpp:409 tests i, not j)
+        bool third = (d == 1) ? (i < g.ny - 1) : (pos[d] < n[d] - 1);
+        if (third)
+          gr = P.fd3r[d][0] * phi[c - s] + P.fd3r[d][1] * phi[c] + P.fd3r[d][2] * phi[c + s] + P.fd3r[d][3] * phi[c + 2 * s];
+        else
+          gr = 0.0 * phi[c - s] + (-1.0 / h[d]) * phi[c] + (1.0 / h[d]) * phi[c + s] + 0.0 * phi[c + 2 * s];
+      } else
+        gr = (phi[c + s] - phi[c]) / h[d];
+    }
+    term[d] = gr * vel[d];
+  }
+  return (term[0] + term[1] + term[2]) * -1.0;
+}
+
+// ---------------------------------------------------------------------------
+// K3: residual gather in the reference's accumulation order
+// (SpaceOperator.cpp:1703-1705, 1863-1865, 2022-2024, then r /= -vol at
+// 2628-2632), the Runge-Kutta stage combination with clipping
+// (TimeIntegrator.cpp:355-369, 409-417, 565-579, 617-631, 667-676), the
+// level-set stage update and, on the final stage, the sign-change detection of
+// MultiPhaseOperator::UpdateMaterialIDByLevelSet (MultiPhaseOperator.cpp:177-222).
+__global__ void k_update(Params P, StageArgs A, const int32_t* __restrict__ id, int32_t* __restrict__ id_new,
+                         double* const* F, IfaceList L, const DevScalars* __restrict__ sc,
+                         int64_t* __restrict__ swept, unsigned long long* swept_count, int64_t swept_cap,
+                         unsigned long long* cnt) {
+  int i, j, k;
+  if (!real_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
+  if (!sc->active && !A.residual_only) return;
+  const Grid& g = P.g;
+  int64_t c = g.at(i, j, k);
+  const int64_t st[3] = {1, g.sy, g.sz};
+  int myid = id[c];
+  // f = sum_d (F(c + 1/2 e_d) - F(c - 1/2 e_d)) * A_d.  The reference accumulates
+  // -F_minus*A (x, y, z) then +F_plus*A (SpaceOperator.cpp:1703-1705, 1863-1865,
+  // 2022-2024); differencing first gives the same value to rounding and an exact
+  // zero wherever the two fluxes of a direction are equal, as the reference does
+  // for a uniform flux.
+  double f[5] = {0, 0, 0, 0, 0};
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    int64_t m = c - st[d], pc = c + st[d];
+    const double a = P.area[d];
+    double fm[5], fp[5];
+    if (id[m] != myid) {
+      int s = L.slot[d][c];
+#pragma unroll
+      for (int p = 0; p < 5; p++) fm[p] = L.lf2[p][s];
+    } else {
+#pragma unroll
+      for (int p = 0; p < 5; p++) fm[p] = F[d * 5 + p][c];
+    }
+    if (id[pc] != myid) {
+      int s = L.slot[d][pc];
+#pragma unroll
+      for (int p = 0; p < 5; p++) fp[p] = L.lf1[p][s];
+    } else {
+#pragma unroll
+      for (int p = 0; p < 5; p++) fp[p] = F[d * 5 + p][pc];
+    }
+#pragma unroll
+    for (int p = 0; p < 5; p++) f[p] += (fp[p] - fm[p]) * a;
+  }
+  double R[5];
+#pragma unroll
+  for (int p = 0; p < 5; p++) R[p] = f[p] * P.inv_negvol;
+  if (A.residual_only) {
+#pragma unroll
+    for (int p = 0; p < 5; p++) A.R[p][c] = R[p];
+    return;
+  }
+  const double dt = sc->dt;
+  const DevMat& M = P.mats.m[myid];
+  double U[5];
+  if (A.stage == 0) {
+    double Vn[5], Un[5];
+#pragma unroll
+    for (int p = 0; p < 5; p++) Vn[p] = A.in.q[p][c];
+    prim_to_cons(M, Vn, Un);
+    if (A.store_un) {
+#pragma unroll
+      for (int p = 0; p < 5; p++) A.Un[p][c] = Un[p];
+    }
+#pragma unroll
+    for (int p = 0; p < 5; p++) U[p] = Un[p] + dt * R[p];
+  } else {
+    const double cdt = A.c_dt * dt;
+#pragma unroll
+    for (int p = 0; p < 5; p++) U[p] = (A.a_own * A.Us[p][c] + A.b_un * A.Un[p][c]) + cdt * R[p];
+  }
+  double V[5];
+  cons_to_prim(M, U, V);
+  bool clipped = eos_clip(M, V);
+  if (clipped) atomic_inc(&cnt[CNT_CLIPCELL]);
+  if (eos_bad5(M, V)) atomic_inc(&cnt[CNT_BAD]);
+  if (!A.last) {
+    if (clipped) prim_to_cons(M, V, U);
+#pragma unroll
+    for (int p = 0; p < 5; p++) A.Us[p][c] = U[p];
+  }
+#pragma unroll
+  for (int p = 0; p < 5; p++) A.out.q[p][c] = V[p];
+  // level set
+  if (P.n_ls > 0) {
+    double vel[3];
+    if (A.ls_use_updated_v) { vel[0] = V[1]; vel[1] = V[2]; vel[2] = V[3]; }
+    else { vel[0] = A.in.q[1][c]; vel[1] = A.in.q[2][c]; vel[2] = A.in.q[3][c]; }
+    double rls = ls_residual(P, A.phi_lsin, c, i, j, k, vel);
+    double ph;
+    double phin = A.phi_tmp[c];
+    if (A.stage == 0) ph = A.phi_own[c] + dt * rls;
+    else ph = (A.la * A.phi_own[c] + A.lb * phin) + (A.lc * dt) * rls;
+    A.out.q[5][c] = ph;
+    if (A.last) {
+      // sign change (MultiPhaseOperator.cpp:190-222) -> new ID or "remaining" tag (negative)
+      int nid = myid;
+      if (!(ph * phin > 0.0)) {
+        if (ph < 0) nid = P.ls_matid;
+        else nid = -1 - myid;  // resolved from the neighbors after this kernel
+        unsigned long long s = atomicAdd(swept_count, 1ull);
+        if ((int64_t)s < swept_cap) swept[s] = c;
+        else atomic_inc(&cnt[CNT_SWEPT_OVERFLOW]);
+      }
+      id_new[c] = nid;
+    }
+  } else if (A.last) {
+    id_new[c] = myid;
+  }
+}
+
+// Level-set residual only (LevelSetOperator::ComputeResidual).
+__global__ void k_ls_residual(Params P, StateSet S, double* __restrict__ out) {
+  int i, j, k;
+  if (!real_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
+  int64_t c = P.g.at(i, j, k);
+  double vel[3] = {S.q[1][c], S.q[2][c], S.q[3][c]};
+  out[c] = ls_residual(P, S.q[5], c, i, j, k, vel);
+}
+
+// ---------------------------------------------------------------------------
+// Boundary conditions on the face-ghost cells: SpaceOperator.cpp:738-821 (V),
+// LevelSetOperator.cpp:408-508 (phi), MultiPhaseOperator.cpp:919-942 (ID).
+__global__ void k_bc(Params P, StateSet S, int do_v, int do_phi, int32_t* id, const DevScalars* sc) {
+  int side, i, j, k, ii, jj, kk;
+  if (!ghost_face_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, side, i, j, k, ii, jj, kk)) return;
+  if (sc && !sc->active) return;
+  const Grid& g = P.g;
+  int64_t c = g.at(i, j, k), im = g.at(ii, jj, kk);
+  if (do_v) {
+    int bc = P.bc[side];
+    if (bc == M2CG_BC_INLET) {
+#pragma unroll
+      for (int p = 0; p < 5; p++) S.q[p][c] = P.inlet[p];
+    } else if (bc == M2CG_BC_INLET2) {
+#pragma unroll
+      for (int p = 0; p < 5; p++) S.q[p][c] = P.inlet2[p];
+    } else {
+      double t[5];
+#pragma unroll
+      for (int p = 0; p < 5; p++) t[p] = S.q[p][im];
+      if (bc == M2CG_BC_SYMMETRY || bc == M2CG_BC_SLIPWALL) t[1 + side / 2] *= -1.0;
+      else if (bc == M2CG_BC_STICKWALL) { t[1] = -1.0 * t[1]; t[2] = -1.0 * t[2]; t[3] = -1.0 * t[3]; }
+#pragma unroll
+      for (int p = 0; p < 5; p++) S.q[p][c] = t[p];
+    }
+  }
+  if (do_phi && P.n_ls > 0) {
+    double* phi = S.q[5];
+    int bc = P.ls_bc[side];
+    if (bc == M2CG_LSBC_ZERO_NEUMANN) phi[c] = phi[im];
+    else {
+      int d = side / 2, sgn = (side % 2 == 0) ? 1 : -1;
+      int pos[3] = {i, j, k};
+      int n[3] = {g.nx, g.ny, g.nz};
+      const double h[3] = {g.dx, g.dy, g.dz};
+      const int64_t st[3] = {1, g.sy, g.sz};
+      bool ok = (sgn > 0) ? (pos[d] + 2 < n[d]) : (pos[d] - 2 >= 0);
+      double v;
+      if (ok) {
+        double r = pos[d] * h[d], r1 = (pos[d] + sgn) * h[d], r2 = (pos[d] + 2 * sgn) * h[d];
+        double f1 = phi[c + sgn * st[d]], f2 = phi[c + 2 * sgn * st[d]];
+        v = f1 + (f2 - f1) / (r2 - r1) * (r - r1);
+      } else v = phi[im];
+      if (bc == M2CG_LSBC_NON_NEGATIVE) v = fmax(-0.5 * h[d], v);
+      phi[c] = v;
+    }
+  }
+  if (id) id[c] = id[im];
+}
+
+// ---------------------------------------------------------------------------
+// CFL time step: FindExtremeValuesOfFlowVariables + ComputeTimeStepSize
+// (SpaceOperator.cpp:1223-1330).  Warp-shuffle min, then one atomicMin per block
+// on the bit pattern of the positive minimum.
+__global__ void k_dt_reduce(Params P, StateSet S, const int32_t* __restrict__ id, DevScalars* sc) {
+  int i, j, k;
+  double m = DBL_MAX;
+  if (real_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) {
+    const Grid& g = P.g;
+    int64_t c = g.at(i, j, k);
+    const DevMat& M = P.mats.m[id[c]];
+    double rho = S.q[0][c], p = S.q[4][c];
+    double cc = sqrt(fmax(eos_c2(M, rho, eos_e(M, rho, p)), 0.0));
+    if (g.nx > 1) m = fmin(m, g.dx / (fabs(S.q[1][c]) + cc));
+    if (g.ny > 1) m = fmin(m, g.dy / (fabs(S.q[2][c]) + cc));
+    if (g.nz > 1) m = fmin(m, g.dz / (fabs(S.q[3][c]) + cc));
+  }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+  __shared__ double wmin[32];
+  int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) wmin[w] = m;
+  __syncthreads();
+  if (w == 0) {
+    int nw = (blockDim.x + 31) >> 5;
+    m = lane < nw ? wmin[lane] : DBL_MAX;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
+    if (lane == 0 && m < DBL_MAX) atomicMin(&sc->min_dx_over_lambda, (unsigned long long)__double_as_longlong(m));
+  }
+}
+
+// dt, cfl and the MaxTime clamp of Main.cpp:653-681, kept on the device.
+// mode 0: query (dt and cfl only); 1: CFL-driven step; 2: step with a given dt.
+__global__ void k_dt_finalize(Params P, DevScalars* sc, int mode, double fixed_dt) {
+  double m = __longlong_as_double((long long)sc->min_dx_over_lambda);
+  sc->min_dx_over_lambda = 0x7fefffffffffffffull;  // DBL_MAX for the next reduction
+  double dt, cfl;
+  if (mode == 2) { dt = fixed_dt; cfl = dt / m; }
+  else if (P.timestep > 0) { dt = P.timestep; cfl = dt / m; }
+  else { cfl = P.cfl; dt = cfl * m; }
+  if (mode == 0) { sc->dt = dt; sc->cfl = cfl; return; }
+  double t = sc->time;
+  if (mode == 1) {
+    if (!(t < P.max_time - 1.0e-6 * dt)) { sc->active = 0; return; }
+    if (t + dt > P.max_time) { cfl *= (P.max_time - t) / dt; dt = P.max_time - t; }
+  }
+  sc->active = 1;
+  sc->dt = dt;
+  sc->cfl = cfl;
+  sc->time = t + dt;
+  sc->steps += 1;
+}
+
+// ---------------------------------------------------------------------------
+// End of step.  "Remaining" swept cells (phi >= 0 after a sign change) take the
+// smallest material ID among their 26 neighbors that are decided and not the
+// level-set material (MultiPhaseOperator.cpp:236-340).  Jacobi passes: each
+// pass decides from the previous pass's IDs; the reference resolves in
+// lexicographic order within a pass.
+__global__ void k_resolve_remaining(Params P, int32_t* id_new, const int64_t* swept, const unsigned long long* count,
+                                    int64_t cap, int32_t* cand_out, int final_pass, const DevScalars* sc) {
+  if (!sc->active) return;
+  int64_t n = (int64_t)min((unsigned long long)cap, *count);
+  const Grid& g = P.g;
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+    int64_t c = swept[s];
+    int cur = id_new[c];
+    if (cur >= 0) { cand_out[s] = cur; continue; }
+    int64_t r = c;
+    int i = (int)(r % g.px) - 1; r /= g.px;
+    int j = (int)(r % g.py) - 1;
+    int k = (int)(r / g.py) - 1;
+    int best = 0x7fffffff;
+    for (int nk = k - 1; nk <= k + 1; nk++)
+      for (int nj = j - 1; nj <= j + 1; nj++)
+        for (int ni = i - 1; ni <= i + 1; ni++) {
+          if (ni < 0 || ni >= g.nx || nj < 0 || nj >= g.ny || nk < 0 || nk >= g.nz) continue;
+          int v = id_new[g.at(ni, nj, nk)];
+          if (v < 0 || v == P.ls_matid) continue;
+          best = min(best, v);
+        }
+    if (best != 0x7fffffff) cand_out[s] = best;
+    else cand_out[s] = final_pass ? 0 : cur;  // orphans become material 0 (MultiPhaseOperator.cpp:327-334)
+  }
+}
+
+__global__ void k_commit_remaining(int32_t* id_new, const int64_t* swept, const unsigned long long* count, int64_t cap,
+                                   const int32_t* cand, const DevScalars* sc) {
+  if (!sc->active) return;
+  int64_t n = (int64_t)min((unsigned long long)cap, *count);
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x)
+    id_new[swept[s]] = cand[s];
+}
+
+// UpdateStateVariablesByRiemannSolutions / LocalUpdateByRiemannSolutions
+// (MultiPhaseOperator.cpp:980-1150) or by extrapolation (1155-1274) for every
+// swept cell whose ID changed; then ClipDensityAndPressure (TimeIntegrator.cpp:800).
+__global__ void k_swept_update(Params P, StateSet S, const int32_t* __restrict__ id_old, const int32_t* __restrict__ id_new,
+                               IfaceList L, const int64_t* swept, const unsigned long long* count, int64_t cap,
+                               unsigned long long* cnt, const DevScalars* sc) {
+  if (!sc->active) return;
+  int64_t n = (int64_t)min((unsigned long long)cap, *count);
+  const Grid& g = P.g;
+  const int64_t st[3] = {1, g.sy, g.sz};
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+    int64_t c = swept[s];
+    int myid = id_new[c];
+    if (myid == id_old[c]) continue;
+    atomic_inc(&cnt[CNT_SWEPT]);
+    double out[5];
+    int counter = 0;
+    if (P.mp_phasechange == M2CG_PHASECHANGE_RIEMANN) {
+      for (int pass = 0; pass < 2 && counter == 0; pass++) {
+        bool upwind = (pass == 0);
+        double acc[5] = {0, 0, 0, 0, 0};
+        double sum_w = 0.0;
+        for (int d = 0; d < 3; d++)
+          for (int side = 0; side < 2; side++) {
+            int64_t fc = side == 0 ? c : c + st[d];
+            int64_t nb = side == 0 ? c - st[d] : c + st[d];
+            int idm = id_old[fc - st[d]], idp = id_old[fc];
+            if (idm == idp) continue;           // not an interface face this step
+            int sl = L.slot[d][fc];
+            if (L.err[sl]) continue;            // solution not stored on failure
+            int sid = side == 0 ? idm : idp;
+            if (sid != myid) continue;
+            double vel = S.q[1 + d][nb];
+            bool upw_ok = side == 0 ? (vel > 0) : (vel < 0);
+            if (upwind && !upw_ok) continue;
+            double vx = S.q[1][nb], vy = S.q[2][nb], vz = S.q[3][nb];
+            double nrm = sqrt(vx * vx + vy * vy + vz * vz);
+            double w = upwind ? (side == 0 ? vel / nrm : -vel / nrm) : 1.0;
+            sum_w += w;
+            for (int p = 0; p < 5; p++) {
+              double sv = side == 0 ? L.vsm[p][sl] : L.vsp[p][sl];
+              if (counter == 0) acc[p] = w * sv;
+              else acc[p] += w * sv;
+            }
+            counter++;
+          }
+        if (counter > 0) {
+          if (sum_w > 0.0) { double inv = 1.0 / sum_w; for (int p = 0; p < 5; p++) out[p] = acc[p] * inv; }
+          else for (int p = 0; p < 5; p++) out[p] = acc[p];
+        }
+      }
+    } else {
+      int64_t r = c;
+      int i = (int)(r % g.px) - 1; r /= g.px;
+      int j = (int)(r % g.py) - 1;
+      int k = (int)(r / g.py) - 1;
+      double sum_w = 0.0, vs[5] = {0, 0, 0, 0, 0};
+      const double h[3] = {g.dx, g.dy, g.dz};
+      for (int nk = k - 1; nk <= k + 1; nk++)
+        for (int nj = j - 1; nj <= j + 1; nj++)
+          for (int ni = i - 1; ni <= i + 1; ni++) {
+            int64_t nc = g.at(ni, nj, nk);
+            if (id_new[nc] != myid) continue;
+            if (id_new[nc] != id_old[nc]) continue;
+            if (ni < 0 || ni >= g.nx || nj < 0 || nj >= g.ny || nk < 0 || nk >= g.nz) continue;
+            double x[3] = {(i - ni) * h[0], (j - nj) * h[1], (k - nk) * h[2]};
+            double dist = sqrt(x[0] * x[0] + x[1] * x[1] + x[2] * x[2]);
+            double w;
+            if (P.mp_pcdir == M2CG_PCDIR_ALL) w = 1.0 / dist;
+            else {
+              double v1[3] = {S.q[1][nc], S.q[2][nc], S.q[3][nc]};
+              double vn = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+              if (vn != 0) for (int m = 0; m < 3; m++) v1[m] /= vn;
+              for (int m = 0; m < 3; m++) x[m] /= dist;
+              w = fmax(0.0, x[0] * v1[0] + x[1] * v1[1] + x[2] * v1[2]);
+            }
+            if (w > 0) { sum_w += w; for (int p = 0; p < 5; p++) vs[p] += w * S.q[p][nc]; }
+          }
+      if (sum_w > 0) { counter = 1; for (int p = 0; p < 5; p++) out[p] = vs[p] / sum_w; }
+    }
+    if (counter == 0) { atomic_inc(&cnt[CNT_UNRES]); continue; }
+    const DevMat& M = P.mats.m[myid];
+    eos_clip(M, out);
+    if (eos_bad5(M, out)) atomic_inc(&cnt[CNT_BAD]);
+    for (int p = 0; p < 5; p++) S.q[p][c] = out[p];
+  }
+}
+
+__global__ void k_commit_ids(int32_t* id, const int32_t* id_new, const int64_t* swept, const unsigned long long* count,
+                             int64_t cap, const DevScalars* sc) {
+  if (!sc->active) return;
+  int64_t n = (int64_t)min((unsigned long long)cap, *count);
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x)
+    id[swept[s]] = id_new[swept[s]];
+}
+
+// ---------------------------------------------------------------------------
+// Interface-face compaction: every face whose two cells carry different IDs
+// (SpaceOperator.cpp:1613, 1772, 1931) gets a slot in the work list.
+__global__ void k_compact_interfaces(Params P, const int32_t* __restrict__ id, IfaceList L, unsigned long long* cnt,
+                                     const DevScalars* sc) {
+  if (sc && !sc->active) return;
+  const Grid& g = P.g;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t ex = g.nx + 1, ey = g.ny + 1;
+  int64_t n = ex * ey * (g.nz + 1);
+  bool valid = t < n;
+  int i = 0, j = 0, k = 0;
+  if (valid) {
+    k = (int)(t / (ex * ey));
+    int64_t r = t - (int64_t)k * ex * ey;
+    j = (int)(r / ex); i = (int)(r - (int64_t)j * ex);
+  }
+  const int64_t st[3] = {1, g.sy, g.sz};
+  for (int d = 0; d < 3; d++) {
+    bool is_if = false;
+    int64_t c = 0;
+    if (valid) {
+      bool has = d == 0 ? (j < g.ny && k < g.nz) : d == 1 ? (i < g.nx && k < g.nz) : (i < g.nx && j < g.ny);
+      c = g.at(i, j, k);
+      is_if = has && id[c - st[d]] != id[c];
+    }
+    // warp-aggregated slot allocation
+    unsigned mask = __ballot_sync(0xffffffffu, is_if);
+    if (!mask) continue;
+    int lane = threadIdx.x & 31;
+    int leader = __ffs(mask) - 1;
+    unsigned long long base = 0;
+    if (lane == leader) base = atomicAdd(L.count, (unsigned long long)__popc(mask));
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (is_if) {
+      unsigned long long s = base + __popc(mask & ((1u << lane) - 1u));
+      if ((int64_t)s < L.cap) {
+        L.face[s] = c * 4 + d;
+        L.slot[d][c] = (int32_t)s;
+      } else if (lane == leader) {
+        atomic_inc(&cnt[CNT_IF_OVERFLOW]);
+      }
+    }
+  }
+}
+
+// Sum of U * vol over real cells (conserved totals), per block partials.
+__global__ void k_conserved(Params P, StateSet S, const int32_t* __restrict__ id, double* partial) {
+  int i, j, k;
+  double u[5] = {0, 0, 0, 0, 0};
+  if (real_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) {
+    int64_t c = P.g.at(i, j, k);
+    double V[5] = {S.q[0][c], S.q[1][c], S.q[2][c], S.q[3][c], S.q[4][c]};
+    prim_to_cons(P.mats.m[id[c]], V, u);
+  }
+  __shared__ double red[5][256];
+  for (int p = 0; p < 5; p++) red[p][threadIdx.x] = u[p];
+  __syncthreads();
+  for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+    if ((int)threadIdx.x < o)
+      for (int p = 0; p < 5; p++) red[p][threadIdx.x] += red[p][threadIdx.x + o];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0)
+    for (int p = 0; p < 5; p++) partial[(int64_t)blockIdx.x * 5 + p] = red[p][0];
+}
+
+// Pack / unpack between the AoS host layout (real cells) and the ghosted SoA device layout.
+__global__ void k_unpack(Params P, const double* __restrict__ Vh, const int32_t* __restrict__ idh,
+                         const double* __restrict__ phih, StateSet S, int32_t* id, unsigned long long* cnt) {
+  int i, j, k;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!real_cell(P.g, t, i, j, k)) return;
+  int64_t c = P.g.at(i, j, k);
+  for (int p = 0; p < 5; p++) S.q[p][c] = Vh[t * 5 + p];
+  int v = idh[t];
+  if (v < 0 || v >= P.n_mat) { atomic_inc(&cnt[CNT_BADID]); v = 0; }
+  id[c] = v;
+  if (phih) S.q[5][c] = phih[t];
+}
+__global__ void k_pack(Params P, StateSet S, const int32_t* id, double* Vh, int32_t* idh, double* phih, double* const* R,
+                       double* Rh, const double* rphi, double* rphih) {
+  int i, j, k;
+  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (!real_cell(P.g, t, i, j, k)) return;
+  int64_t c = P.g.at(i, j, k);
+  if (Vh) for (int p = 0; p < 5; p++) Vh[t * 5 + p] = S.q[p][c];
+  if (idh) idh[t] = id[c];
+  if (phih) phih[t] = S.q[5][c];
+  if (Rh) for (int p = 0; p < 5; p++) Rh[t * 5 + p] = R[p][c];
+  if (rphih) rphih[t] = rphi[c];
+}
+
+// ---------------------------------------------------------------------------
+// Host-side launchers
+static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
+
+void launch_reconstruct(cudaStream_t s, const Params& P, const StateSet& S, const int32_t* id, double* const* fs,
+                        unsigned long long* cnt) {
+  int64_t n = (int64_t)P.g.nx * P.g.ny * P.g.nz;
+  k_reconstruct<<<nblk(n, 128), 128, 0, s>>>(P, S, id, fs, cnt);
+  int64_t ng = 2 * ((int64_t)P.g.ny * P.g.nz + (int64_t)P.g.nx * P.g.nz + (int64_t)P.g.nx * P.g.ny);
+  k_reconstruct_ghosts<<<nblk(ng, 128), 128, 0, s>>>(P, S, id, fs, cnt);
+}
+void launch_face_flux(cudaStream_t s, const Params& P, const int32_t* id, double* const* fs, double* const* F,
+                      unsigned long long* cnt) {
+  int64_t n = (int64_t)(P.g.nx + 1) * (P.g.ny + 1) * (P.g.nz + 1);
+  k_face_flux<<<nblk(n, 128), 128, 0, s>>>(P, id, fs, F, cnt);
+}
+void launch_update(cudaStream_t s, const Params& P, const StageArgs& A, const int32_t* id, int32_t* id_new,
+                   double* const* F, const IfaceList& L, const DevScalars* sc, int64_t* swept,
+                   unsigned long long* swept_count, int64_t swept_cap, unsigned long long* cnt) {
+  int64_t n = (int64_t)P.g.nx * P.g.ny * P.g.nz;
+  k_update<<<nblk(n, 128), 128, 0, s>>>(P, A, id, id_new, F, L, sc, swept, swept_count, swept_cap, cnt);
+}
+void launch_ls_residual(cudaStream_t s, const Params& P, const StateSet& S, double* out) {
+  int64_t n = (int64_t)P.g.nx * P.g.ny * P.g.nz;
+  k_ls_residual<<<nblk(n, 128), 128, 0, s>>>(P, S, out);
+}
+void launch_bc(cudaStream_t s, const Params& P, const StateSet& S, int do_v, int do_phi, int32_t* id,
+               const DevScalars* sc) {
+  int64_t ng = 2 * ((int64_t)P.g.ny * P.g.nz + (int64_t)P.g.nx * P.g.nz + (int64_t)P.g.nx * P.g.ny);
+  k_bc<<<nblk(ng, 128), 128, 0, s>>>(P, S, do_v, do_phi, id, sc);
+}
+void launch_dt(cudaStream_t s, const Params& P, const StateSet& S, const int32_t* id, DevScalars* sc, int mode,
+               double fixed_dt) {
+  int64_t n = (int64_t)P.g.nx * P.g.ny * P.g.nz;
+  k_dt_reduce<<<nblk(n, 256), 256, 0, s>>>(P, S, id, sc);
+  k_dt_finalize<<<1, 1, 0, s>>>(P, sc, mode, fixed_dt);
+}
+void launch_compact(cudaStream_t s, const Params& P, const int32_t* id, const IfaceList& L, unsigned long long* cnt,
+                    const DevScalars* sc) {
+  int64_t n = (int64_t)(P.g.nx + 1) * (P.g.ny + 1) * (P.g.nz + 1);
+  k_compact_interfaces<<<nblk(n, 256), 256, 0, s>>>(P, id, L, cnt, sc);
+}
+void launch_end_of_step(cudaStream_t s, const Params& P, const StateSet& S, int32_t* id, int32_t* id_new,
+                        const IfaceList& L, const int64_t* swept, const unsigned long long* swept_count,
+                        int64_t swept_cap, int32_t* cand, unsigned long long* cnt, const DevScalars* sc, int nsm) {
+  int blocks = nsm * 2;
+  const int passes = 3;
+  for (int p = 0; p < passes; p++) {
+    k_resolve_remaining<<<blocks, 256, 0, s>>>(P, id_new, swept, swept_count, swept_cap, cand, p == passes - 1, sc);
+    k_commit_remaining<<<blocks, 256, 0, s>>>(id_new, swept, swept_count, swept_cap, cand, sc);
+  }
+  k_swept_update<<<blocks, 128, 0, s>>>(P, S, id, id_new, L, swept, swept_count, swept_cap, cnt, sc);
+  k_commit_ids<<<blocks, 256, 0, s>>>(id, id_new, swept, swept_count, swept_cap, sc);
+  launch_bc(s, P, S, 1, 1, id, sc);
+}
+void launch_conserved(cudaStream_t s, const Params& P, const StateSet& S, const int32_t* id, double* partial,
+                      int* nblocks) {
+  int64_t n = (int64_t)P.g.nx * P.g.ny * P.g.nz;
+  *nblocks = nblk(n, 256);
+  k_conserved<<<*nblocks, 256, 0, s>>>(P, S, id, partial);
+}
+void launch_unpack(cudaStream_t s, const Params& P, const double* Vh, const int32_t* idh, const double* phih,
+                   const StateSet& S, int32_t* id, unsigned long long* cnt) {
+  int64_t n = (int64_t)P.g.nx * P.g.ny * P.g.nz;
+  k_unpack<<<nblk(n, 256), 256, 0, s>>>(P, Vh, idh, phih, S, id, cnt);
+}
+void launch_pack(cudaStream_t s, const Params& P, const StateSet& S, const int32_t* id, double* Vh, int32_t* idh,
+                 double* phih, double* const* R, double* Rh, const double* rphi, double* rphih) {
+  int64_t n = (int64_t)P.g.nx * P.g.ny * P.g.nz;
+  k_pack<<<nblk(n, 256), 256, 0, s>>>(P, S, id, Vh, idh, phih, R, Rh, rphi, rphih);
+}
+
+}  // namespace m2cg

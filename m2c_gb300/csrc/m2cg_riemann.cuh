@@ -1,0 +1,539 @@
+// Device exact two-material Riemann solver: the algorithm of
+// ExactRiemannSolverBase::ComputeRiemannSolution (ExactRiemannSolverBase.cpp:59-347)
+// -- acoustic-theory start, bracketing, safeguarded secant on p*, adaptive
+// Cash-Karp rarefaction integration with the per-solve integration-path cache,
+// secant/bisection Hugoniot root (the reference's WITHOUT_BOOST branch,
+// ExactRiemannSolverBase.cpp:1545-1587) and the xi = 0 sampling.
+//
+// One thread solves one problem.  Every loop is bounded by the reference's own
+// caps (MaxIts, MaxItsBracketing, MaxItsShock, 3 x IntegrationSteps), so a
+// solve always ends.  The integration-path cache lives in global scratch:
+// `cap` entries of {p, rho, u} per wave, strided by `stride` doubles so that
+// the lanes of a warp touch adjacent words.
+#pragma once
+#include "m2cg_device.cuh"
+
+namespace m2cg {
+
+struct RiemannPrm {
+  int maxIts_main, maxIts_bracket, maxIts_shock, numSteps;
+  double tol_main, tol_shock, tol_rare, min_pressure, failure_threshold, pressure_at_failure;
+};
+
+// Status bits returned alongside the reference's error code.
+enum { RS_PATH_CAPPED = 1 };
+
+struct PathCache {
+  double* base;    // entry e, component c at base[(e * 3 + c) * stride]
+  int64_t stride;
+  int cap;
+  int n;
+  int capped;
+  M2CG_DEV double get(int e, int c) const { return base[(int64_t)(e * 3 + c) * stride]; }
+  M2CG_DEV void put(int e, double p, double rho, double u) {
+    base[(int64_t)(e * 3 + 0) * stride] = p;
+    base[(int64_t)(e * 3 + 1) * stride] = rho;
+    base[(int64_t)(e * 3 + 2) * stride] = u;
+  }
+  M2CG_DEV void reset(double p, double rho, double u) { n = 1; capped = 0; put(0, p, rho, u); }
+  M2CG_DEV void push(double p, double rho, double u) {
+    if (n < cap) { put(n, p, rho, u); n++; }
+    else capped = 1;
+  }
+};
+
+struct ExactRiemannDev {
+  const Mats* mats;
+  RiemannPrm P;
+  PathCache path1, path3;
+  int evals;
+  double warm_p;   // > 0 replaces the acoustic-theory p0 (learned warm start)
+
+  M2CG_DEV const DevMat& mat(int id) const { return mats->m[id]; }
+
+  // Cash-Karp step, ExactRiemannSolverBase.cpp:1771-1896
+  __device__ __noinline__ bool rk45(int wave, const DevMat& M, double rho_0, double u_0, double p_0, double dp,
+                     double& rho, double& u, double& p, double& xi, double& uErr, double& rhoErr) const {
+    dp = -dp;
+    double e_0 = eos_e(M, rho_0, p_0);
+    double c_0_square = eos_c2(M, rho_0, e_0);
+    if (rho_0 <= 0 || c_0_square < 0) return false;
+    double c_0 = sqrt(c_0_square);
+    double rho_1 = rho_0 + 0.2 * dp / c_0_square;
+    double p_1 = p_0 + 0.2 * dp;
+    double e_1 = eos_e(M, rho_1, p_1);
+    double c_1_square = eos_c2(M, rho_1, e_1);
+    if (rho_1 <= 0 || c_1_square < 0) return false;
+    double rho_2 = rho_0 + 3. / 40. * dp / c_0_square + 9. / 40. * dp / c_1_square;
+    double p_2 = p_1 + 3. / 10. * dp;
+    double e_2 = eos_e(M, rho_2, p_2);
+    double c_2_square = eos_c2(M, rho_2, e_2);
+    if (rho_2 <= 0 || c_2_square < 0) return false;
+    double c_2 = sqrt(c_2_square);
+    double rho_3 = rho_0 + 3. / 10. * dp / c_0_square - 9. / 10. * dp / c_1_square + 6. / 5. * dp / c_2_square;
+    double p_3 = p_0 + 3. / 5. * dp;
+    double e_3 = eos_e(M, rho_3, p_3);
+    double c_3_square = eos_c2(M, rho_3, e_3);
+    if (rho_3 <= 0 || c_3_square < 0) return false;
+    double c_3 = sqrt(c_3_square);
+    double rho_4 = rho_0 - 11. / 54. * dp / c_0_square + 2.5 * dp / c_1_square - 70. / 27. * dp / c_2_square +
+                   35. / 27. * dp / c_3_square;
+    double p_4 = p_0 + dp;
+    double e_4 = eos_e(M, rho_4, p_4);
+    double c_4_square = eos_c2(M, rho_4, e_4);
+    if (rho_4 <= 0 || c_4_square < 0) return false;
+    double c_4 = sqrt(c_4_square);
+    double rho_5 = rho_0 + 1631. / 55296. * dp / c_0_square + 175. / 512. * dp / c_1_square +
+                   575. / 13824. * dp / c_2_square + 44275. / 110592. * dp / c_3_square + 253. / 4096. * dp / c_4_square;
+    double p_5 = p_0 + 7. / 8. * dp;
+    double e_5 = eos_e(M, rho_5, p_5);
+    double c_5_square = eos_c2(M, rho_5, e_5);
+    if (rho_5 <= 0 || c_5_square < 0) return false;
+    double c_5 = sqrt(c_5_square);
+    double drho = (37. / 378. / c_0_square + 250. / 621. / c_2_square + 125. / 594. / c_3_square + 512. / 1771. / c_5_square) * dp;
+    double drho_err = (2825. / 27648. / c_0_square + 18575. / 48384. / c_2_square + 13525. / 55296. / c_3_square +
+                       277. / 14336. / c_4_square + 0.25 / c_5_square) * dp;
+    double du = (37. / 378. / c_0 / rho_0 + 250. / 621. / c_2 / rho_2 + 125. / 594. / c_3 / rho_3 + 512. / 1771. / c_5 / rho_5) * dp;
+    double du_err = (2825. / 27648. / c_0 / rho_0 + 18575. / 48384. / c_2 / rho_2 + 13525. / 55296. / c_3 / rho_3 +
+                     277. / 14336. / c_4 / rho_4 + 0.25 / c_5 / rho_5) * dp;
+    if (isnan(du) || isnan(du_err)) return false;
+    rhoErr = fabs(drho_err - drho);
+    uErr = fabs(du_err - du);
+    rho = rho_0 + drho;
+    p = p_0 + dp;
+    u = (wave == 1) ? u_0 - du : u_0 + du;
+    double e = eos_e(M, rho, p);
+    double c = eos_c2(M, rho, e);
+    if (rho <= 0 || c < 0) return false;
+    c = sqrt(c);
+    xi = (wave == 1) ? u - c : u + c;
+    return true;
+  }
+
+  // Hugoniot residual, ExactRiemannSolverBase.h:66-83
+  M2CG_DEV double hugo(const DevMat& M, double e, double pavg, double one_over_rho, double ps, double rhos) const {
+    double es = eos_e(M, rhos, ps);
+    return es - e + pavg * (1.0 / rhos - one_over_rho);
+  }
+
+  // ExactRiemannSolverBase.cpp:1212-1624
+  __device__ __noinline__ bool rho_u_star(int wave, PathCache& path, double rho, double u, double p, double ps, int id,
+                           double rhos0, double rhos1, double& rhos, double& us, bool* trans_rare, double* Vrare) {
+    const DevMat& M = mat(id);
+    rhos = rho;
+    us = u;
+    if (p > ps) {
+      double rhos_0 = rho, us_0 = u, ps_0 = p, xi_0;
+      double rhos_1 = rho, us_1 = u, ps_1 = p, xi_1 = 0;
+      double dp = (p - ps) / P.numSteps;
+      double dp_min = dp / 2.5;
+      double tol_end = P.tol_rare * fmax(1.0, fabs(p));
+      double e = eos_e(M, rho, p);
+      double c = eos_c2(M, rho, e);
+      if (rho <= 0 || c < 0) return false;
+      c = sqrt(c);
+      int index0 = 0;
+      if (path.n > 1) {
+        for (int j = path.n - 1; j >= 0; j--) {
+          if (path.get(j, 0) > ps) { index0 = j; break; }
+        }
+        ps_0 = path.get(index0, 0);
+        rhos_0 = path.get(index0, 1);
+        us_0 = path.get(index0, 2);
+        dp_min = (ps_0 - ps) / P.numSteps / 2.5;
+        if (index0 != path.n - 1) dp = ps_0 - ps;
+        else dp = fmin(path.get(index0 - 1, 0) - path.get(index0, 0), ps_0 - ps);
+      }
+      double xi = (wave == 1) ? u - c : u + c;
+      xi_0 = xi;
+      bool done = false;
+      double uErr = 0., rhoErr = 0.;
+      const double errBar = fmax(1.0e-8, fmin(1.0e-5, 100.0 * P.tol_rare));
+      for (int i = 0; i < P.numSteps * 3; i++) {
+        if (fabs(ps_1 - ps) <= tol_end) {
+          rhos = rhos_1;
+          us = us_1;
+          if (eos_bad(M, rhos, ps)) return false;
+          done = true;
+          break;
+        }
+        bool ok = rk45(wave, M, rhos_0, us_0, ps_0, dp, rhos_1, us_1, ps_1, xi_1, uErr, rhoErr);
+        if (!ok) { dp = dp / 2.0; continue; }
+        if (ps_1 - ps < -tol_end) { dp = ps_0 - ps; continue; }
+        double uS = uErr / c + 1.e-30;
+        double rS = rhoErr / rho + 1.e-30;
+        if (isnan(rS) || isnan(uS)) return false;
+        if (rS >= errBar && dp > dp_min) {
+          double t = 0.9 * dp * pow(fabs(errBar / rS), 0.25);
+          t = fmax(fmax(t, 0.2 * dp), dp_min);
+          dp = fmin(t, ps_0 - ps);
+          continue;
+        }
+        if (uS >= errBar && dp > dp_min) {
+          double t = 0.9 * dp * pow(fabs(errBar / uS), 0.25);
+          t = fmax(fmax(t, 0.2 * dp), dp_min);
+          dp = fmin(t, ps_0 - ps);
+          continue;
+        }
+        if (ps_1 < path.get(path.n - 1, 0)) path.push(ps_1, rhos_1, us_1);
+        if (trans_rare && Vrare && xi_0 * xi_1 <= 0) {
+          *trans_rare = true;
+          double w0 = fabs(xi_1), w1 = fabs(xi_0);
+          double ww = w0 + w1;
+          w0 /= ww;
+          w1 /= ww;
+          Vrare[0] = w0 * rhos_0 + w1 * rhos_1;
+          Vrare[1] = w0 * us_0 + w1 * us_1;
+          Vrare[2] = w0 * ps_0 + w1 * ps_1;
+        }
+        double tr = 0.9 * dp * pow(fabs(errBar / rS), 0.2);
+        double tu = 0.9 * dp * pow(fabs(errBar / uS), 0.2);
+        double t = fmin(tr, tu);
+        t = fmin(t, 10 * dp);
+        t = fmax(t, dp_min);
+        dp = fmin(t, ps_1 - ps);
+        rhos_0 = rhos_1; us_0 = us_1; ps_0 = ps_1; xi_0 = xi_1;
+      }
+      if (!done) return false;
+    } else {
+      double e = eos_e(M, rho, p);
+      double pavg = 0.5 * (p + ps);
+      double oor = 1.0 / rho;
+      double f0, f1;
+      double drho = fmax(fabs(rhos0 - rhos1), 0.001 * rhos0);
+      bool found0 = false, found1 = false;
+      if (fmin(rhos0, rhos1) >= rho) {
+        f0 = hugo(M, e, pavg, oor, ps, rhos0);
+        f1 = hugo(M, e, pavg, oor, ps, rhos1);
+        if (f0 * f1 <= 0) {
+          if (rhos0 > rhos1) { double t = rhos0; rhos0 = rhos1; rhos1 = t; t = f0; f0 = f1; f1 = t; }
+          found0 = found1 = true;
+        } else { rhos0 = rhos1; f0 = f1; }
+      } else {
+        if (rhos1 > rhos0) { rhos0 = rhos1; f0 = hugo(M, e, pavg, oor, ps, rhos0); }
+        if (rhos0 < rho) { rhos0 = rho; f0 = hugo(M, e, pavg, oor, ps, rhos0); found0 = true; }
+        else f0 = hugo(M, e, pavg, oor, ps, rhos0);
+      }
+      if (!found0 || !found1) {
+        int i = 0;
+        const double factor = 1.5;
+        double tmp, ftmp;
+        rhos1 = rhos0;
+        f1 = f0;
+        while (!found0) {
+          if (++i >= P.maxIts_shock) return false;
+          tmp = rhos1; ftmp = f1;
+          rhos1 = rhos0; f1 = f0;
+          rhos0 = rhos1 - factor * drho;
+          if (rhos0 <= rho) { rhos0 = rho; found0 = true; }
+          f0 = hugo(M, e, pavg, oor, ps, rhos0);
+          if (f0 * f1 <= 0) found0 = found1 = true;
+          else {
+            rhos1 = tmp; f1 = ftmp;
+            tmp = rhos0; ftmp = f0;
+            rhos0 = rhos1; f0 = f1;
+            rhos1 = rhos0 + factor * drho;
+            f1 = hugo(M, e, pavg, oor, ps, rhos1);
+            if (f0 * f1 <= 0) found0 = found1 = true;
+            else { rhos0 = tmp; f0 = ftmp; drho = rhos1 - rhos0; }
+          }
+        }
+        if (!found1) {
+          i = 0;
+          while (!found1) {
+            if (++i >= P.maxIts_shock) return false;
+            rhos0 = rhos1; f0 = f1;
+            rhos1 = rhos0 + 2.5 * drho;
+            f1 = hugo(M, e, pavg, oor, ps, rhos1);
+            if (f0 * f1 <= 0) found1 = true;
+            else drho = rhos1 - rhos0;
+          }
+        }
+      }
+      double loc_tol = P.tol_shock * fmin(rhos0, rhos1);
+      double s_first = 0, s_second = 0;
+      if (f0 == 0.0) s_first = s_second = rhos0;
+      else if (f1 == 0.0) s_first = s_second = rhos1;
+      else {
+        double rhos2 = rhos1, f2 = f1;
+        int it;
+        for (it = 0; it < P.maxIts_shock; it++) {
+          drho = rhos1 - rhos0;
+          rhos2 = rhos2 - f2 * (rhos1 - rhos0) / (f1 - f0);
+          if (rhos2 >= rhos1 || rhos2 <= rhos0) rhos2 = rhos0 + 0.5 * (rhos1 - rhos0);
+          f2 = hugo(M, e, pavg, oor, ps, rhos2);
+          if (f2 == 0.0) { s_first = s_second = rhos2; break; }
+          if (f2 * f0 < 0) { rhos1 = rhos2; f1 = f2; }
+          else { rhos0 = rhos2; f0 = f2; }
+          if (rhos1 - rhos0 < loc_tol) { s_first = rhos0; s_second = rhos1; break; }
+        }
+        if (it == P.maxIts_shock) return false;
+      }
+      rhos = 0.5 * (s_first + s_second);
+      double du = -(ps - p) * (1.0 / rhos - 1.0 / rho);
+      if (du < 0) return false;
+      if (eos_bad(M, rhos, ps)) return false;
+      us = (wave == 1) ? u - sqrt(du) : u + sqrt(du);
+    }
+    return true;
+  }
+
+  M2CG_DEV bool pair(double p, double rhol, double ul, double pl, int idl, double rhor, double ur, double pr, int idr,
+                     double gl0, double gl1, double gr0, double gr1, double& rl, double& uL, double& rr, double& uR) {
+    evals++;
+    bool s = rho_u_star(1, path1, rhol, ul, pl, p, idl, gl0, gl1, rl, uL, nullptr, nullptr);
+    return s && rho_u_star(3, path3, rhor, ur, pr, p, idr, gr0, gr1, rr, uR, nullptr, nullptr);
+  }
+
+  // ExactRiemannSolverBase.cpp:1107-1158
+  __device__ __noinline__ int acoustic(double rhol, double ul, double pl, double cl, int idl, double rhor, double ur, double pr,
+                        double cr, int idr, double& p0, double& rhol0, double& rhor0, double& ul0, double& ur0,
+                        double& p1, double& rhol1, double& rhor1, double& ul1, double& ur1) {
+    double Cl = rhol * cl, Cr = rhor * cr;
+    p0 = (Cr * pl + Cl * pr + Cl * Cr * (ul - ur)) / (Cl + Cr);
+    if (warm_p > 0.0) p0 = warm_p;
+    evals++;
+    if (!rho_u_star(1, path1, rhol, ul, pl, p0, idl, rhol, (p0 > pl) ? rhol * 1.1 : rhol * 0.9, rhol0, ul0, nullptr, nullptr)) return 0;
+    if (!rho_u_star(3, path3, rhor, ur, pr, p0, idr, rhor, (p0 > pr) ? rhor * 1.1 : rhor * 0.9, rhor0, ur0, nullptr, nullptr)) return 0;
+    double Clbar = (ul0 == ul) ? Cl : fabs(p0 - pl) / fabs(ul0 - ul);
+    double Crbar = (ur0 == ur) ? Cr : fabs(p0 - pr) / fabs(ur0 - ur);
+    p1 = (Crbar * pl + Clbar * pr + Clbar * Crbar * (ul - ur)) / (Clbar + Crbar);
+    double tmp = fmax(fabs(p0), fabs(p1));
+    if (fabs(p1 - p0) / tmp < 1.0e-8) p1 = p0 + 1.0e-8 * tmp;
+    evals++;
+    if (!rho_u_star(1, path1, rhol, ul, pl, p1, idl, rhol, rhol0, rhol1, ul1, nullptr, nullptr)) return 1;
+    if (!rho_u_star(3, path3, rhor, ur, pr, p1, idr, rhor, rhor0, rhor1, ur1, nullptr, nullptr)) return 1;
+    return 2;
+  }
+
+  // ExactRiemannSolverBase.cpp:1002-1103
+  __device__ __noinline__ bool feasible(double rhol, double ul, double pl, double cl, int idl, double rhor, double ur, double pr,
+                         double cr, int idr, double& p0, double& rhol0, double& rhor0, double& ul0, double& ur0,
+                         double& p1, double& rhol1, double& rhor1, double& ul1, double& ur1) {
+    int found = acoustic(rhol, ul, pl, cl, idl, rhor, ur, pr, cr, idr, p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
+    if (found == 2) return true;
+    bool ok = true;
+    double dp;
+    if (found != 1) {
+      dp = (pl != pr) ? fabs(pl - pr) : 0.5 * pl;
+      for (int i = 0; i < P.maxIts_bracket; i++) {
+        p0 = fmin(pl, pr) + 0.01 * (i + 1) * (i + 1) * fmin(dp, fmin(fabs(pl), fabs(pr)));
+        if (p0 < P.min_pressure) p0 = P.pressure_at_failure;
+        ok = pair(p0, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol, (p0 > pl) ? rhol * 1.1 : rhol * 0.9, rhor,
+                  (p0 > pr) ? rhor * 1.1 : rhor * 0.9, rhol0, ul0, rhor0, ur0);
+        if (ok) break;
+      }
+      if (!ok) {
+        for (int i = 0; i < P.maxIts_bracket; i++) {
+          p0 = fmin(pl, pr) - 0.01 * (i + 1) * (i + 1) * fmin(dp, fmin(fabs(pl), fabs(pr)));
+          if (p0 < P.min_pressure || i == P.maxIts_bracket / 2) p0 = P.pressure_at_failure;
+          ok = pair(p0, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol, (p0 > pl) ? rhol * 1.1 : rhol * 0.9, rhor,
+                    (p0 > pr) ? rhor * 1.1 : rhor * 0.9, rhol0, ul0, rhor0, ur0);
+          if (ok) break;
+        }
+      }
+      if (!ok) return false;
+    }
+    dp = fmin(fabs(p0 - pl), fabs(p0 - pr));
+    for (int i = 0; i < P.maxIts_bracket; i++) {
+      p1 = p0 + 0.01 * (i + 1) * (i + 1) * dp;
+      ok = pair(p1, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol, rhol0, rhor, rhor0, rhol1, ul1, rhor1, ur1);
+      if (ok) break;
+    }
+    if (!ok) {
+      for (int i = 0; i < P.maxIts_bracket; i++) {
+        p1 = p0 - 0.01 * (i + 1) * (i + 1) * dp;
+        if (p1 < P.min_pressure) p1 = P.pressure_at_failure * 1000.0;
+        ok = pair(p1, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol, rhol0, rhor, rhor0, rhol1, ul1, rhor1, ur1);
+        if (ok) break;
+      }
+    }
+    if (!ok) return false;
+    if (p0 > p1) {
+      double t;
+      t = p0; p0 = p1; p1 = t;
+      t = rhol0; rhol0 = rhol1; rhol1 = t;
+      t = rhor0; rhor0 = rhor1; rhor1 = t;
+      t = ul0; ul0 = ul1; ul1 = t;
+      t = ur0; ur0 = ur1; ur1 = t;
+    }
+    return true;
+  }
+
+  // ExactRiemannSolverBase.cpp:674-839
+  __device__ __noinline__ bool bracket(double rhol, double ul, double pl, double cl, int idl, double rhor, double ur, double pr,
+                        double cr, int idr, double& p0, double& rhol0, double& rhor0, double& ul0, double& ur0,
+                        double& p1, double& rhol1, double& rhor1, double& ul1, double& ur1) {
+    bool ok = feasible(rhol, ul, pl, cl, idl, rhor, ur, pr, cr, idr, p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
+    if (!ok) { p0 = p1 = P.pressure_at_failure; return false; }
+    double p2 = 0, rhol2 = 0, rhor2 = 0, ul2 = 0, ur2 = 0, f0, f1;
+    double fmin_, p_f, rl_f, rr_f, ul_f, ur_f;
+    if (fabs(ul0 - ur0) < fabs(ul1 - ur1)) { fmin_ = fabs(ul0 - ur0); p_f = p0; rl_f = rhol0; rr_f = rhor0; ul_f = ul0; ur_f = ur0; }
+    else { fmin_ = fabs(ul1 - ur1); p_f = p1; rl_f = rhol1; rr_f = rhor1; ul_f = ul1; ur_f = ur1; }
+    int i;
+    for (i = 0; i < P.maxIts_bracket; i++) {
+      f0 = ul0 - ur0;
+      f1 = ul1 - ur1;
+      if (f0 * f1 <= 0.0) return true;
+      if (fabs(f0 - f1) > 1e-9) {
+        p2 = p1 - f1 * (p1 - p0) / (f1 - f0);
+        if (p2 < p0) p2 -= 0.1 * (p1 - p0);
+        else p2 += 0.1 * (p1 - p0);
+      } else p2 = 1.1 * p1;
+      if (p2 < P.min_pressure || i == P.maxIts_bracket / 2) p2 = 1.0e-8;
+      ok = pair(p2, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol0, rhol1, rhor0, rhor1, rhol2, ul2, rhor2, ur2);
+      if (!ok) {
+        for (int j = 0; j < P.maxIts_bracket / 2; j++) {
+          if (p2 < p0) p2 = p0 - 0.5 * (p0 - p2);
+          else p2 = p1 + 0.5 * (p2 - p1);
+          ok = pair(p2, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol0, rhol1, rhor0, rhor1, rhol2, ul2, rhor2, ur2);
+          if (ok) break;
+        }
+      }
+      if (!ok) break;
+      if (fabs(ul2 - ur2) < fmin_) { fmin_ = fabs(ul2 - ur2); p_f = p2; rl_f = rhol2; rr_f = rhor2; ul_f = ul2; ur_f = ur2; }
+      if (p2 < p0) {
+        p1 = p0; rhol1 = rhol0; rhor1 = rhor0; ul1 = ul0; ur1 = ur0;
+        p0 = p2; rhol0 = rhol2; rhor0 = rhor2; ul0 = ul2; ur0 = ur2;
+      } else {
+        p0 = p1; rhol0 = rhol1; rhor0 = rhor1; ul0 = ul1; ur0 = ur1;
+        p1 = p2; rhol1 = rhol2; rhor1 = rhor2; ul1 = ul2; ur1 = ur2;
+      }
+    }
+    if (fmin_ < P.failure_threshold * fabs(ul - ur)) {
+      p0 = p1 = p_f; rhol0 = rhol1 = rl_f; rhor0 = rhor1 = rr_f; ul0 = ul1 = ul_f; ur0 = ur1 = ur_f;
+    } else {
+      p2 = P.pressure_at_failure;
+      ok = pair(p2, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol0, rhol1, rhor0, rhor1, rhol2, ul2, rhor2, ur2);
+      if (ok) { p0 = p1 = p2; rhol0 = rhol1 = rhol2; rhor0 = rhor1 = rhor2; ul0 = ul1 = ul2; ur0 = ur1 = ur2; }
+      else { p0 = p1 = p_f; rhol0 = rhol1 = rl_f; rhor0 = rhor1 = rr_f; ul0 = ul1 = ul_f; ur0 = ur1 = ur_f; }
+    }
+    return false;
+  }
+
+  // ExactRiemannSolverBase.cpp:351-558
+  __device__ __noinline__ void finalize(const double* dir, const double* Vm, const double* Vp, double rhol, double ul, double pl,
+                         int idl, double rhor, double ur, double pr, int idr, double rhol2, double rhor2, double u2,
+                         double p2, bool trans_rare, const double* Vrare, double* Vs, int& id, double* Vsm, double* Vsp) {
+    double utl[3] = {Vm[1] - ul * dir[0], Vm[2] - ul * dir[1], Vm[3] - ul * dir[2]};
+    double utr[3] = {Vp[1] - ur * dir[0], Vp[2] - ur * dir[1], Vp[3] - ur * dir[2]};
+    id = (u2 >= 0) ? idl : idr;
+    if (trans_rare) {
+      Vs[0] = Vrare[0]; Vs[1] = Vrare[1] * dir[0]; Vs[2] = Vrare[1] * dir[1]; Vs[3] = Vrare[1] * dir[2]; Vs[4] = Vrare[2];
+    } else if (u2 >= 0) {
+      bool star = false;
+      if (pl >= p2) {
+        const DevMat& M = mat(idl);
+        double cl2 = sqrt(fmax(eos_c2(M, rhol2, eos_e(M, rhol2, p2)), 0.0));
+        if (u2 - cl2 <= 0) star = true;
+      } else if ((rhol2 * u2 - rhol * ul) / (rhol2 - rhol) <= 0) star = true;
+      if (star) { Vs[0] = rhol2; Vs[1] = u2 * dir[0]; Vs[2] = u2 * dir[1]; Vs[3] = u2 * dir[2]; Vs[4] = p2; }
+      else { Vs[0] = rhol; Vs[1] = ul * dir[0]; Vs[2] = ul * dir[1]; Vs[3] = ul * dir[2]; Vs[4] = pl; }
+    } else {
+      bool star = false;
+      if (pr >= p2) {
+        const DevMat& M = mat(idr);
+        double cr2 = sqrt(fmax(eos_c2(M, rhor2, eos_e(M, rhor2, p2)), 0.0));
+        if (u2 - cr2 >= 0) star = true;
+      } else if ((rhor2 * u2 - rhor * ur) / (rhor2 - rhor) >= 0) star = true;
+      if (star) { Vs[0] = rhor2; Vs[1] = u2 * dir[0]; Vs[2] = u2 * dir[1]; Vs[3] = u2 * dir[2]; Vs[4] = p2; }
+      else { Vs[0] = rhor; Vs[1] = ur * dir[0]; Vs[2] = ur * dir[1]; Vs[3] = ur * dir[2]; Vs[4] = pr; }
+    }
+    for (int i = 1; i <= 3; i++) {
+      if (u2 > 0) Vs[i] += utl[i - 1];
+      else if (u2 < 0) Vs[i] += utr[i - 1];
+      else Vs[i] += 0.5 * (utl[i - 1] + utr[i - 1]);
+    }
+    Vsm[0] = rhol2; Vsm[1] = utl[0] + u2 * dir[0]; Vsm[2] = utl[1] + u2 * dir[1]; Vsm[3] = utl[2] + u2 * dir[2]; Vsm[4] = p2;
+    Vsp[0] = rhor2; Vsp[1] = utr[0] + u2 * dir[0]; Vsp[2] = utr[1] + u2 * dir[1]; Vsp[3] = utr[2] + u2 * dir[2]; Vsp[4] = p2;
+  }
+
+  // ExactRiemannSolverBase.cpp:59-347.  Returns 0 (ok), 1 (failed), -1 (nonphysical input).
+  __device__ __noinline__ int solve(const double* dir, const double* Vm, int idl, const double* Vp, int idr, double* Vs, int& id,
+                     double* Vsm, double* Vsp) {
+    evals = 0;
+    double rhol = Vm[0], ul = Vm[1] * dir[0] + Vm[2] * dir[1] + Vm[3] * dir[2], pl = Vm[4];
+    double rhor = Vp[0], ur = Vp[1] * dir[0] + Vp[2] * dir[1] + Vp[3] * dir[2], pr = Vp[4];
+    path1.reset(pl, rhol, ul);
+    path3.reset(pr, rhor, ur);
+    const DevMat& ML = mat(idl);
+    const DevMat& MR = mat(idr);
+    double cl = eos_c2(ML, rhol, eos_e(ML, rhol, pl));
+    double cr = eos_c2(MR, rhor, eos_e(MR, rhor, pr));
+    if (rhol <= 0 || cl < 0 || rhor <= 0 || cr < 0) {
+      for (int i = 0; i < 5; i++) { Vsm[i] = Vm[i]; Vsp[i] = Vp[i]; Vs[i] = Vm[i]; }
+      id = idl;
+      return -1;
+    }
+    cl = sqrt(cl);
+    cr = sqrt(cr);
+    double p0 = DBL_MIN, ul0 = 0, ur0 = 0, rhol0 = DBL_MIN, rhor0 = DBL_MIN;
+    double p1 = DBL_MIN, ul1 = 0, ur1 = 0, rhol1 = DBL_MIN, rhor1 = DBL_MIN;
+    double p2 = DBL_MIN, ul2 = 0, ur2 = 0, rhol2 = DBL_MIN, rhor2 = DBL_MIN;
+    bool trans_rare = false;
+    double Vrare[3] = {0, 0, 0};
+    if (ul == ur && pl == pr) {
+      finalize(dir, Vm, Vp, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol, rhor, ul, pl, false, Vrare, Vs, id, Vsm, Vsp);
+      return 0;
+    }
+    bool ok = bracket(rhol, ul, pl, cl, idl, rhor, ur, pr, cr, idr, p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
+    if (!ok) {
+      ok = rho_u_star(1, path1, rhol, ul, pl, p1, idl, rhol0, rhol0 * 1.1, rhol2, ul2, &trans_rare, Vrare);
+      ok = ok && rho_u_star(3, path3, rhor, ur, pr, p1, idr, rhor0, rhol0 * 1.1, rhor2, ur2, &trans_rare, Vrare);
+      if (!ok) {
+        for (int i = 0; i < 5; i++) { Vsm[i] = Vm[i]; Vsp[i] = Vp[i]; }
+        double ua = 0.5 * (ul + ur);
+        id = (ua >= 0) ? idl : idr;
+        for (int i = 0; i < 5; i++) Vs[i] = (ua >= 0) ? Vm[i] : Vp[i];
+        return 1;
+      }
+      finalize(dir, Vm, Vp, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol2, rhor2, 0.5 * (ul2 + ur2), p1, trans_rare,
+               Vrare, Vs, id, Vsm, Vsp);
+      return 1;
+    }
+    double f0 = ul0 - ur0, f1 = ul1 - ur1, f2;
+    p2 = p1;
+    f2 = f1;
+    int iter;
+    for (iter = 0; iter < P.maxIts_main; iter++) {
+      double denom = f1 - f0;
+      if (denom == 0) p2 = p0 + 0.5 * (p1 - p0);
+      else {
+        p2 = p2 - f2 * (p1 - p0) / denom;
+        if (p2 <= p0 || p2 >= p1) p2 = p0 + 0.5 * (p1 - p0);
+      }
+      // the reference's "try_again" loop (ExactRiemannSolverBase.cpp:239-278)
+      bool pass = false;
+      while (true) {
+        evals++;
+        if (!rho_u_star(1, path1, rhol, ul, pl, p2, idl, rhol0, rhol1, rhol2, ul2, &trans_rare, Vrare)) {
+          p2 = 0.5 * (p2 + p0);
+          iter++;
+          if (iter < P.maxIts_main) continue;
+          break;
+        }
+        if (!rho_u_star(3, path3, rhor, ur, pr, p2, idr, rhor0, rhor1, rhor2, ur2, &trans_rare, Vrare)) {
+          p2 = 0.5 * (p2 + p1);
+          iter++;
+          if (iter < P.maxIts_main) continue;
+          break;
+        }
+        pass = true;
+        break;
+      }
+      if (!pass) break;
+      f2 = ul2 - ur2;
+      if (f0 * f2 < 0.0) { p1 = p2; f1 = f2; rhol1 = rhol2; rhor1 = rhor2; }
+      else { p0 = p2; f0 = f2; rhol0 = rhol2; rhor0 = rhor2; }
+      double err_p = fabs(p1 - p0) / fmax(fabs(pl + 0.5 * rhol * ul * ul), fabs(pr + 0.5 * rhor * ur * ur));
+      double err_u = fabs(f2) / fmax(cl, cr);
+      if ((err_p < P.tol_main && err_u < P.tol_main) || (err_p < P.tol_main * 1e-3) || (err_u < P.tol_main * 1e-3)) break;
+      trans_rare = false;
+    }
+    finalize(dir, Vm, Vp, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol2, rhor2, 0.5 * (ul2 + ur2), p2, trans_rare, Vrare,
+             Vs, id, Vsm, Vsp);
+    return (iter == P.maxIts_main) ? 1 : 0;
+  }
+};
+
+}  // namespace m2cg

@@ -1,0 +1,112 @@
+"""Host-side mirror of the reference's operator interface for the
+finite-volume step, over the C ABI of libm2cg.so.
+
+`FluidState` is the triple {V, ID, Phi} the reference's operators act on
+(Main.cpp:283-327).  `Solver` exposes the reference's method names:
+ComputeTimeStepSize (SpaceOperator.cpp:1298), ComputeResidual
+(SpaceOperator.cpp:2573), LevelSetResidual (LevelSetOperator.cpp:768),
+AdvanceOneTimeStep (TimeIntegrator.cpp:319/527) and the Main.cpp:653-771 loop
+as run().  Everything executes on the GPU; there is no CPU fallback.
+"""
+import ctypes as C
+from dataclasses import dataclass
+
+import numpy as np
+
+from . import abi
+
+
+@dataclass
+class FluidState:
+    V: np.ndarray      # (N, 5) primitive state rho, u, v, w, p, real cells k-major
+    ID: np.ndarray     # (N,) int32 material IDs
+    Phi: np.ndarray    # (N,) level set (negative inside the tracked material)
+
+
+class Solver:
+    def __init__(self, cfg, state=None, lib=None):
+        self.lib = lib or abi.load()
+        self.cfg = cfg
+        self.n = cfg.nx * cfg.ny * cfg.nz
+        h = C.c_void_p()
+        abi.check(self.lib, self.lib.m2cg_create(C.byref(cfg), C.byref(h)), "m2cg_create")
+        self.ctx = h
+        if state is not None:
+            self.set_state(state)
+
+    def close(self):
+        if getattr(self, "ctx", None):
+            self.lib.m2cg_destroy(self.ctx)
+            self.ctx = None
+
+    def __del__(self):
+        self.close()
+
+    def set_state(self, s):
+        V = np.ascontiguousarray(s.V, np.float64)
+        ID = np.ascontiguousarray(s.ID, np.int32)
+        Phi = None if s.Phi is None else np.ascontiguousarray(s.Phi, np.float64)
+        assert V.shape == (self.n, 5) and ID.shape == (self.n,)
+        abi.check(self.lib, self.lib.m2cg_upload_state(self.ctx, abi.dptr(V), abi.iptr(ID), abi.dptr(Phi)),
+                  "m2cg_upload_state")
+
+    def get_state(self):
+        V = np.zeros((self.n, 5))
+        ID = np.zeros(self.n, np.int32)
+        Phi = np.zeros(self.n)
+        abi.check(self.lib, self.lib.m2cg_download_state(self.ctx, abi.dptr(V), abi.iptr(ID), abi.dptr(Phi)),
+                  "m2cg_download_state")
+        return FluidState(V, ID, Phi)
+
+    def ComputeTimeStepSize(self):
+        dt, cfl = C.c_double(), C.c_double()
+        abi.check(self.lib, self.lib.m2cg_compute_dt(self.ctx, C.byref(dt), C.byref(cfl)), "m2cg_compute_dt")
+        return dt.value, cfl.value
+
+    def ComputeResidual(self):
+        R = np.zeros((self.n, 5))
+        abi.check(self.lib, self.lib.m2cg_compute_residual(self.ctx, abi.dptr(R)), "m2cg_compute_residual")
+        return R
+
+    def LevelSetResidual(self):
+        R = np.zeros(self.n)
+        abi.check(self.lib, self.lib.m2cg_levelset_residual(self.ctx, abi.dptr(R)), "m2cg_levelset_residual")
+        return R
+
+    def AdvanceOneTimeStep(self, dt):
+        abi.check(self.lib, self.lib.m2cg_advance(self.ctx, float(dt)), "m2cg_advance")
+
+    def run(self, nsteps):
+        c = abi.Counters()
+        abi.check(self.lib, self.lib.m2cg_run(self.ctx, int(nsteps), C.byref(c)), "m2cg_run")
+        return c.as_dict()
+
+    def counters(self):
+        c = abi.Counters()
+        abi.check(self.lib, self.lib.m2cg_get_counters(self.ctx, C.byref(c)), "m2cg_get_counters")
+        return c.as_dict()
+
+    def conserved_totals(self):
+        t = np.zeros(5)
+        abi.check(self.lib, self.lib.m2cg_conserved_totals(self.ctx, abi.dptr(t)), "m2cg_conserved_totals")
+        return t
+
+    def riemann_batch(self, Vm, idm, Vp, idp, dirs):
+        n = len(idm)
+        Vs, Vsm, Vsp = np.zeros((n, 5)), np.zeros((n, 5)), np.zeros((n, 5))
+        oid, it, err = np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n, np.int32)
+        abi.check(self.lib, self.lib.m2cg_riemann_batch(
+            self.ctx, n, abi.dptr(np.ascontiguousarray(Vm, np.float64)), abi.iptr(np.ascontiguousarray(idm, np.int32)),
+            abi.dptr(np.ascontiguousarray(Vp, np.float64)), abi.iptr(np.ascontiguousarray(idp, np.int32)),
+            abi.dptr(np.ascontiguousarray(dirs, np.float64)), abi.dptr(Vs), abi.iptr(oid), abi.dptr(Vsm),
+            abi.dptr(Vsp), abi.iptr(it), abi.iptr(err)), "m2cg_riemann_batch")
+        return dict(Vs=Vs, id=oid, Vsm=Vsm, Vsp=Vsp, iters=it, err=err)
+
+    def flux_batch(self, dirs, Vm, Vp, ids):
+        n = len(ids)
+        F = np.zeros((n, 5))
+        abi.check(self.lib, self.lib.m2cg_flux_batch(
+            self.ctx, n, abi.iptr(np.ascontiguousarray(dirs, np.int32)), abi.dptr(np.ascontiguousarray(Vm, np.float64)),
+            abi.dptr(np.ascontiguousarray(Vp, np.float64)), abi.iptr(np.ascontiguousarray(ids, np.int32)),
+            abi.dptr(F)), "m2cg_flux_batch")
+        return F

@@ -1,0 +1,944 @@
+// ORACLE -- test infrastructure only.
+//
+// CPU restatement of M2C's explicit multi-material finite-volume step, used by
+// tests/, __graft_entry__.smoke() and bench.py's CPU-baseline leg as the
+// checker for the GPU library.  No product code links, loads or calls it.
+//
+// What it restates (reference file:line):
+//   SpaceOperator::ComputeAdvectionFluxes   SpaceOperator.cpp:1432-2076
+//   SpaceOperator::CheckReconstructedStates SpaceOperator.cpp:2420-2569
+//   SpaceOperator::ComputeResidual          SpaceOperator.cpp:2573-2641
+//   SpaceOperator::ApplyBoundaryConditions  SpaceOperator.cpp:738-821
+//   SpaceOperator::ClipDensityAndPressure   SpaceOperator.cpp:647-693
+//   SpaceOperator::ComputeTimeStepSize      SpaceOperator.cpp:1223-1330
+//   Reconstructor::Reconstruct (primitive)  Reconstructor.cpp:335-918, limiters Reconstructor.h:96-111
+//   LevelSetOperator FD residual + BCs      LevelSetOperator.cpp:796-870, 408-508
+//   GradientCalculatorFD3 coefficients      GradientCalculatorFD3.cpp:300-470
+//   TimeIntegratorFE/RK2/RK3                TimeIntegrator.cpp:167-250, 319-455, 527-715
+//   UpdateSolutionAfterTimeStepping         TimeIntegrator.cpp:720-843
+//   MultiPhaseOperator ID / state updates   MultiPhaseOperator.cpp:153-357, 919-1274
+//   Main step loop dt clamp                 Main.cpp:653-712
+// EOS, fluxes and the exact Riemann solver are in oracle_eos_flux.h and
+// oracle_riemann.h.  Compiled with -ffp-contract=off (reference order of
+// operations, no fused multiply-add) and optionally OpenMP.
+#include <cstdio>
+#include <cstring>
+#include <cstdint>
+#include <vector>
+#include <set>
+#include <map>
+#include <memory>
+#include <chrono>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+#include "oracle_riemann.h"
+
+using namespace orc;
+
+namespace {
+
+struct Counters {
+  int64_t interface_faces = 0, riemann_errors = 0, riemann_iterations = 0, riemann_solves = 0;
+  int64_t clipped_cells = 0, clipped_faces = 0, nonphysical = 0, swept_cells = 0, unresolved_cells = 0, steps = 0;
+};
+
+// Star states stored at one face (RiemannSolutions.h:12-30; SpaceOperator.cpp:1661-1666).
+struct FaceSol { bool valid = false; double Vsm[5], Vsp[5]; int idm = 0, idp = 0; };
+
+struct Oracle {
+  m2cg_config cfg;
+  int NX, NY, NZ, PX, PY, PZ;  // padded dims (ghost width 1)
+  double dx, dy, dz, vol;
+  std::vector<Eos> vf;
+  RiemannParams rp;
+  // state (ghosted, AoS for V)
+  std::vector<double> V, Phi;
+  std::vector<int> ID;
+  std::vector<FaceSol> sol[3];   // per-face stored star states, indexed by the plus cell
+  Counters cnt;
+  double time = 0.0, last_dt = 0.0, last_cfl = 0.0;
+  int time_step = 0;
+  double fd3_left[4], fd3_right[4][3];  // uniform-mesh FD3 coefficients per direction (set in setup)
+  double cl_[3][4], cr_[3][4];
+
+  size_t idx(int i, int j, int k) const { return ((size_t)(k + 1) * PY + (j + 1)) * PX + (i + 1); }
+  size_t N() const { return (size_t)PX * PY * PZ; }
+  bool outside(int i, int j, int k) const { return i < 0 || i >= NX || j < 0 || j >= NY || k < 0 || k >= NZ; }
+  int nface_ghost(int i, int j, int k) const {
+    return (i < 0 || i >= NX) + (j < 0 || j >= NY) + (k < 0 || k >= NZ);
+  }
+
+  void setup(const m2cg_config& c);
+  void ApplyBC(std::vector<double>& v);
+  void ApplyLSBC(std::vector<double>& phi);
+  void UpdateIDGhosts(std::vector<int>& id);
+  int  ClipAll(std::vector<double>& v, const std::vector<int>& id);
+  bool Reconstruct(const std::vector<double>& v, const std::vector<int>& id, std::vector<double> fs[6]);
+  void CheckReconstructed(const std::vector<double>& v, const std::vector<int>& id, std::vector<double> fs[6]);
+  void ComputeResidual(const std::vector<double>& v, const std::vector<int>& id, std::vector<double>& R, bool store);
+  void LevelSetResidual(const std::vector<double>& v, const std::vector<double>& phi, std::vector<double>& R);
+  void ComputeDt(const std::vector<double>& v, const std::vector<int>& id, double& dt, double& cfl);
+  void Advance(double dt);
+  void P2C(const std::vector<double>& v, const std::vector<int>& id, std::vector<double>& u);
+  void C2P(const std::vector<double>& u, const std::vector<int>& id, std::vector<double>& v);
+  void EndOfStep(std::vector<double>& phi0);
+  bool NumFlux(int dir, const double* Vm, const double* Vp, int id, double* F);
+};
+
+// Solve the 4x4 Taylor system of GradientCalculatorFD3.cpp:455-470 by Gaussian
+// elimination with partial pivoting.
+void TaylorCoeffs(double d0, double d1, double d2, double d3, double* c) {
+  double A[4][5] = {{1, 1, 1, 1, 0}, {d0, d1, d2, d3, 1}, {d0 * d0, d1 * d1, d2 * d2, d3 * d3, 0},
+                    {d0 * d0 * d0, d1 * d1 * d1, d2 * d2 * d2, d3 * d3 * d3, 0}};
+  for (int col = 0; col < 4; col++) {
+    int piv = col;
+    for (int r = col + 1; r < 4; r++) if (std::fabs(A[r][col]) > std::fabs(A[piv][col])) piv = r;
+    for (int k = 0; k < 5; k++) std::swap(A[col][k], A[piv][k]);
+    for (int r = col + 1; r < 4; r++) {
+      double f = A[r][col] / A[col][col];
+      for (int k = col; k < 5; k++) A[r][k] -= f * A[col][k];
+    }
+  }
+  for (int r = 3; r >= 0; r--) {
+    double s = A[r][4];
+    for (int k = r + 1; k < 4; k++) s -= A[r][k] * c[k];
+    c[r] = s / A[r][r];
+  }
+}
+
+void Oracle::setup(const m2cg_config& c) {
+  cfg = c;
+  NX = c.nx; NY = c.ny; NZ = c.nz;
+  PX = NX + 2; PY = NY + 2; PZ = NZ + 2;
+  dx = (c.xmax - c.x0) / NX; dy = (c.ymax - c.y0) / NY; dz = (c.zmax - c.z0) / NZ;  // MeshGenerator.cpp:166
+  vol = dx * dy * dz;                                                              // SpaceOperator.cpp:217
+  vf.resize(c.n_materials);
+  for (int m = 0; m < c.n_materials; m++) vf[m].setup(c.mat[m]);
+  rp.maxIts_main = c.maxits_main; rp.maxIts_bracket = c.maxits_bracket; rp.maxIts_shock = c.maxits_shock;
+  rp.numSteps_rarefaction = c.numsteps_rarefaction; rp.tol_main = c.tol_main; rp.tol_shock = c.tol_shock;
+  rp.tol_rarefaction = c.tol_rarefaction; rp.min_pressure = c.min_pressure; rp.failure_threshold = c.failure_threshold;
+  rp.pressure_at_failure = c.pressure_at_failure;
+  V.assign(N() * 5, 0.0); Phi.assign(N(), 0.0); ID.assign(N(), 0);
+  for (int d = 0; d < 3; d++) sol[d].assign(N(), FaceSol());
+  double h[3] = {dx, dy, dz};
+  for (int d = 0; d < 3; d++) {
+    // left-biased: nodes i-2, i-1, i, i+1 (GradientCalculatorFD3.cpp:318-324)
+    TaylorCoeffs(-2 * h[d], -h[d], 0.0, h[d], cl_[d]);
+    // right-biased: nodes i-1, i, i+1, i+2 (GradientCalculatorFD3.cpp:395-401)
+    TaylorCoeffs(-h[d], 0.0, h[d], 2 * h[d], cr_[d]);
+  }
+}
+
+// SpaceOperator.cpp:738-821 (FACE ghosts only; edges and corners stay untouched).
+void Oracle::ApplyBC(std::vector<double>& v) {
+  for (int k = -1; k <= NZ; k++)
+    for (int j = -1; j <= NY; j++)
+      for (int i = -1; i <= NX; i++) {
+        if (nface_ghost(i, j, k) != 1) continue;
+        int side = (i < 0) ? 0 : (i >= NX) ? 1 : (j < 0) ? 2 : (j >= NY) ? 3 : (k < 0) ? 4 : 5;
+        int ii = i < 0 ? -i - 1 : i >= NX ? NX + (i - NX) - 1 : i;   // SpaceOperator.cpp:493-519
+        int jj = j < 0 ? -j - 1 : j >= NY ? NY + (j - NY) - 1 : j;
+        int kk = k < 0 ? -k - 1 : k >= NZ ? NZ + (k - NZ) - 1 : k;
+        double* g = &v[idx(i, j, k) * 5];
+        const double* im = &v[idx(ii, jj, kk) * 5];
+        int bc = cfg.bc[side];
+        if (bc == M2CG_BC_INLET) for (int p = 0; p < 5; p++) g[p] = cfg.inlet[p];
+        else if (bc == M2CG_BC_INLET2) for (int p = 0; p < 5; p++) g[p] = cfg.inlet2[p];
+        else if (bc == M2CG_BC_SLIPWALL || bc == M2CG_BC_SYMMETRY) {
+          for (int p = 0; p < 5; p++) g[p] = im[p];
+          g[1 + side / 2] *= -1.0;
+        } else if (bc == M2CG_BC_STICKWALL) {
+          g[0] = im[0]; g[1] = -1.0 * im[1]; g[2] = -1.0 * im[2]; g[3] = -1.0 * im[3]; g[4] = im[4];
+        } else {  // OUTLET
+          for (int p = 0; p < 5; p++) g[p] = im[p];
+        }
+      }
+}
+
+// LevelSetOperator.cpp:408-508
+void Oracle::ApplyLSBC(std::vector<double>& phi) {
+  double h[3] = {dx, dy, dz};
+  for (int k = -1; k <= NZ; k++)
+    for (int j = -1; j <= NY; j++)
+      for (int i = -1; i <= NX; i++) {
+        if (nface_ghost(i, j, k) != 1) continue;
+        int side = (i < 0) ? 0 : (i >= NX) ? 1 : (j < 0) ? 2 : (j >= NY) ? 3 : (k < 0) ? 4 : 5;
+        int ii = i < 0 ? -i - 1 : i >= NX ? NX + (i - NX) - 1 : i;
+        int jj = j < 0 ? -j - 1 : j >= NY ? NY + (j - NY) - 1 : j;
+        int kk = k < 0 ? -k - 1 : k >= NZ ? NZ + (k - NZ) - 1 : k;
+        int bc = cfg.ls_bc[side];
+        double& g = phi[idx(i, j, k)];
+        if (bc == M2CG_LSBC_ZERO_NEUMANN) { g = phi[idx(ii, jj, kk)]; continue; }
+        int d = side / 2, sgn = (side % 2 == 0) ? +1 : -1;  // direction into the domain
+        int n[3] = {NX, NY, NZ};
+        int pos[3] = {i, j, k};
+        int ok = (sgn > 0) ? (pos[d] + 2 < n[d]) : (pos[d] - 2 >= 0);
+        if (ok) {
+          int p1[3] = {i, j, k}, p2[3] = {i, j, k};
+          p1[d] += sgn; p2[d] += 2 * sgn;
+          // coordinates along d (uniform): r = x0 + (pos+0.5)h
+          double lo[3] = {cfg.x0, cfg.y0, cfg.z0};
+          double r = lo[d] + 0.5 * h[d] + pos[d] * h[d];
+          double r1 = lo[d] + 0.5 * h[d] + p1[d] * h[d];
+          double r2 = lo[d] + 0.5 * h[d] + p2[d] * h[d];
+          double f1 = phi[idx(p1[0], p1[1], p1[2])], f2 = phi[idx(p2[0], p2[1], p2[2])];
+          g = f1 + (f2 - f1) / (r2 - r1) * (r - r1);
+        } else g = phi[idx(ii, jj, kk)];
+        if (bc == M2CG_LSBC_NON_NEGATIVE) {
+          double d2wall = 0.5 * h[d];  // 0.5*|x_image - x_ghost| for the first ghost layer
+          g = std::max(-d2wall, g);
+        }
+      }
+}
+
+// MultiPhaseOperator.cpp:919-942
+void Oracle::UpdateIDGhosts(std::vector<int>& id) {
+  for (int k = -1; k <= NZ; k++)
+    for (int j = -1; j <= NY; j++)
+      for (int i = -1; i <= NX; i++) {
+        if (nface_ghost(i, j, k) != 1) continue;
+        int ii = i < 0 ? -i - 1 : i >= NX ? NX + (i - NX) - 1 : i;
+        int jj = j < 0 ? -j - 1 : j >= NY ? NY + (j - NY) - 1 : j;
+        int kk = k < 0 ? -k - 1 : k >= NZ ? NZ + (k - NZ) - 1 : k;
+        id[idx(i, j, k)] = id[idx(ii, jj, kk)];
+      }
+}
+
+// SpaceOperator.cpp:647-693 (real cells)
+int Oracle::ClipAll(std::vector<double>& v, const std::vector<int>& id) {
+  int n = 0;
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < NX; i++) {
+        size_t c = idx(i, j, k);
+        n += vf[id[c]].ClipDensityAndPressure(&v[c * 5]);
+        if (vf[id[c]].CheckState(&v[c * 5])) cnt.nonphysical++;
+      }
+  return n;
+}
+
+void Oracle::P2C(const std::vector<double>& v, const std::vector<int>& id, std::vector<double>& u) {
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < NX; i++) {
+        size_t c = idx(i, j, k);
+        vf[id[c]].PrimitiveToConservative(&v[c * 5], &u[c * 5]);
+      }
+}
+void Oracle::C2P(const std::vector<double>& u, const std::vector<int>& id, std::vector<double>& v) {
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < NX; i++) {
+        size_t c = idx(i, j, k);
+        vf[id[c]].ConservativeToPrimitive(&u[c * 5], &v[c * 5]);
+      }
+}
+
+inline double GenMinMod(double A, double B, double alpha, double dq0, double dq1) {  // Reconstructor.h:96-103
+  if (dq0 < 0.0 && dq1 < 0.0) return std::max(alpha * dq0, std::max(B / (A + 1.0) * (dq0 + dq1), alpha * dq1));
+  else if (dq0 > 0.0 && dq1 > 0.0) return std::min(alpha * dq0, std::min(B / (A + 1.0) * (dq0 + dq1), alpha * dq1));
+  return 0.0;
+}
+inline double VanAlbada(double A, double B, int k, double dq0, double dq1) {  // Reconstructor.h:105-111
+  if (dq0 * dq1 <= 0) return 0.0;
+  if (std::fabs(dq0 * dq1) < 1e-16) return 0.0;
+  double a = std::pow(dq0, k), b = std::pow(dq1, k);
+  return B * (dq1 * a + dq0 * b) / (a + A * b);
+}
+
+// Reconstructor.cpp:335-918, primitive variables.  fs[0..5] = vl, vr, vb, vt, vk, vf (ghosted, AoS).
+bool Oracle::Reconstruct(const std::vector<double>& v, const std::vector<int>& id, std::vector<double> fs[6]) {
+  for (int f = 0; f < 6; f++) fs[f].assign(N() * 5, 0.0);
+  const double A = 1.0, B = 1.0;   // uniform mesh: Reconstructor.cpp:78-84 give exactly 1
+  int kay = 2;                     // CalculateSlopeLimiterCoefficientK(1,1) -> 2
+  if (cfg.limiter == M2CG_LIM_VANALBADA) {
+    for (kay = 2; kay < 1000; kay++) {
+      double rhs = 2.0 / (1.0 + std::pow((kay - 1.0) / kay, kay - 1) / kay) * std::min(A, 1.0);
+      if (B <= rhs) break;
+    }
+  }
+  double alpha = cfg.minmod_coeff;
+  int64_t sx = 5, sy = (int64_t)PX * 5, sz = (int64_t)PX * PY * 5;
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < NX; i++) {
+        size_t c = idx(i, j, k);
+        const double* q = &v[c * 5];
+        if (cfg.rec_type == M2CG_REC_CONSTANT) {
+          for (int f = 0; f < 6; f++) for (int p = 0; p < 5; p++) fs[f][c * 5 + p] = q[p];
+          continue;
+        }
+        double sig[3][5];
+        int64_t st[3] = {sx, sy, sz};
+        for (int d = 0; d < 3; d++)
+          for (int p = 0; p < 5; p++) {
+            double dq0 = q[p] - q[p - st[d]];
+            double dq1 = q[p + st[d]] - q[p];
+            double s;
+            if (cfg.limiter == M2CG_LIM_GENERALIZED_MINMOD) s = GenMinMod(A, B, alpha, dq0, dq1);
+            else if (cfg.limiter == M2CG_LIM_VANALBADA) s = VanAlbada(A, B, kay, dq0, dq1);
+            else s = 0.5 * (dq0 + dq1);
+            sig[d][p] = s;
+          }
+        if (cfg.slope_near_interface == M2CG_SLOPE_ZERO) {   // Reconstructor.cpp:649-658
+          size_t cs[3] = {1, (size_t)PX, (size_t)PX * PY};
+          for (int d = 0; d < 3; d++)
+            if (id[c] != id[c - cs[d]] || id[c] != id[c + cs[d]])
+              for (int p = 0; p < 5; p++) sig[d][p] = 0.0;
+        }
+        for (int p = 0; p < 5; p++) {   // Reconstructor.cpp:676-688
+          fs[0][c * 5 + p] = q[p] - 0.5 * sig[0][p];
+          fs[1][c * 5 + p] = q[p] + 0.5 * sig[0][p];
+          fs[2][c * 5 + p] = q[p] - 0.5 * sig[1][p];
+          fs[3][c * 5 + p] = q[p] + 0.5 * sig[1][p];
+          fs[4][c * 5 + p] = q[p] - 0.5 * sig[2][p];
+          fs[5][c * 5 + p] = q[p] + 0.5 * sig[2][p];
+        }
+        // Reconstructor.cpp:722-778: the first nonphysical face reverts to the cell value
+        const Eos& e = vf[id[c]];
+        for (int f = 0; f < 6; f++) {
+          if (e.CheckState(&fs[f][c * 5])) {
+            for (int p = 0; p < 5; p++) fs[f][c * 5 + p] = q[p];
+            break;
+          }
+        }
+      }
+  // Ghost faces by boundary condition, Reconstructor.cpp:807-889
+  for (int k = -1; k <= NZ; k++)
+    for (int j = -1; j <= NY; j++)
+      for (int i = -1; i <= NX; i++) {
+        if (nface_ghost(i, j, k) != 1) continue;
+        int side = (i < 0) ? 0 : (i >= NX) ? 1 : (j < 0) ? 2 : (j >= NY) ? 3 : (k < 0) ? 4 : 5;
+        int ii = i < 0 ? -i - 1 : i >= NX ? NX + (i - NX) - 1 : i;
+        int jj = j < 0 ? -j - 1 : j >= NY ? NY + (j - NY) - 1 : j;
+        int kk = k < 0 ? -k - 1 : k >= NZ ? NZ + (k - NZ) - 1 : k;
+        size_t g = idx(i, j, k), im = idx(ii, jj, kk);
+        int inward = side ^ 1;      // face state of the ghost facing the domain: vr for the x0 ghost, ...
+        int src = side;             // face state of the image on the boundary: vl of the image for x0
+        int bc = cfg.bc[side];
+        double* dst = &fs[inward][g * 5];
+        if (bc == M2CG_BC_INLET || bc == M2CG_BC_INLET2) {
+          for (int p = 0; p < 5; p++) dst[p] = v[g * 5 + p];
+        } else if (bc == M2CG_BC_OUTLET) {
+          for (int p = 0; p < 5; p++) dst[p] = fs[src][im * 5 + p];
+        } else if (bc == M2CG_BC_SYMMETRY || bc == M2CG_BC_SLIPWALL) {
+          for (int p = 0; p < 5; p++) dst[p] = fs[src][im * 5 + p];
+          dst[1 + side / 2] *= -1.0;
+        } else {  // STICKWALL: copyarray_flip(.., 1, 3) flips all three velocity components
+          for (int p = 0; p < 5; p++) dst[p] = fs[src][im * 5 + p];
+          dst[1] *= -1.0; dst[2] *= -1.0; dst[3] *= -1.0;
+        }
+      }
+  return true;
+}
+
+// SpaceOperator.cpp:2420-2569
+void Oracle::CheckReconstructed(const std::vector<double>& v, const std::vector<int>& id, std::vector<double> fs[6]) {
+  int64_t nclip = 0, nbad = 0;
+#pragma omp parallel for schedule(static) reduction(+ : nclip, nbad)
+  for (int k = -1; k <= NZ; k++)
+    for (int j = -1; j <= NY; j++)
+      for (int i = -1; i <= NX; i++) {
+        int boundary = (k == -1 || k == NZ) + (j == -1 || j == NY) + (i == -1 || i == NX);
+        if (boundary >= 2) continue;
+        size_t c = idx(i, j, k);
+        const Eos& e = vf[id[c]];
+        auto clip_one = [&](int f) {
+          double* s = &fs[f][c * 5];
+          double tmp[5];
+          for (int p = 0; p < 5; p++) tmp[p] = s[p];
+          if (e.ClipDensityAndPressure(tmp)) {
+            for (int p = 0; p < 5; p++) s[p] = v[c * 5 + p];
+            nclip++;
+          }
+          if (e.CheckState(s)) nbad++;
+        };
+        if (boundary == 0) { for (int f = 0; f < 6; f++) clip_one(f); }
+        else {
+          if (i == -1) clip_one(1);
+          else if (i == NX) clip_one(0);
+          else if (j == -1) clip_one(3);
+          else if (j == NY) clip_one(2);
+          else if (k == -1) clip_one(5);
+          else if (k == NZ) clip_one(4);
+        }
+      }
+  cnt.clipped_faces += nclip;
+  cnt.nonphysical += nbad;
+}
+
+bool Oracle::NumFlux(int dir, const double* Vm, const double* Vp, int id, double* F) {
+  if (cfg.flux == M2CG_FLUX_HLLC) return FluxHLLC(vf[id], dir, Vm, Vp, F);
+  if (cfg.flux == M2CG_FLUX_LLF) return FluxLLF2(vf[id], vf[id], dir, Vm, Vp, F);
+  return FluxGenRoe(vf[id], dir, Vm, Vp, cfg.roe_delta, F);
+}
+
+// SpaceOperator.cpp:1432-2076 then 2573-2641.  R is ghosted AoS; only real cells are meaningful.
+void Oracle::ComputeResidual(const std::vector<double>& v, const std::vector<int>& id, std::vector<double>& R, bool store) {
+  std::vector<double> fs[6];
+  Reconstruct(v, id, fs);
+  CheckReconstructed(v, id, fs);
+  if (store) for (int d = 0; d < 3; d++) for (auto& s : sol[d]) s.valid = false;
+  // Per-face fluxes: lf1 goes to the minus cell, lf2 to the plus cell.  Face d of
+  // cell c (plus cell) sits between c - e_d and c.
+  std::vector<double> lf1[3], lf2[3];
+  for (int d = 0; d < 3; d++) { lf1[d].assign(N() * 5, 0.0); lf2[d].assign(N() * 5, 0.0); }
+  size_t cs[3] = {1, (size_t)PX, (size_t)PX * PY};
+  int64_t n_if = 0, n_err = 0, n_iter = 0, n_solve = 0;
+#pragma omp parallel reduction(+ : n_if, n_err, n_iter, n_solve)
+  {
+    ExactRiemann riemann(vf, rp);
+    Counters local;
+#pragma omp for schedule(dynamic, 1)
+    for (int k = 0; k <= NZ; k++)
+      for (int j = 0; j <= NY; j++)
+        for (int i = 0; i <= NX; i++) {
+          int lim[3] = {(k != NZ && j != NY), (k != NZ && i != NX), (j != NY && i != NX)};
+          size_t c = idx(i, j, k);
+          int myid = id[c];
+          for (int d = 0; d < 3; d++) {
+            if (!lim[d]) continue;
+            size_t m = c - cs[d];
+            int nid = id[m];
+            double* L1 = &lf1[d][c * 5];
+            double* L2 = &lf2[d][c * 5];
+            const double* vm_face = &fs[2 * d + 1][m * 5];   // vr / vt / vf of the minus cell
+            const double* vp_face = &fs[2 * d][c * 5];       // vl / vb / vk of the plus cell
+            if (nid != myid) {
+              n_if++;
+              const double* Vm = (cfg.mp_recon == M2CG_MPREC_CONSTANT) ? &v[m * 5] : vm_face;
+              const double* Vp = (cfg.mp_recon == M2CG_MPREC_CONSTANT) ? &v[c * 5] : vp_face;
+              if (cfg.mp_flux == M2CG_MPFLUX_LLF) {   // SpaceOperator.cpp:1617-1626
+                FluxLLF2(vf[nid], vf[myid], d, Vm, Vp, L1);
+                for (int p = 0; p < 5; p++) L2[p] = L1[p];
+              } else {
+                double dirv[3] = {0, 0, 0};
+                dirv[d] = 1.0;  // RiemannNormal = Mesh (SpaceOperator.cpp:2186-2203)
+                double Vmid[5], Vsm[5], Vsp[5];
+                int midid = 0;
+                int err = riemann.Solve(dirv, Vm, nid, Vp, myid, Vmid, midid, Vsm, Vsp);
+                n_solve++;
+                n_iter += riemann.evals;
+                if (err) n_err++;
+                vf[nid].ClipDensityAndPressure(Vsm);
+                if (vf[nid].CheckState(Vsm)) local.nonphysical++;
+                vf[myid].ClipDensityAndPressure(Vsp);
+                if (vf[myid].CheckState(Vsp)) local.nonphysical++;
+                if (store && !err) {
+                  FaceSol& s = sol[d][c];
+                  s.valid = true;
+                  for (int p = 0; p < 5; p++) { s.Vsm[p] = Vsm[p]; s.Vsp[p] = Vsp[p]; }
+                  s.idm = nid; s.idp = myid;
+                }
+                if (cfg.mp_flux == M2CG_MPFLUX_EXACT) {
+                  EvaluateFlux(vf[midid], d, Vmid, L1);
+                  for (int p = 0; p < 5; p++) L2[p] = L1[p];
+                } else {
+                  if (!NumFlux(d, Vm, Vsm, nid, L1)) local.nonphysical++;
+                  if (!NumFlux(d, Vsp, Vp, myid, L2)) local.nonphysical++;
+                }
+              }
+            } else {
+              if (!NumFlux(d, vm_face, vp_face, myid, L1)) local.nonphysical++;
+              for (int p = 0; p < 5; p++) L2[p] = L1[p];
+            }
+          }
+        }
+#pragma omp critical
+    cnt.nonphysical += local.nonphysical;
+  }
+  cnt.interface_faces += n_if;
+  cnt.riemann_errors += n_err;
+  cnt.riemann_iterations += n_iter;
+  cnt.riemann_solves += n_solve;
+  // Gather in the reference's accumulation order: -x, -y, -z faces, then +x, +y, +z.
+  R.assign(N() * 5, 0.0);
+  double area[3] = {dy * dz, dx * dz, dx * dy};
+  double inv = 1.0 / (-vol);   // Vector5D.h:174-183 (r /= -vol multiplies by the reciprocal)
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < NX; i++) {
+        size_t c = idx(i, j, k);
+        double f[5] = {0, 0, 0, 0, 0};
+        for (int d = 0; d < 3; d++)
+          for (int p = 0; p < 5; p++) f[p] -= lf2[d][c * 5 + p] * area[d];
+        for (int d = 0; d < 3; d++)
+          for (int p = 0; p < 5; p++) f[p] += lf1[d][(c + cs[d]) * 5 + p] * area[d];
+        for (int p = 0; p < 5; p++) R[c * 5 + p] = f[p] * inv;
+      }
+}
+
+// LevelSetOperator.cpp:796-870 (full domain, finite difference)
+void Oracle::LevelSetResidual(const std::vector<double>& v, const std::vector<double>& phi, std::vector<double>& R) {
+  R.assign(N(), 0.0);
+  double h[3] = {dx, dy, dz};
+  size_t cs[3] = {1, (size_t)PX, (size_t)PX * PY};
+  int n[3] = {NX, NY, NZ};
+#pragma omp parallel for schedule(static)
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < NX; i++) {
+        size_t c = idx(i, j, k);
+        int pos[3] = {i, j, k};
+        double res = 0.0;
+        double term[3];
+        for (int d = 0; d < 3; d++) {
+          size_t s = cs[d];
+          // left-biased derivative (a, c, e): 3rd order if pos >= 1, else one-sided first order
+          double gm, gp;
+          if (pos[d] - 2 >= -1)
+            gm = cl_[d][0] * phi[c - 2 * s] + cl_[d][1] * phi[c - s] + cl_[d][2] * phi[c] + cl_[d][3] * phi[c + s];
+          else
+            gm = (phi[c] - phi[c - s]) / h[d];
+          // right-biased (b, d, f): 3rd order if pos + 2 <= N.  The reference's
+          // right-biased y coefficients are 3rd order only when i < NY-1
+          // (GradientCalculatorFD3.cpp:409, tests i instead of j).
+          bool third = (pos[d] + 2 <= n[d]);
+          if (third) {
+            bool coeff3 = (d == 1) ? (i < NY - 1) : (pos[d] < n[d] - 1);
+            if (coeff3)
+              gp = cr_[d][0] * phi[c - s] + cr_[d][1] * phi[c] + cr_[d][2] * phi[c + s] + cr_[d][3] * phi[c + 2 * s];
+            else
+              gp = 0.0 * phi[c - s] + (-1.0 / h[d]) * phi[c] + (1.0 / h[d]) * phi[c + s] + 0.0 * phi[c + 2 * s];
+          } else
+            gp = (phi[c + s] - phi[c]) / h[d];
+          double vel = v[c * 5 + 1 + d];
+          term[d] = (vel >= 0 ? gm * vel : gp * vel);
+        }
+        res = term[0] + term[1] + term[2];
+        R[c] = res * -1.0;
+      }
+}
+
+// SpaceOperator.cpp:1223-1330
+void Oracle::ComputeDt(const std::vector<double>& v, const std::vector<int>& id, double& dt, double& cfl) {
+  double m = DBL_MAX;
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < NX; i++) {
+        size_t c = idx(i, j, k);
+        const double* q = &v[c * 5];
+        const Eos& e = vf[id[c]];
+        double cc = e.ComputeSoundSpeedSquare(q[0], e.GetInternalEnergyPerUnitMass(q[0], q[4]));
+        cc = std::sqrt(std::max(cc, 0.0));
+        // FluxFcnBase::EvaluateMaxEigenvalues (FluxFcnBase.h:286-303) recomputes c the same way
+        double lf = std::fabs(q[1]) + cc, lg = std::fabs(q[2]) + cc, lh = std::fabs(q[3]) + cc;
+        if (NX > 1) m = std::min(m, dx / lf);
+        if (NY > 1) m = std::min(m, dy / lg);
+        if (NZ > 1) m = std::min(m, dz / lh);
+      }
+  if (cfg.timestep > 0) { dt = cfg.timestep; cfl = dt / m; }
+  else { cfl = cfg.cfl; dt = cfl * m; }
+}
+
+void Oracle::Advance(double dt) {
+  // TimeIntegrator.cpp:333-339: Phi_tmp = Phi (including ghosts)
+  std::vector<double> phi0 = Phi;
+  size_t n5 = N() * 5;
+  std::vector<double> R, Un(n5, 0.0), U1(n5, 0.0), V1 = V, V2, Rls, Phi1 = Phi;
+  bool ls = cfg.n_levelsets > 0;
+  int64_t nclip = 0;
+  auto axpby = [&](std::vector<double>& x, double a, double b, const std::vector<double>& y, int dof) {
+    for (int k = 0; k < NZ; k++)
+      for (int j = 0; j < NY; j++)
+        for (int i = 0; i < NX; i++) {
+          size_t c = idx(i, j, k);
+          for (int p = 0; p < dof; p++) x[c * dof + p] = a * x[c * dof + p] + b * y[c * dof + p];
+        }
+  };
+  // Stage 1 (all schemes): U1 = Un + dt R(V)
+  ComputeResidual(V, ID, R, true);
+  P2C(V, ID, Un);
+  axpby(U1, 0.0, 1.0, Un, 5);
+  axpby(U1, 1.0, dt, R, 5);
+  if (cfg.ts_type == M2CG_TS_FORWARD_EULER) {  // TimeIntegrator.cpp:167-250
+    C2P(U1, ID, V);
+    nclip += ClipAll(V, ID);
+    ApplyBC(V);
+    if (ls) {
+      LevelSetResidual(V, Phi, Rls);   // FE uses the updated V (TimeIntegrator.cpp:215)
+      axpby(Phi, 1.0, dt, Rls, 1);
+      ApplyLSBC(Phi);
+    }
+  } else {
+    C2P(U1, ID, V1);
+    int clipped = ClipAll(V1, ID);
+    nclip += clipped;
+    if (clipped) P2C(V1, ID, U1);
+    ApplyBC(V1);
+    if (ls) {
+      LevelSetResidual(V, Phi, Rls);
+      axpby(Phi1, 0.0, 1.0, Phi, 1);
+      axpby(Phi1, 1.0, dt, Rls, 1);
+      ApplyLSBC(Phi1);
+    }
+    if (cfg.ts_type == M2CG_TS_RK2) {  // TimeIntegrator.cpp:400-428
+      ComputeResidual(V1, ID, R, false);
+      axpby(U1, 0.5, 0.5, Un, 5);
+      axpby(U1, 1.0, 0.5 * dt, R, 5);
+      C2P(U1, ID, V);
+      nclip += ClipAll(V, ID);
+      ApplyBC(V);
+      if (ls) {
+        LevelSetResidual(V1, Phi1, Rls);
+        axpby(Phi, 0.5, 0.5, Phi1, 1);
+        axpby(Phi, 1.0, 0.5 * dt, Rls, 1);
+        ApplyLSBC(Phi);
+      }
+    } else {  // RK3, TimeIntegrator.cpp:602-680
+      ComputeResidual(V1, ID, R, false);
+      axpby(U1, 0.25, 0.75, Un, 5);
+      axpby(U1, 1.0, 0.25 * dt, R, 5);
+      V2 = V1;
+      C2P(U1, ID, V2);
+      clipped = ClipAll(V2, ID);
+      nclip += clipped;
+      if (clipped) P2C(V2, ID, U1);
+      ApplyBC(V2);
+      if (ls) {
+        LevelSetResidual(V1, Phi1, Rls);
+        axpby(Phi1, 0.25, 0.75, Phi, 1);
+        axpby(Phi1, 1.0, 0.25 * dt, Rls, 1);
+        ApplyLSBC(Phi1);
+      }
+      ComputeResidual(V2, ID, R, false);
+      axpby(U1, 2.0 / 3.0, 1.0 / 3.0, Un, 5);
+      axpby(U1, 1.0, 2.0 / 3.0 * dt, R, 5);
+      C2P(U1, ID, V);
+      nclip += ClipAll(V, ID);
+      ApplyBC(V);
+      if (ls) {
+        LevelSetResidual(V2, Phi1, Rls);
+        axpby(Phi, 1.0 / 3.0, 2.0 / 3.0, Phi1, 1);
+        axpby(Phi, 1.0, 2.0 / 3.0 * dt, Rls, 1);
+        ApplyLSBC(Phi);
+      }
+    }
+  }
+  cnt.clipped_cells += nclip;
+  if (ls) EndOfStep(phi0);
+  cnt.steps++;
+}
+
+// TimeIntegrator.cpp:720-843 with MultiPhaseOperator.cpp:153-357, 947-1274.
+void Oracle::EndOfStep(std::vector<double>& phi0) {
+  std::vector<int> IDn = ID;
+  int lsmat = cfg.ls_matid;
+  // UpdateMaterialIDByLevelSet (one level set)
+  std::vector<char> tag(N(), 0);
+  std::vector<std::array<int, 3>> remaining;
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < NX; i++) {
+        size_t c = idx(i, j, k);
+        if (Phi[c] * phi0[c] > 0.0) continue;
+        if (Phi[c] < 0) ID[c] = lsmat;
+        else { tag[c] = 1; remaining.push_back({i, j, k}); }
+      }
+  for (int iter = 0; iter < 100 && !remaining.empty(); iter++) {
+    int progress = 0;
+    auto tmp = remaining;
+    std::vector<std::array<int, 3>> still;
+    std::set<std::array<int, 3>> done;
+    // the reference walks a std::set<Int3> ordered by (i, j, k) components
+    std::sort(tmp.begin(), tmp.end());
+    for (auto& p : tmp) {
+      int i = p[0], j = p[1], k = p[2];
+      std::set<int> cands;
+      for (int nk = k - 1; nk <= k + 1; nk++)
+        for (int nj = j - 1; nj <= j + 1; nj++)
+          for (int ni = i - 1; ni <= i + 1; ni++) {
+            if (outside(ni, nj, nk)) continue;
+            size_t nc = idx(ni, nj, nk);
+            if (tag[nc] == 1) continue;
+            int nid = ID[nc];
+            if (nid == lsmat) continue;
+            cands.insert(nid);
+          }
+      if (cands.empty()) continue;
+      size_t c = idx(i, j, k);
+      ID[c] = *cands.begin();
+      tag[c] = 0;
+      done.insert(p);
+      progress++;
+    }
+    for (auto& p : remaining) if (!done.count(p)) still.push_back(p);
+    remaining.swap(still);
+    if (progress == 0) {
+      for (auto& p : tmp) ID[idx(p[0], p[1], p[2])] = 0;
+      remaining.clear();
+      break;
+    }
+  }
+  UpdateIDGhosts(ID);
+  // UpdateStateVariablesAfterInterfaceMotion
+  std::vector<std::array<int, 3>> unresolved;
+  std::vector<double> Vold = V;
+  size_t cs[3] = {1, (size_t)PX, (size_t)PX * PY};
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < NX; i++) {
+        size_t c = idx(i, j, k);
+        if (ID[c] == IDn[c]) continue;
+        cnt.swept_cells++;
+        int myid = ID[c];
+        if (cfg.mp_phasechange == M2CG_PHASECHANGE_RIEMANN) {
+          // LocalUpdateByRiemannSolutions, MultiPhaseOperator.cpp:1039-1150 (upwind, then not)
+          int counter = 0;
+          for (int pass = 0; pass < 2 && counter == 0; pass++) {
+            bool upwind = (pass == 0);
+            double acc[5] = {0, 0, 0, 0, 0};
+            double sum_weight = 0;
+            for (int d = 0; d < 3; d++)
+              for (int side = 0; side < 2; side++) {
+                // side 0: face at c - e_d (left/bottom/back entry: Vsm, id of the minus cell)
+                // side 1: face at c + e_d (right/top/front entry: Vsp, id of the plus cell)
+                size_t fc = side == 0 ? c : c + cs[d];
+                const FaceSol& s = sol[d][fc];
+                if (!s.valid) continue;
+                int sid = side == 0 ? s.idm : s.idp;
+                const double* sv = side == 0 ? s.Vsm : s.Vsp;
+                size_t nb = side == 0 ? c - cs[d] : c + cs[d];
+                const double* vn = &V[nb * 5];
+                double vel = vn[1 + d];
+                bool upw_ok = side == 0 ? (vel > 0) : (vel < 0);
+                if (sid != myid || (upwind && !upw_ok)) continue;
+                double nrm = std::sqrt(vn[1] * vn[1] + vn[2] * vn[2] + vn[3] * vn[3]);
+                double weight = upwind ? (side == 0 ? vel / nrm : -vel / nrm) : 1.0;
+                sum_weight += weight;
+                for (int p = 0; p < 5; p++) {
+                  if (counter == 0) acc[p] = weight * sv[p];
+                  else acc[p] += weight * sv[p];
+                }
+                counter++;
+              }
+            if (counter > 0) {
+              double* dst = &V[c * 5];
+              if (sum_weight > 0.0) { double inv = 1.0 / sum_weight; for (int p = 0; p < 5; p++) dst[p] = acc[p] * inv; }
+              else for (int p = 0; p < 5; p++) dst[p] = acc[p];
+            }
+          }
+          if (counter == 0) unresolved.push_back({i, j, k});
+        } else {
+          // UpdateStateVariablesByExtrapolation, MultiPhaseOperator.cpp:1155-1274
+          double sum_weight = 0.0, vsum[5] = {0, 0, 0, 0, 0};
+          double hx[3] = {dx, dy, dz};
+          for (int nk = k - 1; nk <= k + 1; nk++)
+            for (int nj = j - 1; nj <= j + 1; nj++)
+              for (int ni = i - 1; ni <= i + 1; ni++) {
+                size_t nc = idx(ni, nj, nk);
+                if (ID[nc] != ID[c]) continue;
+                if (ID[nc] != IDn[nc]) continue;
+                if (outside(ni, nj, nk)) continue;
+                double x1x0[3] = {(i - ni) * hx[0], (j - nj) * hx[1], (k - nk) * hx[2]};
+                double dist = std::sqrt(x1x0[0] * x1x0[0] + x1x0[1] * x1x0[1] + x1x0[2] * x1x0[2]);
+                double weight;
+                if (cfg.mp_phasechange_dir == M2CG_PCDIR_ALL) weight = 1.0 / dist;
+                else {
+                  const double* q = &V[nc * 5];
+                  double v1[3] = {q[1], q[2], q[3]};
+                  double v1n = std::sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+                  if (v1n != 0) for (int m = 0; m < 3; m++) v1[m] /= v1n;
+                  for (int m = 0; m < 3; m++) x1x0[m] /= dist;
+                  weight = std::max(0.0, x1x0[0] * v1[0] + x1x0[1] * v1[1] + x1x0[2] * v1[2]);
+                }
+                if (weight > 0) {
+                  sum_weight += weight;
+                  for (int p = 0; p < 5; p++) vsum[p] += weight * V[nc * 5 + p];
+                }
+              }
+          if (sum_weight == 0) unresolved.push_back({i, j, k});
+          else for (int p = 0; p < 5; p++) V[c * 5 + p] = vsum[p] / sum_weight;  // Vector5D.h:190-200
+        }
+      }
+  cnt.unresolved_cells += (int64_t)unresolved.size();
+  // Unresolved cells: the reference reinitializes phi here, which needs a
+  // configured reinitializer (TimeIntegrator.cpp:776-797); without one it
+  // stops.  The oracle counts them and leaves their state as advected.
+  ClipAll(V, ID);
+  ApplyBC(V);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+// C API for the tests (ctypes).
+extern "C" {
+
+void* orc_create(const m2cg_config* cfg) {
+  Oracle* o = new Oracle();
+  o->setup(*cfg);
+  return o;
+}
+void orc_destroy(void* h) { delete (Oracle*)h; }
+
+void orc_set_threads(int n) {
+#ifdef _OPENMP
+  omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+}
+int orc_max_threads() {
+#ifdef _OPENMP
+  return omp_get_max_threads();
+#else
+  return 1;
+#endif
+}
+
+void orc_upload(void* h, const double* V, const int32_t* id, const double* phi) {
+  Oracle* o = (Oracle*)h;
+  size_t n = 0;
+  for (int k = 0; k < o->NZ; k++)
+    for (int j = 0; j < o->NY; j++)
+      for (int i = 0; i < o->NX; i++, n++) {
+        size_t c = o->idx(i, j, k);
+        for (int p = 0; p < 5; p++) o->V[c * 5 + p] = V[n * 5 + p];
+        o->ID[c] = id[n];
+        if (phi) o->Phi[c] = phi[n];
+      }
+  o->UpdateIDGhosts(o->ID);
+  o->ApplyBC(o->V);
+  if (o->cfg.n_levelsets > 0) o->ApplyLSBC(o->Phi);
+}
+
+void orc_download(void* h, double* V, int32_t* id, double* phi) {
+  Oracle* o = (Oracle*)h;
+  size_t n = 0;
+  for (int k = 0; k < o->NZ; k++)
+    for (int j = 0; j < o->NY; j++)
+      for (int i = 0; i < o->NX; i++, n++) {
+        size_t c = o->idx(i, j, k);
+        if (V) for (int p = 0; p < 5; p++) V[n * 5 + p] = o->V[c * 5 + p];
+        if (id) id[n] = o->ID[c];
+        if (phi) phi[n] = o->Phi[c];
+      }
+}
+
+void orc_residual(void* h, double* Rout) {
+  Oracle* o = (Oracle*)h;
+  std::vector<double> R;
+  o->ComputeResidual(o->V, o->ID, R, true);
+  size_t n = 0;
+  for (int k = 0; k < o->NZ; k++)
+    for (int j = 0; j < o->NY; j++)
+      for (int i = 0; i < o->NX; i++, n++)
+        for (int p = 0; p < 5; p++) Rout[n * 5 + p] = R[o->idx(i, j, k) * 5 + p];
+}
+
+void orc_levelset_residual(void* h, double* Rout) {
+  Oracle* o = (Oracle*)h;
+  std::vector<double> R;
+  o->LevelSetResidual(o->V, o->Phi, R);
+  size_t n = 0;
+  for (int k = 0; k < o->NZ; k++)
+    for (int j = 0; j < o->NY; j++)
+      for (int i = 0; i < o->NX; i++, n++) Rout[n] = R[o->idx(i, j, k)];
+}
+
+void orc_compute_dt(void* h, double* dt, double* cfl) {
+  Oracle* o = (Oracle*)h;
+  o->ComputeDt(o->V, o->ID, *dt, *cfl);
+}
+
+void orc_advance(void* h, double dt) {
+  Oracle* o = (Oracle*)h;
+  o->time_step++;
+  o->time += dt;
+  o->last_dt = dt;
+  o->Advance(dt);
+}
+
+// Main.cpp:653-712 for n steps; returns steps taken.
+int orc_run(void* h, int nsteps) {
+  Oracle* o = (Oracle*)h;
+  int s = 0;
+  double tmax = o->cfg.max_time;
+  for (; s < nsteps; s++) {
+    double dt, cfl;
+    o->ComputeDt(o->V, o->ID, dt, cfl);
+    if (!(o->time < tmax - 1.0e-6 * dt)) break;
+    if (o->time + dt > tmax) { cfl *= (tmax - o->time) / dt; dt = tmax - o->time; }
+    o->last_cfl = cfl;
+    orc_advance(h, dt);
+  }
+  return s;
+}
+
+void orc_counters(void* h, m2cg_counters* c) {
+  Oracle* o = (Oracle*)h;
+  std::memset(c, 0, sizeof(*c));
+  c->interface_faces = o->cnt.interface_faces;
+  c->riemann_errors = o->cnt.riemann_errors;
+  c->riemann_iterations = o->cnt.riemann_iterations;
+  c->riemann_solves = o->cnt.riemann_solves;
+  c->clipped_cells = o->cnt.clipped_cells;
+  c->clipped_faces = o->cnt.clipped_faces;
+  c->nonphysical = o->cnt.nonphysical;
+  c->swept_cells = o->cnt.swept_cells;
+  c->unresolved_cells = o->cnt.unresolved_cells;
+  c->steps = o->cnt.steps;
+  c->time = o->time;
+  c->dt = o->last_dt;
+  c->cfl = o->last_cfl;
+}
+
+void orc_conserved_totals(void* h, double* tot) {
+  Oracle* o = (Oracle*)h;
+  for (int p = 0; p < 5; p++) tot[p] = 0.0;
+  for (int k = 0; k < o->NZ; k++)
+    for (int j = 0; j < o->NY; j++)
+      for (int i = 0; i < o->NX; i++) {
+        size_t c = o->idx(i, j, k);
+        double U[5];
+        o->vf[o->ID[c]].PrimitiveToConservative(&o->V[c * 5], U);
+        for (int p = 0; p < 5; p++) tot[p] += U[p] * o->vol;
+      }
+}
+
+// Batched exact Riemann solves (ExactRiemannSolverBase.cpp:59-347).
+void orc_riemann_batch(const m2cg_config* cfg, int64_t n, const double* Vm, const int32_t* idm, const double* Vp,
+                       const int32_t* idp, const double* dir, double* Vs, int32_t* id, double* Vsm, double* Vsp,
+                       int32_t* iters, int32_t* err, const double* warm_p) {
+  std::vector<Eos> vf(cfg->n_materials);
+  for (int m = 0; m < cfg->n_materials; m++) vf[m].setup(cfg->mat[m]);
+  RiemannParams rp;
+  rp.maxIts_main = cfg->maxits_main; rp.maxIts_bracket = cfg->maxits_bracket; rp.maxIts_shock = cfg->maxits_shock;
+  rp.numSteps_rarefaction = cfg->numsteps_rarefaction; rp.tol_main = cfg->tol_main; rp.tol_shock = cfg->tol_shock;
+  rp.tol_rarefaction = cfg->tol_rarefaction; rp.min_pressure = cfg->min_pressure;
+  rp.failure_threshold = cfg->failure_threshold; rp.pressure_at_failure = cfg->pressure_at_failure;
+#pragma omp parallel
+  {
+    ExactRiemann rs(vf, rp);
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t q = 0; q < n; q++) {
+      int oid = 0;
+      rs.warm_p = warm_p ? warm_p[q] : 0.0;
+      int e = rs.Solve(&dir[q * 3], &Vm[q * 5], idm[q], &Vp[q * 5], idp[q], &Vs[q * 5], oid, &Vsm[q * 5], &Vsp[q * 5]);
+      id[q] = oid;
+      if (iters) iters[q] = rs.evals;
+      if (err) err[q] = e;
+    }
+  }
+}
+
+// Batched numerical fluxes (FluxFcnHLLC.h:196-245, FluxFcnLLF.h:80-111, FluxFcnGenRoe.h:183-213).
+void orc_flux_batch(const m2cg_config* cfg, int64_t n, const int32_t* dir, const double* Vm, const double* Vp,
+                    const int32_t* id, double* F) {
+  std::vector<Eos> vf(cfg->n_materials);
+  for (int m = 0; m < cfg->n_materials; m++) vf[m].setup(cfg->mat[m]);
+  for (int64_t q = 0; q < n; q++) {
+    const Eos& e = vf[id[q]];
+    if (cfg->flux == M2CG_FLUX_HLLC) FluxHLLC(e, dir[q], &Vm[q * 5], &Vp[q * 5], &F[q * 5]);
+    else if (cfg->flux == M2CG_FLUX_LLF) FluxLLF2(e, e, dir[q], &Vm[q * 5], &Vp[q * 5], &F[q * 5]);
+    else FluxGenRoe(e, dir[q], &Vm[q * 5], &Vp[q * 5], cfg->roe_delta, &F[q * 5]);
+  }
+}
+
+}  // extern "C"

@@ -1,0 +1,170 @@
+"""GPU parity against the oracle, through the C ABI.
+
+Tolerances: the product's numbers must match the oracle within 1e-10 relative
+L-infinity (max|a-b| / max|b| per variable) after one step and within 1e-8
+after 100 steps.  Integer outputs (material IDs, Riemann error codes) must be
+identical."""
+import numpy as np
+import pytest
+
+from helpers import config_for_materials, golden_problem, golden_riemann_cases, rel_linf, random_sg_states
+from m2c_gb300 import abi, problems
+from m2c_gb300.solver import FluidState, Solver
+from oracle import binding as ob
+
+pytestmark = pytest.mark.gpu
+TOL1 = 1e-10
+TOL100 = 1e-8
+
+
+def _pair(cfg, V, ID, phi):
+    s = Solver(cfg, FluidState(V, ID, phi))
+    o = ob.OracleSim(cfg)
+    o.upload(V, ID, phi)
+    return s, o
+
+
+def test_riemann_golden_cases_match_oracle():
+    for case in golden_riemann_cases():
+        cfg = config_for_materials(case["materials"], tol=1e-10)
+        Vm, idm, Vp, idp, d = golden_problem(case)
+        s = Solver(cfg)
+        g = s.riemann_batch(Vm, idm, Vp, idp, d)
+        o = ob.riemann_batch(cfg, Vm, idm, Vp, idp, d)
+        assert g["err"][0] == o["err"][0] == 0, case["test"]
+        assert g["id"][0] == o["id"][0]
+        for k in ("Vsm", "Vsp", "Vs"):
+            np.testing.assert_allclose(g[k], o[k], rtol=1e-12, atol=0, err_msg=case["test"] + k)
+
+
+def test_riemann_random_batch_matches_oracle():
+    rng = np.random.default_rng(3)
+    cfg = abi.default_config()
+    cfg.n_materials = 3
+    abi.set_material(cfg.mat[0], abi.EOS_SG, gamma=6.12, pc=3.43e8)
+    abi.set_material(cfg.mat[1], abi.EOS_SG, gamma=1.4, pc=0.0)
+    abi.set_material(cfg.mat[2], abi.EOS_NASG, gamma=1.19, pc=6.2e8, b=6.61e-4, q=0.0)
+    cfg.tol_main = 1e-10
+    n = 4096
+    Vm, Vp = random_sg_states(rng, n), random_sg_states(rng, n)
+    idm = rng.integers(0, 3, n).astype(np.int32)
+    idp = rng.integers(0, 3, n).astype(np.int32)
+    for V, ids in ((Vm, idm), (Vp, idp)):
+        sel = (ids == 2) & (V[:, 0] * 6.61e-4 > 0.5)
+        V[sel, 0] = rng.uniform(50, 700, sel.sum())
+    dirs = np.zeros((n, 3))
+    dirs[np.arange(n), rng.integers(0, 3, n)] = 1.0
+    g = Solver(cfg).riemann_batch(Vm, idm, Vp, idp, dirs)
+    o = ob.riemann_batch(cfg, Vm, idm, Vp, idp, dirs)
+    np.testing.assert_array_equal(g["err"], o["err"])
+    ok = o["err"] == 0
+    assert ok.mean() > 0.95
+    np.testing.assert_array_equal(g["id"][ok], o["id"][ok])
+    # same algorithm in binary64 without contraction on both sides: agreement
+    # is at rounding level except where a pow() ulp moves an adaptive step
+    for k in ("Vsm", "Vsp"):
+        r = np.abs(g[k][ok] - o[k][ok]) / np.maximum(np.abs(o[k][ok]), 1e-300)
+        assert np.quantile(r[:, 4], 0.99) < 1e-11
+        assert (r[:, [0, 4]] > 1e-10).mean() < 0.002
+    assert (np.abs(g["iters"][ok] - o["iters"][ok]) <= 2).mean() > 0.99
+
+
+@pytest.mark.parametrize("flux", [abi.FLUX_HLLC, abi.FLUX_LLF, abi.FLUX_ROE])
+def test_flux_batch_matches_oracle(flux):
+    rng = np.random.default_rng(5 + flux)
+    cfg = abi.default_config()
+    cfg.n_materials = 2
+    abi.set_material(cfg.mat[0], abi.EOS_SG, gamma=6.12, pc=3.43e8)
+    abi.set_material(cfg.mat[1], abi.EOS_MG, rho0=8.96e-3, c0=3.97e6, Gamma0=2.12, s=1.479)
+    cfg.flux = flux
+    n = 8192
+    Vm = random_sg_states(rng, n)
+    ids = rng.integers(0, 2, n).astype(np.int32)
+    Vm[ids == 1, 0] = rng.uniform(8.0e-3, 1.0e-2, (ids == 1).sum())
+    Vp = Vm * (1 + 0.1 * rng.uniform(-1, 1, (n, 5)))
+    dirs = rng.integers(0, 3, n).astype(np.int32)
+    g = Solver(cfg).flux_batch(dirs, Vm, Vp, ids)
+    o = ob.flux_batch(cfg, dirs, Vm, Vp, ids)
+    assert rel_linf(g, o).max() < 1e-13
+
+
+def _residual_case(cfg, V, ID, phi):
+    s, o = _pair(cfg, V, ID, phi)
+    R, Ro = s.ComputeResidual(), o.residual()
+    err = rel_linf(R, Ro)
+    assert np.all(err < TOL1), err
+    if cfg.n_levelsets:
+        assert rel_linf(s.LevelSetResidual(), o.levelset_residual()) < TOL1
+    dt, cfl = s.ComputeTimeStepSize()
+    dto, cflo = o.compute_dt()
+    assert abs(dt - dto) <= 1e-14 * dto and abs(cfl - cflo) <= 1e-14
+    assert s.counters()["interface_faces"] == o.counters()["interface_faces"]
+
+
+def test_residual_riemann1d():
+    _residual_case(*problems.riemann1d())
+
+
+def test_residual_shock_bubble_small():
+    _residual_case(*problems.shock_bubble(n=24))
+
+
+@pytest.mark.parametrize("limiter", [abi.LIM_GENERALIZED_MINMOD, abi.LIM_NONE])
+@pytest.mark.parametrize("flux", [abi.FLUX_LLF, abi.FLUX_ROE])
+def test_residual_variants(limiter, flux):
+    cfg, V, ID, phi = problems.shock_bubble(n=16)
+    cfg.limiter, cfg.flux = limiter, flux
+    cfg.slope_near_interface = abi.SLOPE_ZERO
+    _residual_case(cfg, V, ID, phi)
+
+
+def _steps(cfg, V, ID, phi, nsteps, tol):
+    s, o = _pair(cfg, V, ID, phi)
+    for _ in range(nsteps):
+        dt, _ = o.compute_dt()
+        dts, _ = s.ComputeTimeStepSize()
+        assert abs(dts - dt) <= 1e-9 * dt
+        o.advance(dt)
+        s.AdvanceOneTimeStep(dt)
+    g = s.get_state()
+    Vo, IDo, phio = o.download()
+    err = rel_linf(g.V, Vo)
+    assert np.all(err < tol), err
+    assert rel_linf(g.Phi, phio) < tol
+    np.testing.assert_array_equal(g.ID, IDo)
+    return s, o
+
+
+def test_one_step_riemann1d():
+    _steps(*problems.riemann1d(), 1, TOL1)
+
+
+@pytest.mark.parametrize("ts", [abi.TS_FORWARD_EULER, abi.TS_RK3])
+def test_one_step_other_integrators(ts):
+    cfg, V, ID, phi = problems.riemann1d(nx=128, ny=4, nz=4)
+    cfg.ts_type = ts
+    _steps(cfg, V, ID, phi, 1, TOL1)
+
+
+def test_hundred_steps_riemann1d():
+    s, o = _steps(*problems.riemann1d(), 100, TOL100)
+    c, co = s.counters(), o.counters()
+    assert c["swept_cells"] == co["swept_cells"] > 0
+    assert c["riemann_errors"] == co["riemann_errors"] == 0
+
+
+def test_shock_bubble_small_steps():
+    _steps(*problems.shock_bubble(n=24), 10, TOL100)
+
+
+def test_run_loop_matches_oracle():
+    cfg, V, ID, phi = problems.riemann1d(nx=128, ny=4, nz=4)
+    s, o = _pair(cfg, V, ID, phi)
+    c = s.run(20)
+    o.run(20)
+    g = s.get_state()
+    Vo, IDo, _ = o.download()
+    assert c["steps"] == 20
+    assert abs(c["time"] - o.counters()["time"]) <= 1e-12 * c["time"]
+    assert np.all(rel_linf(g.V, Vo) < TOL100)
+    np.testing.assert_array_equal(g.ID, IDo)

@@ -1,0 +1,121 @@
+"""Pin the oracle: it must reproduce the reference's own compiled code
+(oracle/_ref, built from the reference sources) and the reference's golden
+exact-Riemann files (tests/golden, extracted by make_riemann_golden.py)."""
+import numpy as np
+import pytest
+
+from helpers import config_for_materials, golden_problem, golden_riemann_cases, random_sg_states
+from m2c_gb300 import abi
+from oracle import binding as ob
+
+CASES = golden_riemann_cases()
+# cases whose 1- and 3-waves are both shocks: the reference's Hugoniot path is
+# unchanged since the golden files were written, so they agree to print precision
+SHOCK_SHOCK = {"Test4", "Test8", "Test9", "Test10"}
+
+
+@pytest.fixture(scope="module")
+def ref():
+    r = ob.ref_lib()
+    if r is None:
+        pytest.skip("reference sources not available on this machine")
+    return r
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["test"] for c in CASES])
+def test_oracle_equals_reference_build_on_golden_inputs(ref, case):
+    for tol in (1e-5, 1e-10):
+        cfg = config_for_materials(case["materials"], tol=tol)
+        Vm, idm, Vp, idp, d = golden_problem(case)
+        o = ob.riemann_batch(cfg, Vm, idm, Vp, idp, d)
+        r = ob.ref_riemann_batch(ref, cfg, Vm, idm, Vp, idp, d)
+        assert o["err"][0] == r["err"][0]
+        np.testing.assert_array_equal(o["Vsm"], r["Vsm"])
+        np.testing.assert_array_equal(o["Vsp"], r["Vsp"])
+        np.testing.assert_array_equal(o["Vs"], r["Vs"])
+        assert o["id"][0] == r["id"][0]
+
+
+@pytest.mark.parametrize("case", CASES, ids=[c["test"] for c in CASES])
+def test_oracle_against_golden_star_states(case):
+    cfg = config_for_materials(case["materials"], tol=1e-10)
+    Vm, idm, Vp, idp, d = golden_problem(case)
+    o = ob.riemann_batch(cfg, Vm, idm, Vp, idp, d)
+    assert o["err"][0] == 0
+    got = dict(u_star=o["Vsm"][0, 1], p_star=o["Vsm"][0, 4], rho_l_star=o["Vsm"][0, 0], rho_r_star=o["Vsp"][0, 0])
+    u_scale = max(abs(case["left"][1]), abs(case["right"][1]), abs(case["u_star"]), 1e-300)
+    if case["test"] in SHOCK_SHOCK:
+        tol = 2e-6   # 7 printed digits of the golden file and of its header inputs
+    elif case["test"] in ("Test11", "Test12"):
+        # near-vacuum rarefaction (rho_L = 1.2e-6): the current reference's
+        # Cash-Karp stage pressure (ExactRiemannSolverBase.cpp:1809) moves p* far
+        # from the older golden; the contact velocity and the right star density agree
+        assert abs(got["u_star"] - case["u_star"]) / u_scale < 2e-3
+        assert abs(got["rho_r_star"] - case["rho_r_star"]) / case["rho_r_star"] < 1e-6
+        return
+    else:
+        tol = 3e-3   # rarefaction cases: same stage-pressure difference, bounded
+    assert abs(got["u_star"] - case["u_star"]) / u_scale < tol
+    for k in ("p_star", "rho_l_star", "rho_r_star"):
+        assert abs(got[k] - case[k]) / abs(case[k]) < tol, k
+
+
+def _random_two_material_cfg(rng):
+    c = abi.default_config()
+    c.n_materials = 3
+    abi.set_material(c.mat[0], abi.EOS_SG, gamma=rng.uniform(1.1, 7.0), pc=rng.uniform(0, 6e8))
+    abi.set_material(c.mat[1], abi.EOS_NASG, gamma=rng.uniform(1.1, 3.0), pc=rng.uniform(0, 6e8),
+                     b=rng.uniform(0, 1e-3), q=0.0)
+    abi.set_material(c.mat[2], abi.EOS_SG, gamma=1.4, pc=0.0)
+    c.tol_main = 1e-10
+    return c
+
+
+def _make_physical(cfg, V, ids, rng):
+    # Noble-Abel stiffened gas needs 1/rho > b (VarFcnNASG.h:55); the reference
+    # stops the process on a nonphysical input, so keep the inputs physical.
+    b = cfg.mat[1].b
+    sel = (ids == 1) & (V[:, 0] * b > 0.5)
+    V[sel, 0] = rng.uniform(0.05, 0.5, sel.sum()) / b
+
+
+def test_oracle_equals_reference_build_random_riemann(ref):
+    rng = np.random.default_rng(7)
+    for trial in range(4):
+        cfg = _random_two_material_cfg(rng)
+        n = 200
+        Vm = random_sg_states(rng, n)
+        Vp = random_sg_states(rng, n)
+        idm = rng.integers(0, 3, n).astype(np.int32)
+        idp = rng.integers(0, 3, n).astype(np.int32)
+        _make_physical(cfg, Vm, idm, rng)
+        _make_physical(cfg, Vp, idp, rng)
+        dirs = np.zeros((n, 3))
+        dirs[np.arange(n), rng.integers(0, 3, n)] = 1.0
+        o = ob.riemann_batch(cfg, Vm, idm, Vp, idp, dirs)
+        r = ob.ref_riemann_batch(ref, cfg, Vm, idm, Vp, idp, dirs)
+        # both succeed on the adaptive path; the reference's retry with its
+        # non-adaptive solver (ExactRiemannSolverBase.cpp:178-193, 323-337) after a
+        # failure is not restated, so failed solves are excluded here
+        ok = (o["err"] == 0) & (r["err"] == 0)
+        assert ((o["err"] != 0) & (r["err"] == 0)).sum() <= 2
+        np.testing.assert_array_equal(o["Vsm"][ok], r["Vsm"][ok])
+        np.testing.assert_array_equal(o["Vsp"][ok], r["Vsp"][ok])
+        np.testing.assert_array_equal(o["Vs"][ok], r["Vs"][ok])
+        assert ok.mean() > 0.8
+
+
+@pytest.mark.parametrize("flux", [abi.FLUX_HLLC, abi.FLUX_LLF, abi.FLUX_ROE])
+def test_oracle_equals_reference_build_fluxes(ref, flux):
+    rng = np.random.default_rng(11 + flux)
+    cfg = _random_two_material_cfg(rng)
+    cfg.flux = flux
+    n = 2000
+    Vm = random_sg_states(rng, n)
+    Vp = Vm * (1 + 0.2 * rng.uniform(-1, 1, (n, 5)))
+    Vp[:, 1:4] = Vm[:, 1:4] + rng.uniform(-50, 50, (n, 3))
+    ids = rng.integers(0, 3, n).astype(np.int32)
+    _make_physical(cfg, Vm, ids, rng)
+    _make_physical(cfg, Vp, ids, rng)
+    dirs = rng.integers(0, 3, n).astype(np.int32)
+    np.testing.assert_array_equal(ob.flux_batch(cfg, dirs, Vm, Vp, ids), ob.ref_flux_batch(ref, cfg, dirs, Vm, Vp, ids))
