@@ -139,6 +139,8 @@ typedef struct {
   double time;                 /* simulated time */
   double dt;                   /* last time step */
   double cfl;                  /* last CFL number */
+  int64_t riemann_fallbacks;   /* solves retried with the non-adaptive solver (ExactRiemannSolverBase.cpp:178-193, 323-337) */
+  int64_t path_capped;         /* solves whose integration-path cache reached its capacity */
 } m2cg_counters;
 
 typedef struct m2cg_ctx m2cg_ctx;

@@ -70,7 +70,8 @@ class Counters(C.Structure):
                 ("riemann_iterations", C.c_int64), ("riemann_solves", C.c_int64),
                 ("clipped_cells", C.c_int64), ("clipped_faces", C.c_int64), ("nonphysical", C.c_int64),
                 ("swept_cells", C.c_int64), ("unresolved_cells", C.c_int64), ("steps", C.c_int64),
-                ("time", C.c_double), ("dt", C.c_double), ("cfl", C.c_double)]
+                ("time", C.c_double), ("dt", C.c_double), ("cfl", C.c_double),
+                ("riemann_fallbacks", C.c_int64), ("path_capped", C.c_int64)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}

@@ -510,6 +510,8 @@ m2cg_status m2cg_get_counters(m2cg_ctx* x, m2cg_counters* c) {
   c->time = s.time;
   c->dt = s.dt;
   c->cfl = s.cfl;
+  c->riemann_fallbacks = (int64_t)h[CNT_FALLBACK];
+  c->path_capped = (int64_t)h[CNT_PATH_CAPPED];
   if (h[CNT_IF_OVERFLOW] || h[CNT_SWEPT_OVERFLOW]) {
     set_err("interface or swept-cell list overflow");
     return M2CG_ERR_CAPACITY;

@@ -21,7 +21,7 @@ struct Grid {
 // Device counter slots (int64).
 enum {
   CNT_IFACE = 0, CNT_RERR, CNT_RITER, CNT_RSOLVE, CNT_CLIPCELL, CNT_CLIPFACE, CNT_BAD, CNT_SWEPT, CNT_UNRES,
-  CNT_IF_OVERFLOW, CNT_PATH_CAPPED, CNT_SWEPT_OVERFLOW, CNT_BADID, CNT_N
+  CNT_IF_OVERFLOW, CNT_PATH_CAPPED, CNT_SWEPT_OVERFLOW, CNT_BADID, CNT_FALLBACK, CNT_N
 };
 
 // Scalars that live on the device for the whole run (no host round trip per step).

@@ -48,6 +48,8 @@ struct ExactRiemannDev {
   PathCache path1, path3;
   int evals;
   double warm_p;   // > 0 replaces the acoustic-theory p0 (learned warm start)
+  bool nonadaptive;  // running as the reference's non-adaptive fallback solver
+  int fallback;      // 1 if the last solve needed the non-adaptive retry
 
   M2CG_DEV const DevMat& mat(int id) const { return mats->m[id]; }
 
@@ -110,6 +112,104 @@ struct ExactRiemannDev {
     return true;
   }
 
+  // Classical RK4 step of the non-adaptive solver, ExactRiemannSolverBase.cpp:2896-2990
+  __device__ __noinline__ bool rk4(int wave, const DevMat& M, double rho_0, double u_0, double p_0, double dp,
+                                   double& rho, double& u, double& p, double& xi) const {
+    dp = -dp;
+    double e_0 = eos_e(M, rho_0, p_0);
+    double c_0_square = eos_c2(M, rho_0, e_0);
+    if (rho_0 <= 0 || c_0_square < 0) return false;
+    double c_0 = sqrt(c_0_square);
+    double rho_1 = rho_0 + 0.5 * dp / c_0_square;
+    double p_1 = p_0 + 0.5 * dp;
+    double e_1 = eos_e(M, rho_1, p_1);
+    double c_1_square = eos_c2(M, rho_1, e_1);
+    if (rho_1 <= 0 || c_1_square < 0) return false;
+    double c_1 = sqrt(c_1_square);
+    double rho_2 = rho_0 + 0.5 * dp / c_1_square;
+    double p_2 = p_1;
+    double e_2 = eos_e(M, rho_2, p_2);
+    double c_2_square = eos_c2(M, rho_2, e_2);
+    if (rho_2 <= 0 || c_2_square < 0) return false;
+    double c_2 = sqrt(c_2_square);
+    double rho_3 = rho_0 + dp / c_2_square;
+    double p_3 = p_0 + dp;
+    double e_3 = eos_e(M, rho_3, p_3);
+    double c_3_square = eos_c2(M, rho_3, e_3);
+    if (rho_3 <= 0 || c_3_square < 0) return false;
+    double c_3 = sqrt(c_3_square);
+    double drho = 1.0 / 6.0 * dp * (1. / c_0_square + 2.0 * (1. / c_1_square + 1. / c_2_square) + 1. / c_3_square);
+    double du = 1.0 / 6.0 * dp * (1. / c_0 / rho_0 + 2.0 * (1. / c_1 / rho_1 + 1. / c_2 / rho_2) + 1. / c_3 / rho_3);
+    if (isnan(du)) return false;
+    rho = rho_0 + drho;
+    p = p_0 + dp;
+    u = (wave == 1) ? u_0 - du : u_0 + du;
+    double e = eos_e(M, rho, p);
+    double c = eos_c2(M, rho, e);
+    if (rho <= 0 || c < 0) return false;
+    c = sqrt(c);
+    xi = (wave == 1) ? u - c : u + c;
+    return true;
+  }
+
+  // Fixed-step rarefaction of the non-adaptive solver, ExactRiemannSolverBase.cpp:2534-2651
+  __device__ __noinline__ bool rarefaction_fixed(int wave, PathCache& path, const DevMat& M, double rho, double u,
+                                                 double p, double ps, double& rhos, double& us, bool* trans_rare,
+                                                 double* Vrare) {
+    double rhos_0 = rho, us_0 = u, ps_0 = p, xi_0;
+    double rhos_1 = rho, us_1 = u, ps_1 = p, xi_1 = 0;
+    double dp_target = (p - ps) / P.numSteps;
+    double e = eos_e(M, rho, p);
+    double dpdrho = eos_dpdrho(M, rho, e);
+    double drho_op1 = (p - ps) / dpdrho / P.numSteps;
+    double drho_op2 = rho / (2.5 * P.numSteps);
+    double drho_target = fmin(drho_op1, drho_op2);
+    double dp = fmin(dp_target, drho_target * dpdrho);
+    double tol_end = P.tol_rare * fmax(1.0, fabs(p));
+    double c = eos_c2(M, rho, e);
+    if (rho <= 0 || c < 0) return false;
+    c = sqrt(c);
+    if (path.n > 1) {
+      int index0 = 0;
+      for (int j = path.n - 1; j >= 0; j--) {
+        if (path.get(j, 0) > ps) { index0 = j; break; }
+      }
+      ps_0 = path.get(index0, 0);
+      rhos_0 = path.get(index0, 1);
+      us_0 = path.get(index0, 2);
+      dp = fmin((p - ps) / P.numSteps, ps_0 - ps);
+    }
+    xi_0 = (wave == 1) ? u - c : u + c;
+    for (int i = 0; i < P.numSteps * 5; i++) {
+      if (fabs(ps_1 - ps) <= tol_end) {
+        rhos = rhos_1;
+        us = us_1;
+        return !eos_bad(M, rhos, ps);
+      }
+      bool ok = rk4(wave, M, rhos_0, us_0, ps_0, dp, rhos_1, us_1, ps_1, xi_1);
+      if (!ok) {
+        dp = dp / 2.0;
+        if (dp == 0.0) break;
+        continue;
+      }
+      if (ps_1 - ps < -tol_end) { dp = ps_0 - ps; continue; }
+      if (ps_1 < path.get(path.n - 1, 0)) path.push(ps_1, rhos_1, us_1);
+      if (trans_rare && Vrare && xi_0 * xi_1 <= 0) {
+        *trans_rare = true;
+        double w0 = fabs(xi_1), w1 = fabs(xi_0);
+        double ww = w0 + w1;
+        w0 /= ww;
+        w1 /= ww;
+        Vrare[0] = w0 * rhos_0 + w1 * rhos_1;
+        Vrare[1] = w0 * us_0 + w1 * us_1;
+        Vrare[2] = w0 * ps_0 + w1 * ps_1;
+      }
+      dp = fmin(fmin(dp_target, ps_1 - ps), 4.0 * dp);
+      rhos_0 = rhos_1; us_0 = us_1; ps_0 = ps_1; xi_0 = xi_1;
+    }
+    return false;
+  }
+
   // Hugoniot residual, ExactRiemannSolverBase.h:66-83
   M2CG_DEV double hugo(const DevMat& M, double e, double pavg, double one_over_rho, double ps, double rhos) const {
     double es = eos_e(M, rhos, ps);
@@ -122,6 +222,7 @@ struct ExactRiemannDev {
     const DevMat& M = mat(id);
     rhos = rho;
     us = u;
+    if (p > ps && nonadaptive) return rarefaction_fixed(wave, path, M, rho, u, p, ps, rhos, us, trans_rare, Vrare);
     if (p > ps) {
       double rhos_0 = rho, us_0 = u, ps_0 = p, xi_0;
       double rhos_1 = rho, us_1 = u, ps_1 = p, xi_1 = 0;
@@ -448,9 +549,31 @@ struct ExactRiemannDev {
     Vsp[0] = rhor2; Vsp[1] = utr[0] + u2 * dir[0]; Vsp[2] = utr[1] + u2 * dir[1]; Vsp[3] = utr[2] + u2 * dir[2]; Vsp[4] = p2;
   }
 
-  // ExactRiemannSolverBase.cpp:59-347.  Returns 0 (ok), 1 (failed), -1 (nonphysical input).
-  __device__ __noinline__ int solve(const double* dir, const double* Vm, int idl, const double* Vp, int idr, double* Vs, int& id,
-                     double* Vsm, double* Vsp) {
+  // ExactRiemannSolverBase.cpp:59-347 with the non-adaptive retry after a failure
+  // (lines 178-193 and 323-337).  Returns 0 (ok), 1 (failed), -1 (nonphysical input).
+  __device__ __noinline__ int solve(const double* dir, const double* Vm, int idl, const double* Vp, int idr, double* Vs,
+                                    int& id, double* Vsm, double* Vsp) {
+    nonadaptive = false;
+    fallback = 0;
+    int e = solve_once(dir, Vm, idl, Vp, idr, Vs, id, Vsm, Vsp);
+    if (e == 1) {
+      int ev = evals;
+      double w = warm_p;
+      warm_p = 0.0;   // the fallback solver starts from acoustic theory
+      nonadaptive = true;
+      fallback = 1;
+      e = solve_once(dir, Vm, idl, Vp, idr, Vs, id, Vsm, Vsp);
+      evals += ev;
+      nonadaptive = false;
+      warm_p = w;
+    }
+    return e;
+  }
+
+  // One pass of ComputeRiemannSolution (the adaptive solver, or the
+  // non-adaptive one of ExactRiemannSolverBase.cpp:2243-2519).
+  __device__ __noinline__ int solve_once(const double* dir, const double* Vm, int idl, const double* Vp, int idr,
+                                         double* Vs, int& id, double* Vsm, double* Vsp) {
     evals = 0;
     double rhol = Vm[0], ul = Vm[1] * dir[0] + Vm[2] * dir[1] + Vm[3] * dir[2], pl = Vm[4];
     double rhor = Vp[0], ur = Vp[1] * dir[0] + Vp[2] * dir[1] + Vp[3] * dir[2], pr = Vp[4];

@@ -39,7 +39,7 @@ __global__ void k_riemann_interfaces(Params P, const Mats* __restrict__ md, Stat
   rs.path3.cap = path_cap;
   const int64_t st[3] = {1, g.sy, g.sz};
   if (tid == 0) atomicAdd(&cnt[CNT_IFACE], (unsigned long long)n);
-  unsigned long long iters = 0, solves = 0, errs = 0, bad = 0, capped = 0;
+  unsigned long long iters = 0, solves = 0, errs = 0, bad = 0, capped = 0, fallbacks = 0;
   for (int64_t s = tid; s < n; s += T) {
     int64_t fc = L.face[s];
     int d = (int)(fc & 3);
@@ -67,6 +67,7 @@ __global__ void k_riemann_interfaces(Params P, const Mats* __restrict__ md, Stat
       solves++;
       iters += rs.evals;
       capped += rs.path1.capped | rs.path3.capped;
+      fallbacks += rs.fallback;
       if (err) errs++;
       if (err < 0) bad++;
       eos_clip(P.mats.m[idm], Vsm);
@@ -95,6 +96,7 @@ __global__ void k_riemann_interfaces(Params P, const Mats* __restrict__ md, Stat
   if (errs) atomicAdd(&cnt[CNT_RERR], errs);
   if (bad) atomicAdd(&cnt[CNT_BAD], bad);
   if (capped) atomicAdd(&cnt[CNT_PATH_CAPPED], capped);
+  if (fallbacks) atomicAdd(&cnt[CNT_FALLBACK], fallbacks);
 }
 
 // Batched independent problems (device arrays, AoS rows of 5 / 3).

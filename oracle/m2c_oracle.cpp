@@ -41,6 +41,7 @@ namespace {
 struct Counters {
   int64_t interface_faces = 0, riemann_errors = 0, riemann_iterations = 0, riemann_solves = 0;
   int64_t clipped_cells = 0, clipped_faces = 0, nonphysical = 0, swept_cells = 0, unresolved_cells = 0, steps = 0;
+  int64_t fallbacks = 0;
 };
 
 // Star states stored at one face (RiemannSolutions.h:12-30; SpaceOperator.cpp:1661-1666).
@@ -388,8 +389,8 @@ void Oracle::ComputeResidual(const std::vector<double>& v, const std::vector<int
   std::vector<double> lf1[3], lf2[3];
   for (int d = 0; d < 3; d++) { lf1[d].assign(N() * 5, 0.0); lf2[d].assign(N() * 5, 0.0); }
   size_t cs[3] = {1, (size_t)PX, (size_t)PX * PY};
-  int64_t n_if = 0, n_err = 0, n_iter = 0, n_solve = 0;
-#pragma omp parallel reduction(+ : n_if, n_err, n_iter, n_solve)
+  int64_t n_if = 0, n_err = 0, n_iter = 0, n_solve = 0, n_fb = 0;
+#pragma omp parallel reduction(+ : n_if, n_err, n_iter, n_solve, n_fb)
   {
     ExactRiemann riemann(vf, rp);
     Counters local;
@@ -423,6 +424,7 @@ void Oracle::ComputeResidual(const std::vector<double>& v, const std::vector<int
                 int err = riemann.Solve(dirv, Vm, nid, Vp, myid, Vmid, midid, Vsm, Vsp);
                 n_solve++;
                 n_iter += riemann.evals;
+                n_fb += riemann.fallbacks;
                 if (err) n_err++;
                 vf[nid].ClipDensityAndPressure(Vsm);
                 if (vf[nid].CheckState(Vsm)) local.nonphysical++;
@@ -455,6 +457,7 @@ void Oracle::ComputeResidual(const std::vector<double>& v, const std::vector<int
   cnt.riemann_errors += n_err;
   cnt.riemann_iterations += n_iter;
   cnt.riemann_solves += n_solve;
+  cnt.fallbacks += n_fb;
   // Gather in the reference's accumulation order: -x, -y, -z faces, then +x, +y, +z.
   R.assign(N() * 5, 0.0);
   double area[3] = {dy * dz, dx * dz, dx * dy};
@@ -887,6 +890,7 @@ void orc_counters(void* h, m2cg_counters* c) {
   c->time = o->time;
   c->dt = o->last_dt;
   c->cfl = o->last_cfl;
+  c->riemann_fallbacks = o->cnt.fallbacks;
 }
 
 void orc_conserved_totals(void* h, double* tot) {

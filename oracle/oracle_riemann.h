@@ -27,10 +27,36 @@ class ExactRiemann {
   // Optional warm start: when > 0, replaces the acoustic p0 (used only by the
   // learned-warm-start study; the reference path passes 0).
   double warm_p = 0.0;
+  // true while running as ExactRiemannSolverNonAdaptive (fixed-step RK4
+  // rarefactions, ExactRiemannSolverBase.cpp:2243-2990)
+  bool nonadaptive = false;
+  int fallbacks = 0;
 
-  // ExactRiemannSolverBase.cpp:59-347.  Returns 0 on success, 1 on failure.
+  // ExactRiemannSolverBase.cpp:59-347 including the retries with the
+  // non-adaptive solver after a failure (lines 178-193 and 323-337).
   int Solve(const double* dir, const double* Vm, int idl, const double* Vp, int idr,
             double* Vs, int& id, double* Vsm, double* Vsp) {
+    nonadaptive = false;
+    fallbacks = 0;
+    int e = SolveOnce(dir, Vm, idl, Vp, idr, Vs, id, Vsm, Vsp);
+    if (e == 1) {
+      int ev = evals;
+      double w = warm_p;
+      warm_p = 0.0;  // the fallback solver starts from acoustic theory
+      nonadaptive = true;
+      fallbacks = 1;
+      e = SolveOnce(dir, Vm, idl, Vp, idr, Vs, id, Vsm, Vsp);
+      evals += ev;
+      nonadaptive = false;
+      warm_p = w;
+    }
+    return e;
+  }
+
+  // One pass of ComputeRiemannSolution (ExactRiemannSolverBase.cpp:59-347, or
+  // 2243-2519 when nonadaptive).  Returns 0 on success, 1 on failure.
+  int SolveOnce(const double* dir, const double* Vm, int idl, const double* Vp, int idr,
+                double* Vs, int& id, double* Vsm, double* Vsp) {
     evals = 0; main_iters = 0;
     double rhol = Vm[0];
     double ul = Vm[1] * dir[0] + Vm[2] * dir[1] + Vm[3] * dir[2];
@@ -65,7 +91,7 @@ class ExactRiemann {
 
     bool success = FindInitialInterval(rhol, ul, pl, el, cl, idl, rhor, ur, pr, er, cr, idr,
                                        p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
-    if (!success) {  // :150-194 (the non-adaptive retry is not restated; report failure)
+    if (!success) {  // :150-194 (the caller retries with the non-adaptive solver)
       success = RhoUStar(1, path1_, rhol, ul, pl, p1, idl, rhol0, rhol0 * 1.1, rhol2, ul2, &trans_rare, Vrare_x0);
       success = success && RhoUStar(3, path3_, rhor, ur, pr, p1, idr, rhor0, rhol0 * 1.1, rhor2, ur2, &trans_rare, Vrare_x0);
       if (!success) {
@@ -122,7 +148,7 @@ class ExactRiemann {
     main_iters = iter;
     double u2 = 0.5 * (ul2 + ur2);
     Finalize(dir, Vm, Vp, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol2, rhor2, u2, p2, trans_rare, Vrare_x0, Vs, id, Vsm, Vsp);
-    if (iter == P.maxIts_main) return 1;  // :323-337 (non-adaptive retry not restated)
+    if (iter == P.maxIts_main) return 1;  // :323-337 (the caller retries non-adaptively)
     return 0;
   }
 
@@ -348,6 +374,7 @@ class ExactRiemann {
     const Eos& vf = vf_[id];
     rhos = rho;
     us = u;
+    if (p > ps && nonadaptive) return RarefactionFixed(wavenumber, path, rho, u, p, ps, id, rhos, us, trans_rare, Vrare_x0);
     if (p > ps) {  // rarefaction
       double rhos_0 = rho, us_0 = u, ps_0 = p, xi_0;
       double rhos_1 = rho, us_1 = u, ps_1 = p, xi_1 = 0;
@@ -504,6 +531,108 @@ class ExactRiemann {
       if (vf.CheckState(rhos, ps)) return false;
       us = (wavenumber == 1) ? u - std::sqrt(du) : u + std::sqrt(du);
     }
+    return true;
+  }
+
+  // Non-adaptive rarefaction integration, ExactRiemannSolverBase.cpp:2534-2651
+  bool RarefactionFixed(int wavenumber, std::vector<std::array<double, 3>>& path, double rho, double u, double p,
+                        double ps, int id, double& rhos, double& us, bool* trans_rare, double* Vrare_x0) {
+    const Eos& vf = vf_[id];
+    double rhos_0 = rho, us_0 = u, ps_0 = p, xi_0;
+    double rhos_1 = rho, us_1 = u, ps_1 = p, xi_1 = 0;
+    double dp_target = (p - ps) / P.numSteps_rarefaction;
+    double e = vf.GetInternalEnergyPerUnitMass(rho, p);
+    double dpdrho = vf.GetDpdrho(rho, e);
+    double drho_op1 = (p - ps) / dpdrho / P.numSteps_rarefaction;
+    double drho_op2 = rho / (2.5 * P.numSteps_rarefaction);
+    double drho_target = std::min(drho_op1, drho_op2);
+    double dp = std::min(dp_target, drho_target * dpdrho);
+    double pressure_endpoint_tol = P.tol_rarefaction * std::max(1.0, std::fabs(p));
+    double c = vf.ComputeSoundSpeedSquare(rho, e);
+    if (rho <= 0 || c < 0) return false;
+    c = std::sqrt(c);
+    int index0 = 0;
+    if (path.size() > 1) {
+      for (int j = (int)path.size() - 1; j >= 0; j--) {
+        if (path[j][0] > ps) { index0 = j; break; }
+      }
+      ps_0 = path[index0][0];
+      rhos_0 = path[index0][1];
+      us_0 = path[index0][2];
+      dp = std::min((p - ps) / P.numSteps_rarefaction, ps_0 - ps);
+    }
+    double xi = (wavenumber == 1) ? u - c : u + c;
+    xi_0 = xi;
+    bool done = false;
+    for (int i = 0; i < P.numSteps_rarefaction * 5; i++) {
+      if (std::fabs(ps_1 - ps) <= pressure_endpoint_tol) {
+        rhos = rhos_1;
+        us = us_1;
+        if (vf.CheckState(rhos, ps)) return false;
+        done = true;
+        break;
+      }
+      bool success = RK4(wavenumber, vf, rhos_0, us_0, ps_0, dp, rhos_1, us_1, ps_1, xi_1);
+      if (!success) {
+        dp = dp / 2.0;
+        if (dp == 0.0) break;
+        continue;
+      }
+      if (ps_1 - ps < -pressure_endpoint_tol) { dp = ps_0 - ps; continue; }
+      if (ps_1 < path.back()[0]) path.push_back({ps_1, rhos_1, us_1});
+      if (trans_rare && Vrare_x0 && xi_0 * xi_1 <= 0) {
+        *trans_rare = true;
+        double w0 = std::fabs(xi_1), w1 = std::fabs(xi_0);
+        double ww = w0 + w1;
+        w0 /= ww;
+        w1 /= ww;
+        Vrare_x0[0] = w0 * rhos_0 + w1 * rhos_1;
+        Vrare_x0[1] = w0 * us_0 + w1 * us_1;
+        Vrare_x0[2] = w0 * ps_0 + w1 * ps_1;
+      }
+      dp = std::min(std::min(dp_target, ps_1 - ps), 4.0 * dp);
+      rhos_0 = rhos_1; us_0 = us_1; ps_0 = ps_1; xi_0 = xi_1;
+    }
+    return done;
+  }
+
+  // Classical RK4 step, ExactRiemannSolverBase.cpp:2896-2990
+  bool RK4(int wavenumber, const Eos& vf, double rho_0, double u_0, double p_0, double dp, double& rho, double& u,
+           double& p, double& xi) {
+    dp = -dp;
+    double e_0 = vf.GetInternalEnergyPerUnitMass(rho_0, p_0);
+    double c_0_square = vf.ComputeSoundSpeedSquare(rho_0, e_0);
+    if (rho_0 <= 0 || c_0_square < 0) return false;
+    double c_0 = std::sqrt(c_0_square);
+    double rho_1 = rho_0 + 0.5 * dp / c_0_square;
+    double p_1 = p_0 + 0.5 * dp;
+    double e_1 = vf.GetInternalEnergyPerUnitMass(rho_1, p_1);
+    double c_1_square = vf.ComputeSoundSpeedSquare(rho_1, e_1);
+    if (rho_1 <= 0 || c_1_square < 0) return false;
+    double c_1 = std::sqrt(c_1_square);
+    double rho_2 = rho_0 + 0.5 * dp / c_1_square;
+    double p_2 = p_1;
+    double e_2 = vf.GetInternalEnergyPerUnitMass(rho_2, p_2);
+    double c_2_square = vf.ComputeSoundSpeedSquare(rho_2, e_2);
+    if (rho_2 <= 0 || c_2_square < 0) return false;
+    double c_2 = std::sqrt(c_2_square);
+    double rho_3 = rho_0 + dp / c_2_square;
+    double p_3 = p_0 + dp;
+    double e_3 = vf.GetInternalEnergyPerUnitMass(rho_3, p_3);
+    double c_3_square = vf.ComputeSoundSpeedSquare(rho_3, e_3);
+    if (rho_3 <= 0 || c_3_square < 0) return false;
+    double c_3 = std::sqrt(c_3_square);
+    double drho = 1.0 / 6.0 * dp * (1. / c_0_square + 2.0 * (1. / c_1_square + 1. / c_2_square) + 1. / c_3_square);
+    double du = 1.0 / 6.0 * dp * (1. / c_0 / rho_0 + 2.0 * (1. / c_1 / rho_1 + 1. / c_2 / rho_2) + 1. / c_3 / rho_3);
+    if (std::isnan(du)) return false;
+    rho = rho_0 + drho;
+    p = p_0 + dp;
+    u = (wavenumber == 1) ? u_0 - du : u_0 + du;
+    double e = vf.GetInternalEnergyPerUnitMass(rho, p);
+    double c = vf.ComputeSoundSpeedSquare(rho, e);
+    if (rho <= 0 || c < 0) return false;
+    c = std::sqrt(c);
+    xi = (wavenumber == 1) ? u - c : u + c;
     return true;
   }
 

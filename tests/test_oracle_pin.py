@@ -94,15 +94,32 @@ def test_oracle_equals_reference_build_random_riemann(ref):
         dirs[np.arange(n), rng.integers(0, 3, n)] = 1.0
         o = ob.riemann_batch(cfg, Vm, idm, Vp, idp, dirs)
         r = ob.ref_riemann_batch(ref, cfg, Vm, idm, Vp, idp, dirs)
-        # both succeed on the adaptive path; the reference's retry with its
-        # non-adaptive solver (ExactRiemannSolverBase.cpp:178-193, 323-337) after a
-        # failure is not restated, so failed solves are excluded here
-        ok = (o["err"] == 0) & (r["err"] == 0)
-        assert ((o["err"] != 0) & (r["err"] == 0)).sum() <= 2
+        # every solve, including the failures that go through the reference's
+        # non-adaptive retry (ExactRiemannSolverBase.cpp:178-193, 323-337)
+        np.testing.assert_array_equal(o["err"], r["err"])
+        ok = o["err"] >= 0
         np.testing.assert_array_equal(o["Vsm"][ok], r["Vsm"][ok])
         np.testing.assert_array_equal(o["Vsp"][ok], r["Vsp"][ok])
         np.testing.assert_array_equal(o["Vs"][ok], r["Vs"][ok])
-        assert ok.mean() > 0.8
+        assert ok.all()
+
+
+def test_oracle_equals_reference_build_on_stalled_secant_cases(ref):
+    # nearly-equal states across a gas/water interface whose secant iteration
+    # stalls and falls back to the non-adaptive solver (seen in the shock-bubble run)
+    from m2c_gb300 import problems
+    cfg = problems.shock_bubble(n=8)[0]
+    Vm = np.array([[998.20519390865695, 3.3314753181257264e-12, 0, 0, 99999.991927862167],
+                   [1006.1150592521593, 1.8715164624221656e-14, 0, 0, 99999.991991758347]])
+    Vp = np.array([[1.1938544441698975, -2.7841691152760676e-09, 0, 0, 99999.999999021107],
+                   [1.2008467212565481, -3.0730441045384747e-11, 0, 0, 99999.999999807304]])
+    idm, idp = np.zeros(2, np.int32), np.ones(2, np.int32)
+    dirs = np.array([[1.0, 0, 0], [1.0, 0, 0]])
+    o = ob.riemann_batch(cfg, Vm, idm, Vp, idp, dirs)
+    r = ob.ref_riemann_batch(ref, cfg, Vm, idm, Vp, idp, dirs)
+    np.testing.assert_array_equal(o["err"], r["err"])
+    for k in ("Vsm", "Vsp", "Vs"):
+        np.testing.assert_array_equal(o[k], r[k])
 
 
 @pytest.mark.parametrize("flux", [abi.FLUX_HLLC, abi.FLUX_LLF, abi.FLUX_ROE])
