@@ -138,6 +138,7 @@ static m2cg_status fill_params(const m2cg_config& c, Params& P) {
     d.rho0 = s.rho0; d.s = s.s; d.e0 = s.e0; d.rho0_c0_c0 = s.rho0 * s.c0 * s.c0;
     d.G0_half = 0.5 * s.Gamma0; d.G0_rho0 = s.Gamma0 * s.rho0;
     d.rhomin = s.rhomin; d.pmin = s.pmin; d.rhomax = s.rhomax; d.pmax = s.pmax;
+    d.clip_default = (s.rhomin == 0.0 && s.pmin == -DBL_MAX && s.rhomax == DBL_MAX && s.pmax == DBL_MAX);
   }
   P.flux = c.flux; P.rec_type = c.rec_type; P.limiter = c.limiter; P.slope_zero = (c.slope_near_interface == M2CG_SLOPE_ZERO);
   P.mp_flux = c.mp_flux; P.mp_recon = c.mp_recon; P.mp_phasechange = c.mp_phasechange; P.mp_pcdir = c.mp_phasechange_dir;

@@ -16,7 +16,7 @@ namespace m2cg {
 // Material constants precomputed on the host (one entry per material ID).
 struct DevMat {
   int type;                      // M2CG_EOS_*
-  int pad;
+  int clip_default;              // rhomin = 0, pmin = -DBL_MAX, rhomax = pmax = DBL_MAX
   double gam, gam1, Pstiff, gamPs, invgam1;   // SG / NASG (Pstiff = pc for NASG)
   double b, q;                                // NASG
   double rho0, s, e0, rho0_c0_c0, G0_half, G0_rho0;  // MG
@@ -26,6 +26,43 @@ struct DevMat {
 struct Mats {
   DevMat m[M2CG_MAX_MATERIALS];
 };
+
+// ---- binary64 building blocks on the integer and FP64 pipes -----------------
+// GB300 runs binary64 at 2 FMA/clk/SM; comparisons, min/max and divisions cost
+// FP64-pipe slots too.  Sign and range tests on a double's bit pattern run on
+// the integer pipe instead (IEEE-754 binary64 orders like a sign-magnitude
+// integer).
+M2CG_DEV long long bits(double x) { return __double_as_longlong(x); }
+M2CG_DEV bool is_finite_bits(double x) { return (bits(x) & 0x7ff0000000000000ll) != 0x7ff0000000000000ll; }
+// x <= 0 (both zeros included)
+M2CG_DEV bool le_zero_bits(double x) { return bits(x) <= 0; }
+// x < 0 (negative zero excluded)
+M2CG_DEV bool lt_zero_bits(double x) { long long b = bits(x); return b < 0 && b != (long long)0x8000000000000000ull; }
+// |x| < c for a positive constant c
+M2CG_DEV bool abs_lt_bits(double x, double c) { return (bits(x) & 0x7fffffffffffffffll) < bits(c); }
+M2CG_DEV bool is_pos_inf(double x) { return bits(x) == 0x7ff0000000000000ll; }
+M2CG_DEV bool is_neg_inf(double x) { return bits(x) == (long long)0xfff0000000000000ull; }
+
+// Reciprocal and reciprocal square root: the hardware approximations of the
+// PTX ISA (rcp.approx.ftz.f64, rsqrt.approx.ftz.f64; about 2^-20 relative
+// error) refined by one third-order Householder step,
+//   r' = r (1 + e + e^2),            e = 1 - x r
+//   y' = y (1 + e/2 + 3 e^2 / 8),    e = 1 - x y^2,
+// which leaves at most about one ulp of error (checked on the device against
+// correctly rounded 1/x over 1e-20..1e20: max 2.2e-16).  Call sites pass
+// finite, positive, normal arguments.
+M2CG_DEV double rcp_fast(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  double e = fma(-x, r, 1.0);
+  return fma(r, fma(e, e, e), r);
+}
+M2CG_DEV double rsqrt_fast(double x) {
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  double e = fma(-x, y * y, 1.0);
+  return fma(y * e, fma(e, 0.375, 0.5), y);
+}
 
 // ---- equation of state ----------------------------------------------------
 M2CG_DEV double eos_p(const DevMat& M, double rho, double e) {
@@ -77,12 +114,48 @@ M2CG_DEV bool eos_clip(const DevMat& M, double* V) {
   if (V[4] > M.pmax) { V[4] = M.pmax; c = true; }
   return c;
 }
+// CheckState and ClipDensityAndPressure with the integer-pipe tests above
+// (same results for finite and infinite inputs).
+M2CG_DEV bool eos_bad5_fast(const DevMat& M, const double* V) {
+  if (!is_finite_bits(V[0]) || !is_finite_bits(V[1]) || !is_finite_bits(V[2]) || !is_finite_bits(V[3]) ||
+      !is_finite_bits(V[4]))
+    return true;
+  if (M.type == M2CG_EOS_SG || M.type == M2CG_EOS_NASG) return le_zero_bits(V[0]) || le_zero_bits(V[4] + M.Pstiff);
+  return eos_bad(M, V[0], V[4]);
+}
+M2CG_DEV bool eos_clip_fast(const DevMat& M, double* V) {
+  if (!M.clip_default) return eos_clip(M, V);
+  bool c = false;
+  if (lt_zero_bits(V[0])) { V[0] = 0.0; c = true; }
+  if (is_neg_inf(V[4])) { V[4] = M.pmin; c = true; }
+  if (is_pos_inf(V[0])) { V[0] = M.rhomax; c = true; }
+  if (is_pos_inf(V[4])) { V[4] = M.pmax; c = true; }
+  return c;
+}
+
 // VarFcnBase.h:190-201
 M2CG_DEV void prim_to_cons(const DevMat& M, const double* V, double* U) {
   U[0] = V[0];
   U[1] = V[0] * V[1]; U[2] = V[0] * V[2]; U[3] = V[0] * V[3];
   double e = eos_e(M, V[0], V[4]);
   U[4] = V[0] * (e + 0.5 * (V[1] * V[1] + V[2] * V[2] + V[3] * V[3]));
+}
+// Conversions with one reciprocal and no division (SG and NASG closed forms);
+// equal to prim_to_cons / cons_to_prim to rounding.
+M2CG_DEV void prim_to_cons_fast(const DevMat& M, const double* V, double* U) {
+  double k2 = V[1] * V[1] + V[2] * V[2] + V[3] * V[3];
+  U[0] = V[0];
+  U[1] = V[0] * V[1]; U[2] = V[0] * V[2]; U[3] = V[0] * V[3];
+  if (M.type == M2CG_EOS_SG) U[4] = fma(0.5 * V[0], k2, (V[4] + M.gamPs) * M.invgam1);
+  else U[4] = V[0] * (eos_e(M, V[0], V[4]) + 0.5 * k2);
+}
+M2CG_DEV void cons_to_prim_fast(const DevMat& M, const double* U, double* V) {
+  V[0] = U[0];
+  double ir = rcp_fast(U[0]);
+  V[1] = U[1] * ir; V[2] = U[2] * ir; V[3] = U[3] * ir;
+  double rhoe = U[4] - 0.5 * V[0] * (V[1] * V[1] + V[2] * V[2] + V[3] * V[3]);
+  if (M.type == M2CG_EOS_SG) V[4] = fma(M.gam1, rhoe, -M.gam * M.Pstiff);
+  else V[4] = eos_p(M, V[0], rhoe * ir);
 }
 // VarFcnBase.h:173-186
 M2CG_DEV void cons_to_prim(const DevMat& M, const double* U, double* V) {
@@ -182,6 +255,102 @@ M2CG_DEV bool flux_hllc(const DevMat& M, int dir, const double* Vm, const double
   return ok;
 }
 
+// ---- HLLC with shared reciprocals ------------------------------------------
+// The same flux as flux_hllc (FluxFcnHLLC.h:57-245) with every division of the
+// reference rewritten as a product with a reciprocal that is computed once:
+// 1/rho and sqrt(rho) come from one rsqrt per side, the Roe-average weight
+// 1/(sqrt(rho_m)+sqrt(rho_p)) is shared by all five averages, and the star-state
+// algebra uses three more reciprocals.  Results agree with the reference order
+// to a few ulps.
+struct Side {
+  double rho, vn, p, inv_rho, sr, e, dpdrho, Gamma, c2, c;
+};
+M2CG_DEV void side_eos(const DevMat& M, const double* V, int dir, Side& S) {
+  S.rho = V[0];
+  S.vn = V[1 + dir];
+  S.p = V[4];
+  double y = rsqrt_fast(S.rho);
+  S.sr = S.rho * y;
+  S.inv_rho = y * y;
+  if (M.type == M2CG_EOS_SG) {
+    S.e = (S.p + M.gamPs) * M.invgam1 * S.inv_rho;
+    S.dpdrho = M.gam1 * S.e;
+    S.Gamma = M.gam1;
+  } else if (M.type == M2CG_EOS_NASG) {
+    double vb = S.inv_rho - M.b;
+    S.e = M.invgam1 * (S.p + M.gamPs) * vb + M.q;
+    double r = S.inv_rho * rcp_fast(vb);
+    S.dpdrho = M.gam1 * (S.e - M.q) * r * r;
+    S.Gamma = M.gam1 * rcp_fast(1.0 - M.b * S.rho);
+  } else {
+    S.e = eos_e(M, S.rho, S.p);
+    S.dpdrho = eos_dpdrho(M, S.rho, S.e);
+    S.Gamma = eos_Gamma(M, S.rho);
+  }
+  S.c2 = S.dpdrho + S.p * S.inv_rho * S.Gamma;
+  S.c = (S.c2 > 0.0) ? S.c2 * rsqrt_fast(S.c2) : 0.0;
+}
+M2CG_DEV void phys_flux_side(int dir, const double* V, const Side& S, double* F) {
+  double k2 = V[1] * V[1] + V[2] * V[2] + V[3] * V[3];
+  double H = S.e + 0.5 * k2 + S.p * S.inv_rho;
+  double m = S.rho * S.vn;
+  F[0] = m;
+  F[1] = m * V[1]; F[2] = m * V[2]; F[3] = m * V[3];
+  F[1 + dir] = fma(m, S.vn, S.p);
+  F[4] = m * H;
+}
+M2CG_DEV void hllc_fstar_side(int dir, const double* V, const Side& S, double Sw, double Sstar, double* F) {
+  double t = Sw - S.vn;
+  double rhostar = S.rho * t * rcp_fast(Sw - Sstar);
+  double k2 = V[1] * V[1] + V[2] * V[2] + V[3] * V[3];
+  double Eo = S.e + 0.5 * k2;   // U[4] / rho
+  double U[5] = {S.rho, S.rho * V[1], S.rho * V[2], S.rho * V[3], S.rho * Eo};
+  double Us[5] = {1.0, V[1], V[2], V[3], Eo + (Sstar - S.vn) * (Sstar + S.p * S.inv_rho * rcp_fast(t))};
+  Us[1 + dir] = Sstar;
+  phys_flux_side(dir, V, S, F);
+#pragma unroll
+  for (int i = 0; i < 5; i++) F[i] = fma(Sw, fma(Us[i], rhostar, -U[i]), F[i]);
+}
+M2CG_DEV bool flux_hllc_fast(const DevMat& M, int dir, const double* Vm, const double* Vp, double* F) {
+  const double eps = 1e-10;
+  Side A, B;
+  side_eos(M, Vm, dir, A);
+  side_eos(M, Vp, dir, B);
+  double inv_s = rcp_fast(A.sr + B.sr);
+  double rho_hat = A.sr * B.sr;
+  double irr = A.inv_rho * B.inv_rho;          // 1 / rho_hat^2
+  double drho = B.rho - A.rho;
+  double dp = B.p - A.p;
+  double diff = (B.vn - A.vn) * inv_s;
+  double p_over_rho_hat = (A.sr * (A.p * A.inv_rho) + B.sr * (B.p * B.inv_rho)) * inv_s + 0.5 * diff * diff;
+  double de = B.e - A.e;
+  double e_hat = (A.sr * A.e + B.sr * B.e) * inv_s;
+  double inv_e = rcp_fast(e_hat);
+  double w_rho = drho * drho * irr;
+  double de_e = de * inv_e;
+  double w_e = de_e * de_e;
+  double inv_den = rcp_fast(w_rho + w_e + eps);
+  double dpdrho_avg = (A.sr * A.dpdrho + B.sr * B.dpdrho) * inv_s;
+  double Gamma_avg = (A.sr * A.Gamma + B.sr * B.Gamma) * inv_s;
+  double dpdrho_hat = ((w_e + eps) * dpdrho_avg + (dp - Gamma_avg * rho_hat * de) * drho * irr) * inv_den;
+  double Gamma_hat = ((w_rho + eps) * Gamma_avg + (dp - dpdrho_avg * drho) * de_e * inv_e * (A.inv_rho * B.sr * B.inv_rho * A.sr)) * inv_den;
+  double c2_hat = dpdrho_hat + Gamma_hat * p_over_rho_hat;
+  double c_hat = (c2_hat <= 0.0) ? eps : c2_hat * rsqrt_fast(c2_hat);
+  double vh = (A.sr * A.vn + B.sr * B.vn) * inv_s;
+  double Sm = fmin(A.vn - A.c, vh - c_hat);
+  double Sp = fmax(B.vn + B.c, vh + c_hat);
+  bool ok = !(A.c2 < 0.0) && !(B.c2 < 0.0);
+  if (0.0 <= Sm) phys_flux_side(dir, Vm, A, F);
+  else if (0.0 >= Sp) phys_flux_side(dir, Vp, B, F);
+  else {
+    double am = A.rho * (Sm - A.vn), bp = B.rho * (Sp - B.vn);
+    double Sstar = (dp + am * A.vn - bp * B.vn) * rcp_fast(am - bp);
+    if (Sstar >= 0.0) hllc_fstar_side(dir, Vm, A, Sm, Sstar, F);
+    else hllc_fstar_side(dir, Vp, B, Sp, Sstar, F);
+  }
+  return ok;
+}
+
 // FluxFcnLLF.h:46-111 and 118-185 (two materials)
 M2CG_DEV bool flux_llf2(const DevMat& Mm, const DevMat& Mp, int dir, const double* Vm, const double* Vp, double* F) {
   double em = eos_e(Mm, Vm[0], Vm[4]);
@@ -262,6 +431,14 @@ M2CG_DEV double gen_minmod(double alpha, double dq0, double dq1) {
   if (dq0 < 0.0 && dq1 < 0.0) return fmax(alpha * dq0, fmax(0.5 * (dq0 + dq1), alpha * dq1));
   if (dq0 > 0.0 && dq1 > 0.0) return fmin(alpha * dq0, fmin(0.5 * (dq0 + dq1), alpha * dq1));
   return 0.0;
+}
+// van Albada with the sign / magnitude tests on the integer pipe and one
+// reciprocal (same value as van_albada to an ulp)
+M2CG_DEV double van_albada_fast(double dq0, double dq1) {
+  double pr = dq0 * dq1;
+  if (le_zero_bits(pr) || abs_lt_bits(pr, 1e-16)) return 0.0;
+  double a = dq0 * dq0, b = dq1 * dq1;
+  return fma(dq1, a, dq0 * b) * rcp_fast(a + b);
 }
 // k = 2 on a uniform mesh (Reconstructor.cpp:103-121 with A = B = 1)
 M2CG_DEV double van_albada(double dq0, double dq1) {

@@ -29,8 +29,8 @@ __device__ __forceinline__ bool real_cell(const Grid& g, int64_t t, int& i, int&
 // K1: MUSCL reconstruction of the six face states of every real cell
 // (Reconstructor.cpp:426-782) followed by CheckReconstructedStates
 // (SpaceOperator.cpp:2446-2484).  fs[f*5+p]: f = vl, vr, vb, vt, vk, vf.
-__global__ void k_reconstruct(Params P, StateSet S, const int32_t* __restrict__ id, double* const* fs,
-                              unsigned long long* cnt) {
+__global__ void __launch_bounds__(128) k_reconstruct(Params P, StateSet S, const int32_t* __restrict__ id,
+                                                     double* const* fs, unsigned long long* cnt) {
   int i, j, k;
   if (!real_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
   const Grid& g = P.g;
@@ -38,6 +38,8 @@ __global__ void k_reconstruct(Params P, StateSet S, const int32_t* __restrict__ 
   double q[5];
 #pragma unroll
   for (int p = 0; p < 5; p++) q[p] = S.q[p][c];
+  const int myid = id[c];
+  const DevMat& M = P.mats.m[myid];
   double face[6][5];
   if (P.rec_type == M2CG_REC_CONSTANT) {
 #pragma unroll
@@ -46,7 +48,6 @@ __global__ void k_reconstruct(Params P, StateSet S, const int32_t* __restrict__ 
       for (int p = 0; p < 5; p++) face[f][p] = q[p];
   } else {
     const int64_t st[3] = {1, g.sy, g.sz};
-    int myid = id[c];
 #pragma unroll
     for (int d = 0; d < 3; d++) {
       bool zero = P.slope_zero && (id[c - st[d]] != myid || id[c + st[d]] != myid);
@@ -55,37 +56,37 @@ __global__ void k_reconstruct(Params P, StateSet S, const int32_t* __restrict__ 
         double dq0 = q[p] - S.q[p][c - st[d]];
         double dq1 = S.q[p][c + st[d]] - q[p];
         double s;
-        if (P.limiter == M2CG_LIM_VANALBADA) s = van_albada(dq0, dq1);
+        if (P.limiter == M2CG_LIM_VANALBADA) s = van_albada_fast(dq0, dq1);
         else if (P.limiter == M2CG_LIM_GENERALIZED_MINMOD) s = gen_minmod(P.minmod_coeff, dq0, dq1);
         else s = 0.5 * (dq0 + dq1);
         if (zero) s = 0.0;
-        face[2 * d][p] = q[p] - 0.5 * s;
-        face[2 * d + 1][p] = q[p] + 0.5 * s;
+        face[2 * d][p] = fma(-0.5, s, q[p]);
+        face[2 * d + 1][p] = fma(0.5, s, q[p]);
       }
     }
     // Reconstructor.cpp:722-778: the first nonphysical face state reverts to the cell value
-    const DevMat& M = P.mats.m[myid];
+    bool done = false;
 #pragma unroll
     for (int f = 0; f < 6; f++) {
-      if (eos_bad5(M, face[f])) {
+      bool bad = !done && eos_bad5_fast(M, face[f]);
+      if (bad) {
 #pragma unroll
         for (int p = 0; p < 5; p++) face[f][p] = q[p];
-        break;
+        done = true;
       }
     }
   }
   // CheckReconstructedStates: clip -> revert to the cell value
-  const DevMat& M = P.mats.m[id[c]];
   int nclip = 0, nbad = 0;
 #pragma unroll
   for (int f = 0; f < 6; f++) {
     double t[5] = {face[f][0], face[f][1], face[f][2], face[f][3], face[f][4]};
-    if (eos_clip(M, t)) {
+    if (eos_clip_fast(M, t)) {
 #pragma unroll
       for (int p = 0; p < 5; p++) face[f][p] = q[p];
       nclip++;
     }
-    nbad += eos_bad5(M, face[f]);
+    nbad += eos_bad5_fast(M, face[f]);
   }
   if (nclip) atomic_inc(&cnt[CNT_CLIPFACE], nclip);
   if (nbad) atomic_inc(&cnt[CNT_BAD], nbad);
@@ -160,7 +161,7 @@ __global__ void k_reconstruct_ghosts(Params P, StateSet S, const int32_t* __rest
 
 __device__ __forceinline__ bool num_flux(const Params& P, int dir, const double* Vm, const double* Vp, int id, double* F) {
   const DevMat& M = P.mats.m[id];
-  if (P.flux == M2CG_FLUX_HLLC) return flux_hllc(M, dir, Vm, Vp, F);
+  if (P.flux == M2CG_FLUX_HLLC) return flux_hllc_fast(M, dir, Vm, Vp, F);
   if (P.flux == M2CG_FLUX_LLF) return flux_llf2(M, M, dir, Vm, Vp, F);
   return flux_genroe(M, dir, Vm, Vp, P.roe_delta, F);
 }
@@ -168,7 +169,7 @@ __device__ __forceinline__ bool num_flux(const Params& P, int dir, const double*
 // ---------------------------------------------------------------------------
 // K2: numerical flux of every same-material face (SpaceOperator.cpp:1692-1701,
 // 1852-1861, 2011-2020).  The thread of cell c owns the faces at its minus side.
-__global__ void k_face_flux(Params P, const int32_t* __restrict__ id, double* const* fs, double* const* F,
+__global__ void __launch_bounds__(128) k_face_flux(Params P, const int32_t* __restrict__ id, double* const* fs, double* const* F,
                             unsigned long long* cnt) {
   const Grid& g = P.g;
   int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -298,7 +299,7 @@ __global__ void k_update(Params P, StageArgs A, const int32_t* __restrict__ id, 
     double Vn[5], Un[5];
 #pragma unroll
     for (int p = 0; p < 5; p++) Vn[p] = A.in.q[p][c];
-    prim_to_cons(M, Vn, Un);
+    prim_to_cons_fast(M, Vn, Un);
     if (A.store_un) {
 #pragma unroll
       for (int p = 0; p < 5; p++) A.Un[p][c] = Un[p];
@@ -311,12 +312,12 @@ __global__ void k_update(Params P, StageArgs A, const int32_t* __restrict__ id, 
     for (int p = 0; p < 5; p++) U[p] = (A.a_own * A.Us[p][c] + A.b_un * A.Un[p][c]) + cdt * R[p];
   }
   double V[5];
-  cons_to_prim(M, U, V);
-  bool clipped = eos_clip(M, V);
+  cons_to_prim_fast(M, U, V);
+  bool clipped = eos_clip_fast(M, V);
   if (clipped) atomic_inc(&cnt[CNT_CLIPCELL]);
-  if (eos_bad5(M, V)) atomic_inc(&cnt[CNT_BAD]);
+  if (eos_bad5_fast(M, V)) atomic_inc(&cnt[CNT_BAD]);
   if (!A.last) {
-    if (clipped) prim_to_cons(M, V, U);
+    if (clipped) prim_to_cons_fast(M, V, U);
 #pragma unroll
     for (int p = 0; p < 5; p++) A.Us[p][c] = U[p];
   }
@@ -421,11 +422,13 @@ __global__ void k_dt_reduce(Params P, StateSet S, const int32_t* __restrict__ id
     const Grid& g = P.g;
     int64_t c = g.at(i, j, k);
     const DevMat& M = P.mats.m[id[c]];
-    double rho = S.q[0][c], p = S.q[4][c];
-    double cc = sqrt(fmax(eos_c2(M, rho, eos_e(M, rho, p)), 0.0));
-    if (g.nx > 1) m = fmin(m, g.dx / (fabs(S.q[1][c]) + cc));
-    if (g.ny > 1) m = fmin(m, g.dy / (fabs(S.q[2][c]) + cc));
-    if (g.nz > 1) m = fmin(m, g.dz / (fabs(S.q[3][c]) + cc));
+    double V[5] = {S.q[0][c], S.q[1][c], S.q[2][c], S.q[3][c], S.q[4][c]};
+    Side sd;
+    side_eos(M, V, 0, sd);
+    double cc = sd.c;
+    if (g.nx > 1) m = fmin(m, g.dx * rcp_fast(fabs(V[1]) + cc));
+    if (g.ny > 1) m = fmin(m, g.dy * rcp_fast(fabs(V[2]) + cc));
+    if (g.nz > 1) m = fmin(m, g.dz * rcp_fast(fabs(V[3]) + cc));
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));

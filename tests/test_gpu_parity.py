@@ -17,6 +17,17 @@ TOL1 = 1e-10
 TOL100 = 1e-8
 
 
+def state_err(a, b):
+    """Relative L-infinity per variable; the three velocity components are
+    normalized by the largest velocity magnitude (a component that is zero
+    everywhere in the oracle would otherwise be judged on rounding noise)."""
+    e = rel_linf(a, b)
+    vmax = np.sqrt((b[:, 1:4] ** 2).sum(1)).max()
+    if vmax > 0:
+        e[1:4] = np.abs(a[:, 1:4] - b[:, 1:4]).max(0) / vmax
+    return e
+
+
 def _pair(cfg, V, ID, phi):
     s = Solver(cfg, FluidState(V, ID, phi))
     o = ob.OracleSim(cfg)
@@ -91,7 +102,7 @@ def test_flux_batch_matches_oracle(flux):
 def _residual_case(cfg, V, ID, phi):
     s, o = _pair(cfg, V, ID, phi)
     R, Ro = s.ComputeResidual(), o.residual()
-    err = rel_linf(R, Ro)
+    err = state_err(R, Ro)
     assert np.all(err < TOL1), err
     if cfg.n_levelsets:
         assert rel_linf(s.LevelSetResidual(), o.levelset_residual()) < TOL1
@@ -128,7 +139,7 @@ def _steps(cfg, V, ID, phi, nsteps, tol):
         s.AdvanceOneTimeStep(dt)
     g = s.get_state()
     Vo, IDo, phio = o.download()
-    err = rel_linf(g.V, Vo)
+    err = state_err(g.V, Vo)
     assert np.all(err < tol), err
     assert rel_linf(g.Phi, phio) < tol
     np.testing.assert_array_equal(g.ID, IDo)
@@ -166,5 +177,5 @@ def test_run_loop_matches_oracle():
     Vo, IDo, _ = o.download()
     assert c["steps"] == 20
     assert abs(c["time"] - o.counters()["time"]) <= 1e-12 * c["time"]
-    assert np.all(rel_linf(g.V, Vo) < TOL100)
+    assert np.all(state_err(g.V, Vo) < TOL100)
     np.testing.assert_array_equal(g.ID, IDo)
