@@ -213,6 +213,27 @@ m2cg_status m2cg_riemann_batch(m2cg_ctx* ctx, int64_t n,
 m2cg_status m2cg_flux_batch(m2cg_ctx* ctx, int64_t n, const int32_t* dir,
                             const double* Vm, const double* Vp, const int32_t* id, double* F);
 
+/* No counterpart in the reference.  The exact Riemann solves of
+ * m2cg_riemann_batch for callers that cannot allocate device memory (a host that
+ * hands the library only its own pre-allocated buffers, or code running where
+ * new allocations are forbidden).  Needs no context and allocates nothing: the
+ * solver's scratch is a 32 MiB file-scope device array that every GPU loading
+ * the library keeps until exit.  Every array argument is a DEVICE pointer with
+ * the layout of m2cg_riemann_batch; iters and err may be NULL; cfg is a host
+ * pointer (materials and ExactRiemannSolution fields are read); stream is a
+ * cudaStream_t (NULL: default stream).  path_cap is the integration-path cache
+ * capacity per wave, 2..1024 (M2CG_ERR_CAPACITY beyond); m2cg_riemann_batch
+ * uses 1024.  Solver concurrency is 32 MiB / (48 * path_cap) threads.  An
+ * invalid material ID gives err = -2 for that problem.  Asynchronous on
+ * `stream`.  All calls share the scratch array: calls that overlap on one GPU
+ * race, so serialize them.  The first call on a device looks up the array's
+ * address; make it before any stream capture. */
+m2cg_status m2cg_riemann_batch_noalloc(const m2cg_config* cfg, int64_t n,
+                                       const double* Vm, const int32_t* idm,
+                                       const double* Vp, const int32_t* idp, const double* dir,
+                                       double* Vs, int32_t* id, double* Vsm, double* Vsp,
+                                       int32_t* iters, int32_t* err, int32_t path_cap, void* stream);
+
 /* ---- timing on the context stream -------------------------------------- */
 m2cg_status m2cg_sync(m2cg_ctx* ctx);
 /* Records CUDA event `slot` (0..15) on the context stream. */

@@ -173,6 +173,9 @@ def load(path=None):
         "m2cg_kernel_launches": (C.c_int64, [_P]),
         "m2cg_host_alloc": (C.c_void_p, [C.c_size_t]),
         "m2cg_phase_times": (C.c_int, [_P, C.c_int32, _D]),
+        "m2cg_riemann_batch_noalloc": (C.c_int, [C.POINTER(Config), C.c_int64, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
+                                                 C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
         "m2cg_host_free": (None, [C.c_void_p]),
     }
     for name, (res, args) in sig.items():

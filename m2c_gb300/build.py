@@ -21,6 +21,7 @@ UNITS = {
     "m2cg_kernels.cu": [],
     "m2cg_riemann_kernels.cu": ["-fmad=false"],
     "m2cg_api.cu": [],
+    "m2cg_noalloc.cu": ["-fmad=false"],
 }
 
 

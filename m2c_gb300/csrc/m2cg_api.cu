@@ -40,7 +40,17 @@ void launch_flux_batch(cudaStream_t, const Params&, int64_t, const int32_t*, con
 using namespace m2cg;
 
 static thread_local std::string g_err;
+void m2cg_set_error(const char* fmt, ...);
 static void set_err(const char* fmt, ...) {
+  char buf[512];
+  va_list a;
+  va_start(a, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, a);
+  va_end(a);
+  g_err = buf;
+}
+
+void m2cg_set_error(const char* fmt, ...) {
   char buf[512];
   va_list a;
   va_start(a, fmt);
@@ -113,7 +123,7 @@ struct m2cg_ctx {
   }
 };
 
-static m2cg_status fill_params(const m2cg_config& c, Params& P) {
+m2cg_status m2cg_fill_params(const m2cg_config& c, m2cg::Params& P) {
   if (c.nx < 1 || c.ny < 1 || c.nz < 1) { set_err("mesh dimensions must be >= 1"); return M2CG_ERR_INVALID_ARG; }
   if (c.n_materials < 1 || c.n_materials > M2CG_MAX_MATERIALS) { set_err("n_materials out of range"); return M2CG_ERR_INVALID_ARG; }
   if (c.rec_var != M2CG_VAR_PRIMITIVE) { set_err("only primitive-variable reconstruction is supported"); return M2CG_ERR_INVALID_ARG; }
@@ -348,7 +358,7 @@ m2cg_status m2cg_create(const m2cg_config* cfg, m2cg_ctx** out) {
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_err("no CUDA device"); return M2CG_ERR_NO_DEVICE; }
   m2cg_ctx* x = new m2cg_ctx();
   x->cfg = *cfg;
-  m2cg_status st = fill_params(*cfg, x->P);
+  m2cg_status st = m2cg_fill_params(*cfg, x->P);
   if (st != M2CG_OK) { delete x; return st; }
   int dev = 0;
   cudaGetDevice(&dev);
