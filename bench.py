@@ -218,11 +218,13 @@ def run_gb300(args):
     solves = c1["riemann_solves"] - c0["riemann_solves"]
     iters = c1["riemann_iterations"] - c0["riemann_iterations"]
 
-    # per-phase device times (CUDA events around every kernel, same stream)
-    ph = np.zeros(8)
+    # per-phase device times (CUDA events around every kernel; the straggler
+    # Riemann solves overlap reconstruction and face fluxes on a second stream)
+    ph = np.zeros(9)
     nph = 2
     abi.check(lib, lib.m2cg_phase_times(ctx, nph, abi.dptr(ph)), "phase_times")
-    names = ["dt", "compact", "reconstruct", "face_flux", "riemann", "update", "bc", "end_of_step"]
+    names = ["dt", "compact", "reconstruct", "face_flux", "riemann", "update", "bc", "end_of_step",
+             "riemann_stragglers"]
     phase = {n: float(v) / nph for n, v in zip(names, ph)}
     dom = max(("reconstruct", "face_flux", "update"), key=lambda n: phase[n])
     # algorithmic bytes per cell-stage for each stage kernel (binary64 state, int32 IDs)

@@ -243,9 +243,12 @@ m2cg_status m2cg_event_elapsed(m2cg_ctx* ctx, int32_t slot0, int32_t slot1, floa
 /* Runs n_steps CFL-driven steps launch by launch with a CUDA event pair around
  * every kernel and returns the summed device milliseconds per phase:
  * [0] dt reduction, [1] interface compaction, [2] reconstruction, [3] face fluxes,
- * [4] interface Riemann solves, [5] residual gather + stage update, [6] boundary
- * conditions, [7] end-of-step material update. */
-m2cg_status m2cg_phase_times(m2cg_ctx* ctx, int32_t n_steps, double ms[8]);
+ * [4] interface Riemann solves (first, budgeted pass), [5] residual gather +
+ * stage update, [6] boundary conditions, [7] end-of-step material update,
+ * [8] interface Riemann solves that outlasted the first pass (these run
+ * concurrently with [2] and [3], so the phases overlap in time). */
+#define M2CG_N_PHASES 9
+m2cg_status m2cg_phase_times(m2cg_ctx* ctx, int32_t n_steps, double ms[M2CG_N_PHASES]);
 /* Kernel launches issued on this context since creation (all kernels are this library's). */
 int64_t     m2cg_kernel_launches(m2cg_ctx* ctx);
 /* Page-locked host memory for fast upload / download (NULL on failure). */

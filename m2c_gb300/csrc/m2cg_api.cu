@@ -4,6 +4,7 @@
 #include <cstdio>
 #include <cstring>
 #include <cstdarg>
+#include <cstdlib>
 #include <vector>
 #include <string>
 #include <algorithm>
@@ -28,8 +29,13 @@ void launch_unpack(cudaStream_t, const Params&, const double*, const int32_t*, c
 void launch_pack(cudaStream_t, const Params&, const StateSet&, const int32_t*, double*, int32_t*, double*,
                  double* const*, double*, const double*, double*);
 void launch_riemann_interfaces(cudaStream_t, const Params&, const Mats*, const StateSet&, const int32_t*,
-                               double* const*, const IfaceList&, int, double*, int, int, int, const float*,
-                               unsigned long long*, const DevScalars*);
+                               double* const*, const IfaceList&, int, double*, int, int, int, int, int32_t*,
+                               unsigned long long*, const float*, unsigned long long*, const DevScalars*);
+void launch_riemann_stragglers(cudaStream_t, const Params&, const Mats*, const StateSet&, const int32_t*,
+                               double* const*, const IfaceList&, int, double*, int, int, size_t, const int32_t*,
+                               const unsigned long long*, const float*, unsigned long long*, const DevScalars*);
+cudaError_t riemann_stragglers_reserve(size_t bytes);
+void launch_hold(cudaStream_t, long long);
 void launch_riemann_batch(cudaStream_t, const Params&, const Mats*, int64_t, const double*, const int32_t*,
                           const double*, const int32_t*, const double*, double*, int32_t*, double*, double*, int32_t*,
                           int32_t*, double*, int, int, int, const double*);
@@ -72,6 +78,8 @@ struct m2cg_ctx {
   m2cg_config cfg;
   Params P;
   cudaStream_t stream = nullptr;
+  cudaStream_t stream2 = nullptr;     // interface Riemann work, overlapped with reconstruction + fluxes
+  cudaEvent_t ev_fork = nullptr, ev_join = nullptr;
   int nsm = 0;
   std::vector<void*> allocs;
   Mats* d_mats = nullptr;
@@ -98,11 +106,22 @@ struct m2cg_ctx {
   // problems (767); a solve that would exceed it is counted in CNT_PATH_CAPPED.
   int path_cap = 1024;
   int rblocks = 0, rthreads = 128;
+  // Interface solves run in two passes (k_riemann_interfaces with an
+  // evaluation budget, then k_riemann_stragglers for the faces that outlast
+  // it) on stream2, which has the highest priority so that the straggler
+  // blocks are placed on empty SMs before the reconstruction kernel's.
+  int eval_limit = 16;
+  int sblocks = 0;             // straggler blocks of 128 threads (one SM each; idle ones exit at once)
+  size_t sreserve = 0;         // their dynamic shared-memory request
+  int32_t* strag = nullptr;
+  unsigned long long* strag_count = nullptr;
+  cudaEvent_t ev_a = nullptr;  // end of the first pass
+  long long hold_cycles = 40000;  // ~20 us head start for the straggler blocks
   double* partial = nullptr;
   double* stage_V = nullptr;
   int32_t* stage_id = nullptr;
   double* stage_phi = nullptr;
-  cudaEvent_t ev[16];
+  cudaEvent_t ev[16] = {};
   int64_t launches = 0;
   int64_t launches_per_step = 0;
   cudaGraphExec_t graph_exec = nullptr;
@@ -215,6 +234,23 @@ static m2cg_status ctx_alloc(m2cg_ctx* x) {
   x->rblocks = x->nsm * 2;
   x->rthreads = 128;
   CK(x->alloc(&x->scratch, (size_t)6 * x->path_cap * x->rblocks * x->rthreads));
+  CK(x->alloc(&x->strag, L.cap));
+  CK(x->alloc(&x->strag_count, 1));
+  x->sblocks = std::max(1, std::min(x->nsm, x->rblocks));
+  // tuning overrides: M2CG_RIEMANN_EVAL_LIMIT (first-pass budget, 0 = none),
+  // M2CG_RIEMANN_STRAGGLER_SMS (blocks of the second pass, one SM each) and
+  // M2CG_RIEMANN_HOLD_CYCLES (head start of the second pass, SM clock cycles)
+  if (const char* e = getenv("M2CG_RIEMANN_EVAL_LIMIT")) x->eval_limit = std::max(0, atoi(e));
+  if (const char* e = getenv("M2CG_RIEMANN_STRAGGLER_SMS")) x->sblocks = std::min(x->rblocks, std::max(1, atoi(e)));
+  if (const char* e = getenv("M2CG_RIEMANN_HOLD_CYCLES")) x->hold_cycles = std::max(0ll, atoll(e));
+  {
+    int dev = 0, optin = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    // without the reservation the results are the same, only slower
+    x->sreserve = (optin > 0 && riemann_stragglers_reserve((size_t)optin) == cudaSuccess) ? (size_t)optin : 0;
+    cudaGetLastError();
+  }
   int64_t nreal = (int64_t)x->P.g.nx * x->P.g.ny * x->P.g.nz;
   CK(x->alloc(&x->partial, (size_t)((nreal + 255) / 256) * 5));
   DevScalars s0;
@@ -228,31 +264,56 @@ static m2cg_status ctx_alloc(m2cg_ctx* x) {
 }
 
 // Optional per-phase CUDA-event timing of a step (m2cg_phase_times).
-enum { PH_DT = 0, PH_COMPACT, PH_RECON, PH_FLUX, PH_RIEMANN, PH_UPDATE, PH_BC, PH_POST, PH_N };
+enum { PH_DT = 0, PH_COMPACT, PH_RECON, PH_FLUX, PH_RIEMANN, PH_UPDATE, PH_BC, PH_POST, PH_RIEMANN_B, PH_N };
+static_assert(PH_N == M2CG_N_PHASES, "phase list");
 struct PhaseTimer {
   std::vector<cudaEvent_t> ev;
   std::vector<int> cat;
   size_t used = 0;
   cudaStream_t s = nullptr;
-  void begin(int c) {
+  cudaStream_t cur = nullptr;
+  void begin(int c, cudaStream_t st) {
     if (used + 2 > ev.size()) { cudaEvent_t a, b; cudaEventCreate(&a); cudaEventCreate(&b); ev.push_back(a); ev.push_back(b); cat.push_back(0); cat.push_back(0); }
     cat[used] = c;
-    cudaEventRecord(ev[used], s);
+    cur = st;
+    cudaEventRecord(ev[used], st);
   }
-  void end() { cudaEventRecord(ev[used + 1], s); used += 2; }
+  void end() { cudaEventRecord(ev[used + 1], cur); used += 2; }
 };
 static PhaseTimer* g_timer = nullptr;  // set only inside m2cg_phase_times (not captured in graphs)
-#define PHASE(c, stmt) do { if (g_timer) g_timer->begin(c); stmt; if (g_timer) g_timer->end(); } while (0)
+#define PHASE_ON(c, st, stmt) do { if (g_timer) g_timer->begin(c, st); stmt; if (g_timer) g_timer->end(); } while (0)
+#define PHASE(c, stmt) PHASE_ON(c, s, stmt)
 
 // Enqueue one Runge-Kutta stage.
 static int64_t enqueue_stage(m2cg_ctx* x, int stage, bool last, const StateSet& in, const StateSet& out) {
   cudaStream_t s = x->stream;
   const Params& P = x->P;
   int64_t n = 0;
-  PHASE(PH_RECON, launch_reconstruct(s, P, in, x->id, x->d_fs, x->cnt)); n += 2;
+  // Interface Riemann solves on stream2: the budgeted first pass alone on the
+  // GPU, then the stragglers on a few reserved SMs while this stream
+  // reconstructs and evaluates the same-material face fluxes on the others.
+  // With ReconstructionAtInterface = Constant the solves read the cell-centre
+  // stage input and go first; otherwise they follow the reconstruction.
+  const bool after_recon = (P.mp_recon != M2CG_MPREC_CONSTANT);
+  if (after_recon) { PHASE(PH_RECON, launch_reconstruct(s, P, in, x->id, x->d_fs, x->cnt)); n += 2; }
+  cudaEventRecord(x->ev_fork, s);
+  cudaStreamWaitEvent(x->stream2, x->ev_fork, 0);
+  PHASE_ON(PH_RIEMANN, x->stream2,
+           launch_riemann_interfaces(x->stream2, P, x->d_mats, in, x->id, x->d_fs, x->L, stage == 0, x->scratch,
+                                     x->path_cap, x->rblocks, x->rthreads, x->eval_limit, x->strag, x->strag_count,
+                                     nullptr, x->cnt, x->sc));
+  cudaEventRecord(x->ev_a, x->stream2);
+  PHASE_ON(PH_RIEMANN_B, x->stream2,
+           launch_riemann_stragglers(x->stream2, P, x->d_mats, in, x->id, x->d_fs, x->L, stage == 0, x->scratch,
+                                     x->path_cap, x->sblocks, x->sreserve, x->strag, x->strag_count, nullptr, x->cnt,
+                                     x->sc));
+  cudaEventRecord(x->ev_join, x->stream2);
+  n += 2;
+  cudaStreamWaitEvent(s, x->ev_a, 0);
+  if (x->hold_cycles > 0) { launch_hold(s, x->hold_cycles); n++; }
+  if (!after_recon) { PHASE(PH_RECON, launch_reconstruct(s, P, in, x->id, x->d_fs, x->cnt)); n += 2; }
   PHASE(PH_FLUX, launch_face_flux(s, P, x->id, x->d_fs, x->d_F, x->cnt)); n++;
-  PHASE(PH_RIEMANN, launch_riemann_interfaces(s, P, x->d_mats, in, x->id, x->d_fs, x->L, stage == 0, x->scratch,
-                                              x->path_cap, x->rblocks, x->rthreads, nullptr, x->cnt, x->sc)); n++;
+  cudaStreamWaitEvent(s, x->ev_join, 0);
   StageArgs A;
   memset(&A, 0, sizeof(A));
   A.in = in;
@@ -363,9 +424,15 @@ m2cg_status m2cg_create(const m2cg_config* cfg, m2cg_ctx** out) {
   int dev = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&x->nsm, cudaDevAttrMultiProcessorCount, dev);
-  if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess) {
-    set_err("cudaStreamCreate failed");
-    delete x;
+  int prio_low = 0, prio_high = 0;
+  if (cudaStreamCreateWithFlags(&x->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaDeviceGetStreamPriorityRange(&prio_low, &prio_high) != cudaSuccess ||
+      cudaStreamCreateWithPriority(&x->stream2, cudaStreamNonBlocking, prio_high) != cudaSuccess ||
+      cudaEventCreateWithFlags(&x->ev_a, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&x->ev_fork, cudaEventDisableTiming) != cudaSuccess ||
+      cudaEventCreateWithFlags(&x->ev_join, cudaEventDisableTiming) != cudaSuccess) {
+    set_err("cudaStreamCreate / cudaEventCreate failed");
+    m2cg_destroy(x);
     return M2CG_ERR_CUDA;
   }
   st = ctx_alloc(x);
@@ -382,6 +449,10 @@ void m2cg_destroy(m2cg_ctx* x) {
   for (void* p : x->batch) cudaFree(p);
   if (x->batch_scratch) cudaFree(x->batch_scratch);
   for (int i = 0; i < 16; i++) if (x->ev[i]) cudaEventDestroy(x->ev[i]);
+  if (x->stream2) { cudaStreamSynchronize(x->stream2); cudaStreamDestroy(x->stream2); }
+  if (x->ev_fork) cudaEventDestroy(x->ev_fork);
+  if (x->ev_a) cudaEventDestroy(x->ev_a);
+  if (x->ev_join) cudaEventDestroy(x->ev_join);
   if (x->stream) cudaStreamDestroy(x->stream);
   delete x;
 }
@@ -453,14 +524,16 @@ m2cg_status m2cg_compute_residual(m2cg_ctx* x, double* R) {
   launch_reconstruct(s, x->P, x->S[0], x->id, x->d_fs, x->cnt);
   launch_face_flux(s, x->P, x->id, x->d_fs, x->d_F, x->cnt);
   launch_riemann_interfaces(s, x->P, x->d_mats, x->S[0], x->id, x->d_fs, x->L, 1, x->scratch, x->path_cap, x->rblocks,
-                            x->rthreads, nullptr, x->cnt, nullptr);
+                            x->rthreads, x->eval_limit, x->strag, x->strag_count, nullptr, x->cnt, nullptr);
+  launch_riemann_stragglers(s, x->P, x->d_mats, x->S[0], x->id, x->d_fs, x->L, 1, x->scratch, x->path_cap, x->sblocks,
+                            x->sreserve, x->strag, x->strag_count, nullptr, x->cnt, nullptr);
   StageArgs A;
   memset(&A, 0, sizeof(A));
   A.in = x->S[0];
   A.residual_only = 1;
   for (int p = 0; p < 5; p++) A.R[p] = x->R[p];
   launch_update(s, x->P, A, x->id, x->id_new, x->d_F, x->L, x->sc, x->swept, x->swept_count, x->swept_cap, x->cnt);
-  x->launches += 6;
+  x->launches += 7;
   if (R) {
     int64_t n = (int64_t)x->P.g.nx * x->P.g.ny * x->P.g.nz;
     double* dR;
@@ -538,7 +611,8 @@ m2cg_status m2cg_run(m2cg_ctx* x, int32_t n_steps, m2cg_counters* counters) {
     CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
     x->launches_per_step = enqueue_step(x, 1, 0.0);
     CK(cudaStreamEndCapture(s, &g));
-    CK(cudaGraphInstantiate(&x->graph_exec, g, 0));
+    // node priorities keep stream2's priority for the straggler kernel
+    CK(cudaGraphInstantiate(&x->graph_exec, g, cudaGraphInstantiateFlagUseNodePriority));
     cudaGraphDestroy(g);
   }
   for (int i = 0; i < n_steps; i++) {
@@ -653,7 +727,7 @@ m2cg_status m2cg_flux_batch(m2cg_ctx* x, int64_t n, const int32_t* dir, const do
   return M2CG_OK;
 }
 
-m2cg_status m2cg_phase_times(m2cg_ctx* x, int32_t n_steps, double ms[8]) {
+m2cg_status m2cg_phase_times(m2cg_ctx* x, int32_t n_steps, double ms[M2CG_N_PHASES]) {
   if (!x || !ms || n_steps < 1) return M2CG_ERR_INVALID_ARG;
   PhaseTimer t;
   t.s = x->stream;

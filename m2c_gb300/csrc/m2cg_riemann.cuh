@@ -50,6 +50,18 @@ struct ExactRiemannDev {
   double warm_p;   // > 0 replaces the acoustic-theory p0 (learned warm start)
   bool nonadaptive;  // running as the reference's non-adaptive fallback solver
   int fallback;      // 1 if the last solve needed the non-adaptive retry
+  // Evaluation budget: with eval_limit > 0 a solve that reaches eval_limit
+  // wave-pair evaluations stops and returns 2 ("suspended"); its outputs are
+  // then meaningless and the caller solves the problem again without a limit.
+  // The evaluations themselves are untouched, so a solve that finishes within
+  // the budget returns exactly what an unlimited solve returns.
+  int eval_limit = 0;
+  bool suspended = false;
+
+  M2CG_DEV bool over_budget() {
+    if (eval_limit > 0 && evals >= eval_limit) suspended = true;
+    return suspended;
+  }
 
   M2CG_DEV const DevMat& mat(int id) const { return mats->m[id]; }
 
@@ -287,12 +299,17 @@ struct ExactRiemannDev {
           Vrare[1] = w0 * us_0 + w1 * us_1;
           Vrare[2] = w0 * ps_0 + w1 * ps_1;
         }
-        double tr = 0.9 * dp * pow(fabs(errBar / rS), 0.2);
-        double tu = 0.9 * dp * pow(fabs(errBar / uS), 0.2);
-        double t = fmin(tr, tu);
-        t = fmin(t, 10 * dp);
-        t = fmax(t, dp_min);
-        dp = fmin(t, ps_1 - ps);
+        // the next step size; skipped when the next pass ends the loop and
+        // never reads it (the common case of a solve that restarts from the
+        // path cache: one step to the end point)
+        if (!(fabs(ps_1 - ps) <= tol_end) && i + 1 < P.numSteps * 3) {
+          double tr = 0.9 * dp * pow(fabs(errBar / rS), 0.2);
+          double tu = 0.9 * dp * pow(fabs(errBar / uS), 0.2);
+          double t = fmin(tr, tu);
+          t = fmin(t, 10 * dp);
+          t = fmax(t, dp_min);
+          dp = fmin(t, ps_1 - ps);
+        }
         rhos_0 = rhos_1; us_0 = us_1; ps_0 = ps_1; xi_0 = xi_1;
       }
       if (!done) return false;
@@ -381,6 +398,7 @@ struct ExactRiemannDev {
 
   M2CG_DEV bool pair(double p, double rhol, double ul, double pl, int idl, double rhor, double ur, double pr, int idr,
                      double gl0, double gl1, double gr0, double gr1, double& rl, double& uL, double& rr, double& uR) {
+    if (over_budget()) return false;
     evals++;
     bool s = rho_u_star(1, path1, rhol, ul, pl, p, idl, gl0, gl1, rl, uL, nullptr, nullptr);
     return s && rho_u_star(3, path3, rhor, ur, pr, p, idr, gr0, gr1, rr, uR, nullptr, nullptr);
@@ -422,7 +440,7 @@ struct ExactRiemannDev {
         if (p0 < P.min_pressure) p0 = P.pressure_at_failure;
         ok = pair(p0, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol, (p0 > pl) ? rhol * 1.1 : rhol * 0.9, rhor,
                   (p0 > pr) ? rhor * 1.1 : rhor * 0.9, rhol0, ul0, rhor0, ur0);
-        if (ok) break;
+        if (ok || suspended) break;
       }
       if (!ok) {
         for (int i = 0; i < P.maxIts_bracket; i++) {
@@ -430,7 +448,7 @@ struct ExactRiemannDev {
           if (p0 < P.min_pressure || i == P.maxIts_bracket / 2) p0 = P.pressure_at_failure;
           ok = pair(p0, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol, (p0 > pl) ? rhol * 1.1 : rhol * 0.9, rhor,
                     (p0 > pr) ? rhor * 1.1 : rhor * 0.9, rhol0, ul0, rhor0, ur0);
-          if (ok) break;
+          if (ok || suspended) break;
         }
       }
       if (!ok) return false;
@@ -439,14 +457,14 @@ struct ExactRiemannDev {
     for (int i = 0; i < P.maxIts_bracket; i++) {
       p1 = p0 + 0.01 * (i + 1) * (i + 1) * dp;
       ok = pair(p1, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol, rhol0, rhor, rhor0, rhol1, ul1, rhor1, ur1);
-      if (ok) break;
+      if (ok || suspended) break;
     }
     if (!ok) {
       for (int i = 0; i < P.maxIts_bracket; i++) {
         p1 = p0 - 0.01 * (i + 1) * (i + 1) * dp;
         if (p1 < P.min_pressure) p1 = P.pressure_at_failure * 1000.0;
         ok = pair(p1, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol, rhol0, rhor, rhor0, rhol1, ul1, rhor1, ur1);
-        if (ok) break;
+        if (ok || suspended) break;
       }
     }
     if (!ok) return false;
@@ -467,6 +485,7 @@ struct ExactRiemannDev {
                         double& p1, double& rhol1, double& rhor1, double& ul1, double& ur1) {
     bool ok = feasible(rhol, ul, pl, cl, idl, rhor, ur, pr, cr, idr, p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
     if (!ok) { p0 = p1 = P.pressure_at_failure; return false; }
+    if (suspended) return false;
     double p2 = 0, rhol2 = 0, rhor2 = 0, ul2 = 0, ur2 = 0, f0, f1;
     double fmin_, p_f, rl_f, rr_f, ul_f, ur_f;
     if (fabs(ul0 - ur0) < fabs(ul1 - ur1)) { fmin_ = fabs(ul0 - ur0); p_f = p0; rl_f = rhol0; rr_f = rhor0; ul_f = ul0; ur_f = ur0; }
@@ -488,10 +507,11 @@ struct ExactRiemannDev {
           if (p2 < p0) p2 = p0 - 0.5 * (p0 - p2);
           else p2 = p1 + 0.5 * (p2 - p1);
           ok = pair(p2, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol0, rhol1, rhor0, rhor1, rhol2, ul2, rhor2, ur2);
-          if (ok) break;
+          if (ok || suspended) break;
         }
       }
       if (!ok) break;
+      if (suspended) return false;
       if (fabs(ul2 - ur2) < fmin_) { fmin_ = fabs(ul2 - ur2); p_f = p2; rl_f = rhol2; rr_f = rhor2; ul_f = ul2; ur_f = ur2; }
       if (p2 < p0) {
         p1 = p0; rhol1 = rhol0; rhor1 = rhor0; ul1 = ul0; ur1 = ur0;
@@ -550,12 +570,15 @@ struct ExactRiemannDev {
   }
 
   // ExactRiemannSolverBase.cpp:59-347 with the non-adaptive retry after a failure
-  // (lines 178-193 and 323-337).  Returns 0 (ok), 1 (failed), -1 (nonphysical input).
+  // (lines 178-193 and 323-337).  Returns 0 (ok), 1 (failed), -1 (nonphysical
+  // input) or 2 (evaluation budget spent, see eval_limit).
   __device__ __noinline__ int solve(const double* dir, const double* Vm, int idl, const double* Vp, int idr, double* Vs,
                                     int& id, double* Vsm, double* Vsp) {
     nonadaptive = false;
     fallback = 0;
+    suspended = false;
     int e = solve_once(dir, Vm, idl, Vp, idr, Vs, id, Vsm, Vsp);
+    if (e == 2) return 2;
     if (e == 1) {
       int ev = evals;
       double w = warm_p;
@@ -600,6 +623,7 @@ struct ExactRiemannDev {
       return 0;
     }
     bool ok = bracket(rhol, ul, pl, cl, idl, rhor, ur, pr, cr, idr, p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
+    if (suspended) return 2;
     if (!ok) {
       ok = rho_u_star(1, path1, rhol, ul, pl, p1, idl, rhol0, rhol0 * 1.1, rhol2, ul2, &trans_rare, Vrare);
       ok = ok && rho_u_star(3, path3, rhor, ur, pr, p1, idr, rhor0, rhol0 * 1.1, rhor2, ur2, &trans_rare, Vrare);
@@ -628,6 +652,7 @@ struct ExactRiemannDev {
       // the reference's "try_again" loop (ExactRiemannSolverBase.cpp:239-278)
       bool pass = false;
       while (true) {
+        if (over_budget()) return 2;
         evals++;
         if (!rho_u_star(1, path1, rhol, ul, pl, p2, idl, rhol0, rhol1, rhol2, ul2, &trans_rare, Vrare)) {
           p2 = 0.5 * (p2 + p0);

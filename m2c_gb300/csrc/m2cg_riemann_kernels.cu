@@ -18,85 +18,163 @@ __device__ __forceinline__ bool num_flux_if(const Params& P, int dir, const doub
   return flux_genroe(M, dir, Vm, Vp, P.roe_delta, F);
 }
 
-// One thread per interface face (grid-stride over the device-side count).
-// scratch: 6 * cap doubles per thread for the two integration-path caches.
-__global__ void k_riemann_interfaces(Params P, const Mats* __restrict__ md, StateSet S, const int32_t* __restrict__ id,
-                                     double* const* fs, IfaceList L, int store, double* scratch, int path_cap,
-                                     const float* warm, unsigned long long* cnt, const DevScalars* sc) {
-  if (sc && !sc->active) return;
-  const Grid& g = P.g;
-  int64_t n = (int64_t)min((unsigned long long)L.cap, *L.count);
-  int64_t T = (int64_t)gridDim.x * blockDim.x;
-  int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  ExactRiemannDev rs;
+// Loads the two states of interface face s (cell centres or reconstructed face
+// states, SpaceOperator.cpp:1633-1639).
+__device__ __forceinline__ void iface_inputs(const Params& P, const StateSet& S, const int32_t* __restrict__ id,
+                                             double* const* fs, const IfaceList& L, int64_t s, int& d, int64_t& c,
+                                             int& idm, int& idp, double* Vm, double* Vp) {
+  const int64_t st[3] = {1, P.g.sy, P.g.sz};
+  int64_t fc = L.face[s];
+  d = (int)(fc & 3);
+  c = fc >> 2;
+  int64_t m = c - st[d];
+  idm = id[m];
+  idp = id[c];
+  if (P.mp_recon == M2CG_MPREC_CONSTANT) {
+    for (int p = 0; p < 5; p++) { Vm[p] = S.q[p][m]; Vp[p] = S.q[p][c]; }
+  } else {
+    for (int p = 0; p < 5; p++) { Vm[p] = fs[(2 * d + 1) * 5 + p][m]; Vp[p] = fs[(2 * d) * 5 + p][c]; }
+  }
+}
+
+// Clip and check the star states, store them for the end-of-step update (first
+// stage only) and form the two one-sided fluxes (SpaceOperator.cpp:1641-1690).
+__device__ __forceinline__ int iface_finish(const Params& P, const IfaceList& L, int64_t s, int d, int idm, int idp,
+                                            const double* Vm, const double* Vp, double* Vs, int midid, double* Vsm,
+                                            double* Vsp, int err, int store) {
+  int bad = 0;
+  eos_clip(P.mats.m[idm], Vsm);
+  bad += eos_bad5(P.mats.m[idm], Vsm);
+  eos_clip(P.mats.m[idp], Vsp);
+  bad += eos_bad5(P.mats.m[idp], Vsp);
+  if (store) {
+    L.err[s] = err ? 1 : 0;
+    for (int p = 0; p < 5; p++) { L.vsm[p][s] = Vsm[p]; L.vsp[p][s] = Vsp[p]; }
+  }
+  double lf1[5], lf2[5];
+  if (P.mp_flux == M2CG_MPFLUX_EXACT) {
+    phys_flux(P.mats.m[midid], d, Vs, lf1);
+    for (int p = 0; p < 5; p++) lf2[p] = lf1[p];
+  } else {
+    bad += !num_flux_if(P, d, Vm, Vsm, idm, lf1);
+    bad += !num_flux_if(P, d, Vsp, Vp, idp, lf2);
+  }
+  for (int p = 0; p < 5; p++) { L.lf1[p][s] = lf1[p]; L.lf2[p][s] = lf2[p]; }
+  return bad;
+}
+
+__device__ __forceinline__ void init_solver(ExactRiemannDev& rs, const Mats* md, const RiemannPrm& rp, double* scratch,
+                                            int path_cap, int64_t tid, int64_t T) {
   rs.mats = md;
-  rs.P = P.rp;
+  rs.P = rp;
+  rs.warm_p = 0.0;
+  rs.nonadaptive = false;
+  rs.fallback = 0;
   rs.path1.base = scratch + tid;
   rs.path1.stride = T;
   rs.path1.cap = path_cap;
   rs.path3.base = scratch + (int64_t)3 * path_cap * T + tid;
   rs.path3.stride = T;
   rs.path3.cap = path_cap;
-  const int64_t st[3] = {1, g.sy, g.sz};
+}
+
+// Solves interface face s and stores its fluxes; returns 2 without storing
+// anything when the solver's evaluation budget ran out.
+__device__ __forceinline__ int iface_solve(const Params& P, StateSet S, const int32_t* __restrict__ id,
+                                           double* const* fs, const IfaceList& L, int store, const float* warm,
+                                           int64_t s, ExactRiemannDev& rs, unsigned long long (&acc)[6]) {
+  int d, idm, idp;
+  int64_t c;
+  double Vm[5], Vp[5];
+  iface_inputs(P, S, id, fs, L, s, d, c, idm, idp, Vm, Vp);
+  if (P.mp_flux == M2CG_MPFLUX_LLF) {   // SpaceOperator.cpp:1617-1626: no Riemann solve
+    double lf[5];
+    acc[3] += !flux_llf2(P.mats.m[idm], P.mats.m[idp], d, Vm, Vp, lf);
+    for (int p = 0; p < 5; p++) { L.lf1[p][s] = lf[p]; L.lf2[p][s] = lf[p]; }
+    if (store) L.err[s] = 1;  // no star states for the phase-change update
+    return 0;
+  }
+  double dir[3] = {0.0, 0.0, 0.0};
+  dir[d] = 1.0;  // RiemannNormal = Mesh (SpaceOperator.cpp:2186-2203)
+  double Vs[5], Vsm[5], Vsp[5];
+  int midid = idm;
+  rs.warm_p = warm ? (double)warm[s] : 0.0;
+  int err = rs.solve(dir, Vm, idm, Vp, idp, Vs, midid, Vsm, Vsp);
+  if (err == 2) return 2;
+  acc[0] += rs.evals;
+  acc[1]++;
+  acc[4] += rs.path1.capped | rs.path3.capped;
+  acc[5] += rs.fallback;
+  L.iters[s] = rs.evals;
+  if (err) acc[2]++;
+  if (err < 0) acc[3]++;
+  acc[3] += iface_finish(P, L, s, d, idm, idp, Vm, Vp, Vs, midid, Vsm, Vsp, err, store);
+  return err;
+}
+
+__device__ __forceinline__ void iface_counts(unsigned long long* cnt, const unsigned long long (&acc)[6]) {
+  if (acc[1]) atomicAdd(&cnt[CNT_RSOLVE], acc[1]);
+  if (acc[0]) atomicAdd(&cnt[CNT_RITER], acc[0]);
+  if (acc[2]) atomicAdd(&cnt[CNT_RERR], acc[2]);
+  if (acc[3]) atomicAdd(&cnt[CNT_BAD], acc[3]);
+  if (acc[4]) atomicAdd(&cnt[CNT_PATH_CAPPED], acc[4]);
+  if (acc[5]) atomicAdd(&cnt[CNT_FALLBACK], acc[5]);
+}
+
+// Interface Riemann solves, first pass: one thread per interface face
+// (grid-stride over the device-side count), each solve limited to eval_limit
+// wave-pair evaluations.  Nearly every face converges within a handful; the
+// few that do not -- the reference's stalled secant iterations that run to
+// MaxIts and then repeat with the non-adaptive solver (ExactRiemannSolverBase.cpp
+// :178-193, 323-337), several hundred evaluations in sequence -- are listed in
+// strag[] for k_riemann_stragglers.  scratch: 6 * path_cap doubles per thread.
+__global__ void k_riemann_interfaces(Params P, const Mats* __restrict__ md, StateSet S, const int32_t* __restrict__ id,
+                                     double* const* fs, IfaceList L, int store, double* scratch, int path_cap,
+                                     int eval_limit, int32_t* strag, unsigned long long* strag_count,
+                                     const float* warm, unsigned long long* cnt, const DevScalars* sc) {
+  if (sc && !sc->active) return;
+  int64_t n = (int64_t)min((unsigned long long)L.cap, *L.count);
+  int64_t T = (int64_t)gridDim.x * blockDim.x;
+  int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  ExactRiemannDev rs;
+  init_solver(rs, md, P.rp, scratch, path_cap, tid, T);
+  rs.eval_limit = eval_limit;
   if (tid == 0) atomicAdd(&cnt[CNT_IFACE], (unsigned long long)n);
-  unsigned long long iters = 0, solves = 0, errs = 0, bad = 0, capped = 0, fallbacks = 0;
+  unsigned long long acc[6] = {0, 0, 0, 0, 0, 0};
   for (int64_t s = tid; s < n; s += T) {
-    int64_t fc = L.face[s];
-    int d = (int)(fc & 3);
-    int64_t c = fc >> 2;
-    int64_t m = c - st[d];
-    int idm = id[m], idp = id[c];
-    double Vm[5], Vp[5];
-    if (P.mp_recon == M2CG_MPREC_CONSTANT) {
-      for (int p = 0; p < 5; p++) { Vm[p] = S.q[p][m]; Vp[p] = S.q[p][c]; }
-    } else {
-      for (int p = 0; p < 5; p++) { Vm[p] = fs[(2 * d + 1) * 5 + p][m]; Vp[p] = fs[(2 * d) * 5 + p][c]; }
+    if (iface_solve(P, S, id, fs, L, store, warm, s, rs, acc) == 2) {
+      unsigned long long k = atomicAdd(strag_count, 1ull);   // k < L.cap: each face is listed once
+      strag[k] = (int32_t)s;
     }
-    double lf1[5], lf2[5];
-    if (P.mp_flux == M2CG_MPFLUX_LLF) {   // SpaceOperator.cpp:1617-1626
-      bad += !flux_llf2(P.mats.m[idm], P.mats.m[idp], d, Vm, Vp, lf1);
-      for (int p = 0; p < 5; p++) lf2[p] = lf1[p];
-      if (store) L.err[s] = 1;  // no star states for the phase-change update
-    } else {
-      double dir[3] = {0.0, 0.0, 0.0};
-      dir[d] = 1.0;  // RiemannNormal = Mesh (SpaceOperator.cpp:2186-2203)
-      double Vs[5], Vsm[5], Vsp[5];
-      int midid = idm;
-      rs.warm_p = warm ? (double)warm[s] : 0.0;
-      int err = rs.solve(dir, Vm, idm, Vp, idp, Vs, midid, Vsm, Vsp);
-      solves++;
-      iters += rs.evals;
-      capped += rs.path1.capped | rs.path3.capped;
-      fallbacks += rs.fallback;
-      if (err) errs++;
-      if (err < 0) bad++;
-      eos_clip(P.mats.m[idm], Vsm);
-      bad += eos_bad5(P.mats.m[idm], Vsm);
-      eos_clip(P.mats.m[idp], Vsp);
-      bad += eos_bad5(P.mats.m[idp], Vsp);
-      if (store) {
-        L.err[s] = err ? 1 : 0;
-        L.iters[s] = rs.evals;
-        for (int p = 0; p < 5; p++) { L.vsm[p][s] = Vsm[p]; L.vsp[p][s] = Vsp[p]; }
-      }
-      if (P.mp_flux == M2CG_MPFLUX_EXACT) {
-        phys_flux(P.mats.m[midid], d, Vs, lf1);
-        for (int p = 0; p < 5; p++) lf2[p] = lf1[p];
-      } else {
-        bad += !num_flux_if(P, d, Vm, Vsm, idm, lf1);
-        bad += !num_flux_if(P, d, Vsp, Vp, idp, lf2);
-      }
-    }
-    for (int p = 0; p < 5; p++) { L.lf1[p][s] = lf1[p]; L.lf2[p][s] = lf2[p]; }
   }
-  if (solves) {
-    atomicAdd(&cnt[CNT_RSOLVE], solves);
-    atomicAdd(&cnt[CNT_RITER], iters);
-  }
-  if (errs) atomicAdd(&cnt[CNT_RERR], errs);
-  if (bad) atomicAdd(&cnt[CNT_BAD], bad);
-  if (capped) atomicAdd(&cnt[CNT_PATH_CAPPED], capped);
-  if (fallbacks) atomicAdd(&cnt[CNT_FALLBACK], fallbacks);
+  iface_counts(cnt, acc);
+}
+
+// Second pass: the listed faces solved without a budget.  Each is one long
+// chain of dependent binary64 operations, so the faces are dealt round-robin
+// over the warps (lane-major), which puts as few as possible in one warp: lanes
+// of a warp that follow different faces diverge and take turns.  The launch
+// asks for (and never touches) nearly all of an SM's shared memory, so no block
+// of another kernel shares an SM -- and its FP64 unit -- with these chains while
+// the reconstruction and face-flux kernels run concurrently on the other SMs.
+__global__ void __launch_bounds__(128) k_riemann_stragglers(Params P, const Mats* __restrict__ md, StateSet S,
+                                                            const int32_t* __restrict__ id, double* const* fs,
+                                                            IfaceList L, int store, double* scratch, int path_cap,
+                                                            const int32_t* __restrict__ strag,
+                                                            const unsigned long long* strag_count, const float* warm,
+                                                            unsigned long long* cnt, const DevScalars* sc) {
+  if (sc && !sc->active) return;
+  int64_t n = (int64_t)min((unsigned long long)L.cap, *strag_count);
+  const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int64_t lane = threadIdx.x & 31;
+  int64_t T = (int64_t)gridDim.x * blockDim.x;
+  int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  ExactRiemannDev rs;
+  init_solver(rs, md, P.rp, scratch, path_cap, tid, T);
+  unsigned long long acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t k = lane * W + w; k < n; k += 32 * W) iface_solve(P, S, id, fs, L, store, warm, strag[k], rs, acc);
+  iface_counts(cnt, acc);
 }
 
 // Batched independent problems (device arrays, AoS rows of 5 / 3).
@@ -135,9 +213,39 @@ __global__ void k_flux_batch(Params P, int64_t n, const int32_t* __restrict__ di
 
 void launch_riemann_interfaces(cudaStream_t s, const Params& P, const Mats* md, const StateSet& S, const int32_t* id,
                                double* const* fs, const IfaceList& L, int store, double* scratch, int path_cap,
-                               int blocks, int threads, const float* warm, unsigned long long* cnt,
+                               int blocks, int threads, int eval_limit, int32_t* strag,
+                               unsigned long long* strag_count, const float* warm, unsigned long long* cnt,
                                const DevScalars* sc) {
-  k_riemann_interfaces<<<blocks, threads, 0, s>>>(P, md, S, id, fs, L, store, scratch, path_cap, warm, cnt, sc);
+  cudaMemsetAsync(strag_count, 0, sizeof(unsigned long long), s);
+  k_riemann_interfaces<<<blocks, threads, 0, s>>>(P, md, S, id, fs, L, store, scratch, path_cap, eval_limit, strag,
+                                                  strag_count, warm, cnt, sc);
+}
+// blocks * 128 threads must not exceed the first pass's thread count (the
+// path-cache scratch is shared); reserve_smem: dynamic shared memory per block.
+void launch_riemann_stragglers(cudaStream_t s, const Params& P, const Mats* md, const StateSet& S, const int32_t* id,
+                               double* const* fs, const IfaceList& L, int store, double* scratch, int path_cap,
+                               int blocks, size_t reserve_smem, const int32_t* strag,
+                               const unsigned long long* strag_count, const float* warm, unsigned long long* cnt,
+                               const DevScalars* sc) {
+  k_riemann_stragglers<<<blocks, 128, reserve_smem, s>>>(P, md, S, id, fs, L, store, scratch, path_cap, strag,
+                                                         strag_count, warm, cnt, sc);
+}
+// One block that holds one SM for a fixed number of clock cycles (bounded
+// loop, waits on nothing).  Launched on the main stream between the first
+// Riemann pass and the reconstruction: without it the reconstruction's blocks,
+// which become ready at the same moment as the straggler blocks, take every
+// SM, and the straggler blocks -- which need an empty SM -- wait for the face
+// fluxes to drain.
+__global__ void k_hold(long long cycles) {
+  long long t0 = clock64();
+  for (int i = 0; i < (1 << 22); i++) {
+    if (clock64() - t0 >= cycles) break;
+  }
+}
+void launch_hold(cudaStream_t s, long long cycles) { k_hold<<<1, 32, 0, s>>>(cycles); }
+
+cudaError_t riemann_stragglers_reserve(size_t bytes) {
+  return cudaFuncSetAttribute(k_riemann_stragglers, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 void launch_riemann_batch(cudaStream_t s, const Params& P, const Mats* md, int64_t n, const double* Vm, const int32_t* idm,
                           const double* Vp, const int32_t* idp, const double* dir, double* Vs, int32_t* id,
