@@ -40,6 +40,21 @@ struct PathCache {
     if (n < cap) { put(n, p, rho, u); n++; }
     else capped = 1;
   }
+  // Largest entry index whose pressure exceeds ps, or 0 if there is none --
+  // what the reference's backward linear scan of the path returns
+  // (ExactRiemannSolverBase.cpp:1246-1251, 2567-2572).  Entries are pushed only
+  // below the last one, so the pressures strictly decrease and a binary search
+  // finds the same index.
+  M2CG_DEV int last_above(double ps) const {
+    if (!(get(0, 0) > ps)) return 0;
+    int lo = 0, hi = n - 1;  // get(lo, 0) > ps
+    while (lo < hi) {
+      int mid = (lo + hi + 1) >> 1;
+      if (get(mid, 0) > ps) lo = mid;
+      else hi = mid - 1;
+    }
+    return lo;
+  }
 };
 
 struct ExactRiemannDev {
@@ -182,10 +197,7 @@ struct ExactRiemannDev {
     if (rho <= 0 || c < 0) return false;
     c = sqrt(c);
     if (path.n > 1) {
-      int index0 = 0;
-      for (int j = path.n - 1; j >= 0; j--) {
-        if (path.get(j, 0) > ps) { index0 = j; break; }
-      }
+      int index0 = path.last_above(ps);
       ps_0 = path.get(index0, 0);
       rhos_0 = path.get(index0, 1);
       us_0 = path.get(index0, 2);
@@ -247,9 +259,7 @@ struct ExactRiemannDev {
       c = sqrt(c);
       int index0 = 0;
       if (path.n > 1) {
-        for (int j = path.n - 1; j >= 0; j--) {
-          if (path.get(j, 0) > ps) { index0 = j; break; }
-        }
+        index0 = path.last_above(ps);
         ps_0 = path.get(index0, 0);
         rhos_0 = path.get(index0, 1);
         us_0 = path.get(index0, 2);

@@ -157,12 +157,17 @@ __global__ void k_riemann_interfaces(Params P, const Mats* __restrict__ md, Stat
 // asks for (and never touches) nearly all of an SM's shared memory, so no block
 // of another kernel shares an SM -- and its FP64 unit -- with these chains while
 // the reconstruction and face-flux kernels run concurrently on the other SMs.
+// That request also takes most of the SM's L1, so lane 0 of each warp -- the
+// one lane in use while there are no more faces than warps -- keeps its
+// integration-path caches in the reserved shared memory instead of going
+// through L1 to the global scratch.
 __global__ void __launch_bounds__(128) k_riemann_stragglers(Params P, const Mats* __restrict__ md, StateSet S,
                                                             const int32_t* __restrict__ id, double* const* fs,
                                                             IfaceList L, int store, double* scratch, int path_cap,
-                                                            const int32_t* __restrict__ strag,
+                                                            size_t reserve_bytes, const int32_t* __restrict__ strag,
                                                             const unsigned long long* strag_count, const float* warm,
                                                             unsigned long long* cnt, const DevScalars* sc) {
+  extern __shared__ __align__(16) double s_path[];
   if (sc && !sc->active) return;
   int64_t n = (int64_t)min((unsigned long long)L.cap, *strag_count);
   const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
@@ -172,6 +177,13 @@ __global__ void __launch_bounds__(128) k_riemann_stragglers(Params P, const Mats
   int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
   ExactRiemannDev rs;
   init_solver(rs, md, P.rp, scratch, path_cap, tid, T);
+  const size_t per_warp = (size_t)6 * path_cap;  // doubles: two waves x cap entries x {p, rho, u}
+  if (lane == 0 && (size_t)(blockDim.x >> 5) * per_warp * sizeof(double) <= reserve_bytes) {
+    rs.path1.base = s_path + (threadIdx.x >> 5) * per_warp;
+    rs.path1.stride = 1;
+    rs.path3.base = rs.path1.base + (size_t)3 * path_cap;
+    rs.path3.stride = 1;
+  }
   unsigned long long acc[6] = {0, 0, 0, 0, 0, 0};
   for (int64_t k = lane * W + w; k < n; k += 32 * W) iface_solve(P, S, id, fs, L, store, warm, strag[k], rs, acc);
   iface_counts(cnt, acc);
@@ -227,8 +239,8 @@ void launch_riemann_stragglers(cudaStream_t s, const Params& P, const Mats* md, 
                                int blocks, size_t reserve_smem, const int32_t* strag,
                                const unsigned long long* strag_count, const float* warm, unsigned long long* cnt,
                                const DevScalars* sc) {
-  k_riemann_stragglers<<<blocks, 128, reserve_smem, s>>>(P, md, S, id, fs, L, store, scratch, path_cap, strag,
-                                                         strag_count, warm, cnt, sc);
+  k_riemann_stragglers<<<blocks, 128, reserve_smem, s>>>(P, md, S, id, fs, L, store, scratch, path_cap, reserve_smem,
+                                                         strag, strag_count, warm, cnt, sc);
 }
 // One block that holds one SM for a fixed number of clock cycles (bounded
 // loop, waits on nothing).  Launched on the main stream between the first
