@@ -207,6 +207,20 @@ m2cg_status m2cg_riemann_batch(m2cg_ctx* ctx, int64_t n,
                                double* Vs, int32_t* id, double* Vsm, double* Vsp,
                                int32_t* iters, int32_t* err);
 
+/* Exact Riemann solves of independent 1D problems, each with its own pair of
+ * stiffened-gas / Noble-Abel stiffened-gas materials -- the learned warm
+ * start's training and evaluation sets (no reference counterpart: the
+ * reference solver is configured with one material table,
+ * ExactRiemannSolverBase.cpp:34-50).  Host arrays:
+ *   W      n x 6  {rho_l, u_l, p_l, rho_r, u_r, p_r}
+ *   eos    n x 10 {type (M2CG_EOS_SG / M2CG_EOS_NASG), gamma, pc, b, q} left, then right
+ *   warm_p n starting pressures (> 0: learned warm start, see m2cg_mlp_*) or NULL
+ *   out    n x 4  {p*, u*, rho*_l, rho*_r}
+ *   iters  wave-pair evaluations (bracketing + main loop), err as m2cg_riemann_batch (optional)
+ *   kernel_ms  device time of the solve kernel alone (optional). */
+m2cg_status m2cg_riemann_batch_eos(m2cg_ctx* ctx, int64_t n, const double* W, const double* eos,
+                                   const double* warm_p, double* out, int32_t* iters, int32_t* err,
+                                   float* kernel_ms);
 /* FluxFcn*::ComputeNumericalFluxAtCellInterface (FluxFcnHLLC.h:196-245,
  * FluxFcnLLF.h:80-111, FluxFcnGenRoe.h:183-213) with the context's flux type,
  * host arrays: dir n; Vm, Vp n x 5; id n; F n x 5 output. */
@@ -233,6 +247,49 @@ m2cg_status m2cg_riemann_batch_noalloc(const m2cg_config* cfg, int64_t n,
                                        const double* Vp, const int32_t* idp, const double* dir,
                                        double* Vs, int32_t* id, double* Vsm, double* Vsp,
                                        int32_t* iters, int32_t* err, int32_t path_cap, void* stream);
+
+/* ---- learned warm start for the interface Riemann solve -----------------
+ * No reference counterpart: a 16 -> 64 -> 64 -> 64 -> 1 SiLU MLP (BF16
+ * tensor-core GEMMs, FP32 accumulate, FP32 Adam) predicts the star pressure
+ * from the two states and their EOS parameters; the exact solver starts from
+ * a pair bracketing the prediction instead of the acoustic pair
+ * (ExactRiemannSolverBase.cpp:1107-1158), falls back to the acoustic start
+ * when that pair does not bracket the root within three secant expansions,
+ * and converges with the reference's stopping rule.  Problems use the
+ * m2cg_riemann_batch_eos row layout (W n x 6, eos n x 10). */
+#define M2CG_MLP_FEATURES 16
+#define M2CG_MLP_PARAMS 9473   /* W1[64][16] b1[64] W2[64][64] b2 W3[64][64] b3 w4[64] b4 (FP32) */
+typedef struct m2cg_mlp m2cg_mlp;
+m2cg_status m2cg_mlp_create(uint64_t seed, m2cg_mlp** out);
+void m2cg_mlp_destroy(m2cg_mlp* mlp);
+m2cg_status m2cg_mlp_set_params(m2cg_mlp* mlp, const float* params);
+m2cg_status m2cg_mlp_get_params(m2cg_mlp* mlp, float* params);
+/* Network inputs (n x 16, BF16-rounded, returned as float), the reference
+ * pressure p_ref of each problem (optional) and, when pstar and t are given,
+ * the targets t = ln(p* / p_ref) / 4 (the prediction is p_ref exp(4 t)). */
+m2cg_status m2cg_mlp_features(int64_t n, const double* W, const double* eos, const double* pstar, float* X,
+                              float* pref, float* t);
+/* Keeps features and targets of a labelled set on the device for training. */
+m2cg_status m2cg_mlp_set_data(m2cg_mlp* mlp, int64_t n, const double* W, const double* eos, const double* pstar);
+/* Mini-batch Adam (cosine learning-rate decay to lr / 20) on the squared error
+ * of t over the stored set, reshuffled every epoch, whole batches only.
+ * loss_per_epoch (optional, epochs entries): mean loss during each epoch;
+ * ms: device time. */
+m2cg_status m2cg_mlp_train(m2cg_mlp* mlp, int32_t epochs, int32_t batch, float lr, uint64_t seed,
+                           float* loss_per_epoch, float* ms);
+/* One forward + backward pass over X (n x 16) and targets t without an update:
+ * gradient of the mean squared error (M2CG_MLP_PARAMS floats) and the loss. */
+m2cg_status m2cg_mlp_grad(m2cg_mlp* mlp, int64_t n, const float* X, const float* t, float* grad, float* loss);
+/* Network output t for features X (n x 16). */
+m2cg_status m2cg_mlp_forward(m2cg_mlp* mlp, int64_t n, const float* X, float* t);
+/* Predicted star pressures (0 where the prediction is not positive) for
+ * problems W / eos; kernel_ms: device time of features + network. */
+m2cg_status m2cg_mlp_predict(m2cg_mlp* mlp, int64_t n, const double* W, const double* eos, double* p_pred,
+                             float* kernel_ms);
+/* Warm-start the interface solves of the finite-volume step with this network
+ * (NULL: cold start, the reference behaviour).  The network must outlive its
+ * use by the context; the step's CUDA graph is captured again. */
+m2cg_status m2cg_set_warm_start(m2cg_ctx* ctx, m2cg_mlp* mlp);
 
 /* ---- timing on the context stream -------------------------------------- */
 m2cg_status m2cg_sync(m2cg_ctx* ctx);

@@ -126,6 +126,7 @@ def set_material(m, eos, gamma=1.4, pc=0.0, b=0.0, q=0.0, rho0=1.0, c0=1.0, Gamm
 _P = C.c_void_p
 _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int32)
+_F = C.POINTER(C.c_float)
 
 
 def dptr(a):
@@ -134,6 +135,14 @@ def dptr(a):
 
 def iptr(a):
     return a.ctypes.data_as(_I) if a is not None else None
+
+
+def fptr(a):
+    return a.ctypes.data_as(_F) if a is not None else None
+
+
+MLP_FEATURES = 16
+MLP_PARAMS = 9473
 
 
 _lib = None
@@ -177,6 +186,18 @@ def load(path=None):
                                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p,
                                                  C.c_void_p, C.c_void_p, C.c_void_p, C.c_int32, C.c_void_p]),
         "m2cg_host_free": (None, [C.c_void_p]),
+        "m2cg_riemann_batch_eos": (C.c_int, [_P, C.c_int64, _D, _D, _D, _D, _I, _I, _F]),
+        "m2cg_mlp_create": (C.c_int, [C.c_uint64, C.POINTER(_P)]),
+        "m2cg_mlp_destroy": (None, [_P]),
+        "m2cg_mlp_set_params": (C.c_int, [_P, _F]),
+        "m2cg_mlp_get_params": (C.c_int, [_P, _F]),
+        "m2cg_mlp_features": (C.c_int, [C.c_int64, _D, _D, _D, _F, _F, _F]),
+        "m2cg_mlp_set_data": (C.c_int, [_P, C.c_int64, _D, _D, _D]),
+        "m2cg_mlp_train": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, _F, _F]),
+        "m2cg_mlp_grad": (C.c_int, [_P, C.c_int64, _F, _F, _F, _F]),
+        "m2cg_mlp_forward": (C.c_int, [_P, C.c_int64, _F, _F]),
+        "m2cg_mlp_predict": (C.c_int, [_P, C.c_int64, _D, _D, _D, _F]),
+        "m2cg_set_warm_start": (C.c_int, [_P, _P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -22,6 +22,7 @@ UNITS = {
     "m2cg_riemann_kernels.cu": ["-fmad=false"],
     "m2cg_api.cu": [],
     "m2cg_noalloc.cu": ["-fmad=false"],
+    "m2cg_mlp.cu": [],
 }
 
 

@@ -8,6 +8,7 @@
 #include <vector>
 #include <string>
 #include <algorithm>
+#include <cuda_bf16.h>
 #include "m2cg_internal.h"
 
 namespace m2cg {
@@ -35,12 +36,17 @@ void launch_riemann_stragglers(cudaStream_t, const Params&, const Mats*, const S
                                double* const*, const IfaceList&, int, double*, int, int, size_t, const int32_t*,
                                const unsigned long long*, const float*, unsigned long long*, const DevScalars*);
 cudaError_t riemann_stragglers_reserve(size_t bytes);
+void mlp_warm_faces(m2cg_mlp*, cudaStream_t, int, const Params&, const StateSet&, const int32_t*, const IfaceList&,
+                    __nv_bfloat16*, float*, float*, float*, const DevScalars*);
+cudaError_t mlp_prepare();
 void launch_hold(cudaStream_t, long long);
 void launch_riemann_batch(cudaStream_t, const Params&, const Mats*, int64_t, const double*, const int32_t*,
                           const double*, const int32_t*, const double*, double*, int32_t*, double*, double*, int32_t*,
                           int32_t*, double*, int, int, int, const double*);
 void launch_flux_batch(cudaStream_t, const Params&, int64_t, const int32_t*, const double*, const double*,
                        const int32_t*, double*);
+void launch_riemann_batch_eos(cudaStream_t, const Params&, int64_t, const double*, const double*, const double*,
+                              double*, int32_t*, int32_t*, double*, int, int, int);
 }  // namespace m2cg
 
 using namespace m2cg;
@@ -117,6 +123,13 @@ struct m2cg_ctx {
   unsigned long long* strag_count = nullptr;
   cudaEvent_t ev_a = nullptr;  // end of the first pass
   long long hold_cycles = 40000;  // ~20 us head start for the straggler blocks
+  // learned warm start (m2cg_set_warm_start): per interface face features,
+  // network output, reference pressure and starting pressure
+  m2cg_mlp* mlp = nullptr;
+  __nv_bfloat16* w_X = nullptr;
+  float* w_t = nullptr;
+  float* w_ref = nullptr;
+  float* w_p = nullptr;
   double* partial = nullptr;
   double* stage_V = nullptr;
   int32_t* stage_id = nullptr;
@@ -179,6 +192,11 @@ m2cg_status m2cg_fill_params(const m2cg_config& c, m2cg::Params& P) {
   r.maxIts_main = c.maxits_main; r.maxIts_bracket = c.maxits_bracket; r.maxIts_shock = c.maxits_shock;
   r.numSteps = c.numsteps_rarefaction; r.tol_main = c.tol_main; r.tol_shock = c.tol_shock; r.tol_rare = c.tol_rarefaction;
   r.min_pressure = c.min_pressure; r.failure_threshold = c.failure_threshold; r.pressure_at_failure = c.pressure_at_failure;
+  r.warm_delta = 1e-5;
+  r.warm_tries = 3;
+  // tuning overrides for the learned warm start
+  if (const char* e = getenv("M2CG_WARM_DELTA")) r.warm_delta = atof(e);
+  if (const char* e = getenv("M2CG_WARM_TRIES")) r.warm_tries = atoi(e);
   P.area[0] = g.dy * g.dz; P.area[1] = g.dx * g.dz; P.area[2] = g.dx * g.dy;
   double vol = g.dx * g.dy * g.dz;
   P.inv_negvol = 1.0 / (-vol);
@@ -298,14 +316,21 @@ static int64_t enqueue_stage(m2cg_ctx* x, int stage, bool last, const StateSet& 
   if (after_recon) { PHASE(PH_RECON, launch_reconstruct(s, P, in, x->id, x->d_fs, x->cnt)); n += 2; }
   cudaEventRecord(x->ev_fork, s);
   cudaStreamWaitEvent(x->stream2, x->ev_fork, 0);
+  const float* warm = nullptr;
+  if (x->mlp) {
+    PHASE_ON(PH_RIEMANN, x->stream2,
+             mlp_warm_faces(x->mlp, x->stream2, x->nsm, P, in, x->id, x->L, x->w_X, x->w_t, x->w_ref, x->w_p, x->sc));
+    warm = x->w_p;
+    n += 3;
+  }
   PHASE_ON(PH_RIEMANN, x->stream2,
            launch_riemann_interfaces(x->stream2, P, x->d_mats, in, x->id, x->d_fs, x->L, stage == 0, x->scratch,
                                      x->path_cap, x->rblocks, x->rthreads, x->eval_limit, x->strag, x->strag_count,
-                                     nullptr, x->cnt, x->sc));
+                                     warm, x->cnt, x->sc));
   cudaEventRecord(x->ev_a, x->stream2);
   PHASE_ON(PH_RIEMANN_B, x->stream2,
            launch_riemann_stragglers(x->stream2, P, x->d_mats, in, x->id, x->d_fs, x->L, stage == 0, x->scratch,
-                                     x->path_cap, x->sblocks, x->sreserve, x->strag, x->strag_count, nullptr, x->cnt,
+                                     x->path_cap, x->sblocks, x->sreserve, x->strag, x->strag_count, warm, x->cnt,
                                      x->sc));
   cudaEventRecord(x->ev_join, x->stream2);
   n += 2;
@@ -523,10 +548,16 @@ m2cg_status m2cg_compute_residual(m2cg_ctx* x, double* R) {
   launch_compact(s, x->P, x->id, x->L, x->cnt, nullptr);
   launch_reconstruct(s, x->P, x->S[0], x->id, x->d_fs, x->cnt);
   launch_face_flux(s, x->P, x->id, x->d_fs, x->d_F, x->cnt);
+  const float* warm = nullptr;
+  if (x->mlp) {
+    mlp_warm_faces(x->mlp, s, x->nsm, x->P, x->S[0], x->id, x->L, x->w_X, x->w_t, x->w_ref, x->w_p, nullptr);
+    warm = x->w_p;
+    x->launches += 3;
+  }
   launch_riemann_interfaces(s, x->P, x->d_mats, x->S[0], x->id, x->d_fs, x->L, 1, x->scratch, x->path_cap, x->rblocks,
-                            x->rthreads, x->eval_limit, x->strag, x->strag_count, nullptr, x->cnt, nullptr);
+                            x->rthreads, x->eval_limit, x->strag, x->strag_count, warm, x->cnt, nullptr);
   launch_riemann_stragglers(s, x->P, x->d_mats, x->S[0], x->id, x->d_fs, x->L, 1, x->scratch, x->path_cap, x->sblocks,
-                            x->sreserve, x->strag, x->strag_count, nullptr, x->cnt, nullptr);
+                            x->sreserve, x->strag, x->strag_count, warm, x->cnt, nullptr);
   StageArgs A;
   memset(&A, 0, sizeof(A));
   A.in = x->S[0];
@@ -599,6 +630,25 @@ m2cg_status m2cg_get_counters(m2cg_ctx* x, m2cg_counters* c) {
   if (h[CNT_IF_OVERFLOW] || h[CNT_SWEPT_OVERFLOW]) {
     set_err("interface or swept-cell list overflow");
     return M2CG_ERR_CAPACITY;
+  }
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_set_warm_start(m2cg_ctx* x, m2cg_mlp* m) {
+  if (!x) { set_err("null context"); return M2CG_ERR_INVALID_ARG; }
+  CK(cudaStreamSynchronize(x->stream));
+  if (m && !x->w_p) {
+    CK(mlp_prepare());
+    CK(x->alloc(&x->w_X, (size_t)x->L.cap * M2CG_MLP_FEATURES));
+    CK(x->alloc(&x->w_t, x->L.cap));
+    CK(x->alloc(&x->w_ref, x->L.cap));
+    CK(x->alloc(&x->w_p, x->L.cap));
+  }
+  x->mlp = m;
+  x->cfg.warm_start = m ? 1 : 0;
+  if (x->graph_exec) {  // the step graph is captured again on the next m2cg_run
+    cudaGraphExecDestroy(x->graph_exec);
+    x->graph_exec = nullptr;
   }
   return M2CG_OK;
 }
@@ -700,6 +750,46 @@ m2cg_status m2cg_riemann_batch(m2cg_ctx* x, int64_t n, const double* Vm, const i
   if (err) CK(cudaMemcpyAsync(err, derr, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   CK(cudaGetLastError());
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_riemann_batch_eos(m2cg_ctx* x, int64_t n, const double* W, const double* eos, const double* warm_p,
+                                   double* out, int32_t* iters, int32_t* err, float* kernel_ms) {
+  if (!x || n < 0 || !W || !eos || !out) { set_err("null argument"); return M2CG_ERR_INVALID_ARG; }
+  if (n == 0) { if (kernel_ms) *kernel_ms = 0.f; return M2CG_OK; }
+  for (int64_t q = 0; q < 2 * n; q++) {
+    const double* e = &eos[q * 5];
+    if ((e[0] != M2CG_EOS_SG && e[0] != M2CG_EOS_NASG) || !(e[1] > 1.0)) {
+      set_err("problem %lld: EOS must be SG or NASG with gamma > 1", (long long)(q / 2));
+      return M2CG_ERR_INVALID_ARG;
+    }
+  }
+  m2cg_status st = batch_reserve(x, n);
+  if (st != M2CG_OK) return st;
+  double* D = (double*)x->batch[0];
+  int32_t* I = (int32_t*)x->batch[1];
+  double *dW = D, *dE = D + 6 * n, *dwarm = D + 16 * n, *dout = D + 17 * n;
+  int32_t *dit = I, *derr = I + n;
+  cudaStream_t s = x->stream;
+  CK(cudaMemcpyAsync(dW, W, n * 6 * sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaMemcpyAsync(dE, eos, n * 10 * sizeof(double), cudaMemcpyHostToDevice, s));
+  if (warm_p) CK(cudaMemcpyAsync(dwarm, warm_p, n * sizeof(double), cudaMemcpyHostToDevice, s));
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, s));
+  launch_riemann_batch_eos(s, x->P, n, dW, dE, warm_p ? dwarm : nullptr, dout, dit, derr, x->batch_scratch,
+                           x->path_cap, (int)(x->batch_threads / 128), 128);
+  CK(cudaEventRecord(e1, s));
+  x->launches++;
+  CK(cudaMemcpyAsync(out, dout, n * 4 * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (iters) CK(cudaMemcpyAsync(iters, dit, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  if (err) CK(cudaMemcpyAsync(err, derr, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  if (kernel_ms) CK(cudaEventElapsedTime(kernel_ms, e0, e1));
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
   return M2CG_OK;
 }
 

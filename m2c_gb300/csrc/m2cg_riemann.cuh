@@ -18,6 +18,10 @@ namespace m2cg {
 struct RiemannPrm {
   int maxIts_main, maxIts_bracket, maxIts_shock, numSteps;
   double tol_main, tol_shock, tol_rare, min_pressure, failure_threshold, pressure_at_failure;
+  // learned warm start: half-width of the starting pair and the number of
+  // secant expansions allowed before a cold restart
+  double warm_delta;
+  int warm_tries;
 };
 
 // Status bits returned alongside the reference's error code.
@@ -62,7 +66,12 @@ struct ExactRiemannDev {
   RiemannPrm P;
   PathCache path1, path3;
   int evals;
-  double warm_p;   // > 0 replaces the acoustic-theory p0 (learned warm start)
+  // Learned warm start: with warm_p > 0 the starting pair is
+  // warm_p (1 -+ P.warm_delta) instead of the acoustic-theory pair; if that
+  // pair is not physical or P.warm_tries secant expansions do not bracket the
+  // root, solve_once returns 3 and solve restarts cold (the reference's path).
+  double warm_p;
+  bool warm_miss = false;
   bool nonadaptive;  // running as the reference's non-adaptive fallback solver
   int fallback;      // 1 if the last solve needed the non-adaptive retry
   // Evaluation budget: with eval_limit > 0 a solve that reaches eval_limit
@@ -418,9 +427,22 @@ struct ExactRiemannDev {
   __device__ __noinline__ int acoustic(double rhol, double ul, double pl, double cl, int idl, double rhor, double ur, double pr,
                         double cr, int idr, double& p0, double& rhol0, double& rhor0, double& ul0, double& ur0,
                         double& p1, double& rhol1, double& rhor1, double& ul1, double& ur1) {
+    if (warm_p > 0.0) {
+      // learned warm start: the two starting points bracket the prediction,
+      // p_hat (1 -+ warm_delta), in place of the acoustic-theory pair; the
+      // bracketing and the secant loop that follow are the reference's
+      p0 = warm_p * (1.0 - P.warm_delta);
+      p1 = warm_p * (1.0 + P.warm_delta);
+      evals++;
+      if (!rho_u_star(1, path1, rhol, ul, pl, p0, idl, rhol, (p0 > pl) ? rhol * 1.1 : rhol * 0.9, rhol0, ul0, nullptr, nullptr)) return 0;
+      if (!rho_u_star(3, path3, rhor, ur, pr, p0, idr, rhor, (p0 > pr) ? rhor * 1.1 : rhor * 0.9, rhor0, ur0, nullptr, nullptr)) return 0;
+      evals++;
+      if (!rho_u_star(1, path1, rhol, ul, pl, p1, idl, rhol, (p1 > pl) ? rhol * 1.1 : rhol * 0.9, rhol1, ul1, nullptr, nullptr)) return 1;
+      if (!rho_u_star(3, path3, rhor, ur, pr, p1, idr, rhor, (p1 > pr) ? rhor * 1.1 : rhor * 0.9, rhor1, ur1, nullptr, nullptr)) return 1;
+      return 2;
+    }
     double Cl = rhol * cl, Cr = rhor * cr;
     p0 = (Cr * pl + Cl * pr + Cl * Cr * (ul - ur)) / (Cl + Cr);
-    if (warm_p > 0.0) p0 = warm_p;
     evals++;
     if (!rho_u_star(1, path1, rhol, ul, pl, p0, idl, rhol, (p0 > pl) ? rhol * 1.1 : rhol * 0.9, rhol0, ul0, nullptr, nullptr)) return 0;
     if (!rho_u_star(3, path3, rhor, ur, pr, p0, idr, rhor, (p0 > pr) ? rhor * 1.1 : rhor * 0.9, rhor0, ur0, nullptr, nullptr)) return 0;
@@ -441,6 +463,7 @@ struct ExactRiemannDev {
                          double& p1, double& rhol1, double& rhor1, double& ul1, double& ur1) {
     int found = acoustic(rhol, ul, pl, cl, idl, rhor, ur, pr, cr, idr, p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
     if (found == 2) return true;
+    if (warm_p > 0.0) { warm_miss = true; return false; }
     bool ok = true;
     double dp;
     if (found != 1) {
@@ -505,6 +528,7 @@ struct ExactRiemannDev {
       f0 = ul0 - ur0;
       f1 = ul1 - ur1;
       if (f0 * f1 <= 0.0) return true;
+      if (warm_p > 0.0 && i >= P.warm_tries) { warm_miss = true; return false; }
       if (fabs(f0 - f1) > 1e-9) {
         p2 = p1 - f1 * (p1 - p0) / (f1 - f0);
         if (p2 < p0) p2 -= 0.1 * (p1 - p0);
@@ -580,8 +604,9 @@ struct ExactRiemannDev {
   }
 
   // ExactRiemannSolverBase.cpp:59-347 with the non-adaptive retry after a failure
-  // (lines 178-193 and 323-337).  Returns 0 (ok), 1 (failed), -1 (nonphysical
-  // input) or 2 (evaluation budget spent, see eval_limit).
+  // (lines 178-193 and 323-337), preceded by a cold restart when a warm start
+  // misses.  Returns 0 (ok), 1 (failed), -1 (nonphysical input) or 2
+  // (evaluation budget spent, see eval_limit).
   __device__ __noinline__ int solve(const double* dir, const double* Vm, int idl, const double* Vp, int idr, double* Vs,
                                     int& id, double* Vsm, double* Vsp) {
     nonadaptive = false;
@@ -589,6 +614,15 @@ struct ExactRiemannDev {
     suspended = false;
     int e = solve_once(dir, Vm, idl, Vp, idr, Vs, id, Vsm, Vsp);
     if (e == 2) return 2;
+    if (e == 3) {  // the warm start did not bracket the root quickly: cold start
+      int ev = evals;
+      double w = warm_p;
+      warm_p = 0.0;
+      e = solve_once(dir, Vm, idl, Vp, idr, Vs, id, Vsm, Vsp);
+      evals += ev;
+      warm_p = w;
+      if (e == 2) return 2;
+    }
     if (e == 1) {
       int ev = evals;
       double w = warm_p;
@@ -632,8 +666,10 @@ struct ExactRiemannDev {
       finalize(dir, Vm, Vp, rhol, ul, pl, idl, rhor, ur, pr, idr, rhol, rhor, ul, pl, false, Vrare, Vs, id, Vsm, Vsp);
       return 0;
     }
+    warm_miss = false;
     bool ok = bracket(rhol, ul, pl, cl, idl, rhor, ur, pr, cr, idr, p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
     if (suspended) return 2;
+    if (warm_miss) return 3;
     if (!ok) {
       ok = rho_u_star(1, path1, rhol, ul, pl, p1, idl, rhol0, rhol0 * 1.1, rhol2, ul2, &trans_rare, Vrare);
       ok = ok && rho_u_star(3, path3, rhor, ur, pr, p1, idr, rhor0, rhol0 * 1.1, rhor2, ur2, &trans_rare, Vrare);

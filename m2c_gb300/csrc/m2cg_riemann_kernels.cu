@@ -216,6 +216,54 @@ __global__ void k_riemann_batch(const Mats* __restrict__ md, RiemannPrm rp, int6
   }
 }
 
+// DevMat of a stiffened-gas / Noble-Abel stiffened-gas material from
+// {type, gamma, pc, b, q}, with the reference's default (no-op) clipping; the
+// same arithmetic as the host-side configuration (m2cg_fill_params).
+__device__ __forceinline__ void make_devmat(const double* e, DevMat& d) {
+  d.type = (int)e[0];
+  d.gam = e[1];
+  d.gam1 = e[1] - 1.0;
+  d.Pstiff = e[2];
+  d.gamPs = e[1] * e[2];
+  d.invgam1 = 1.0 / (e[1] - 1.0);
+  d.b = e[3];
+  d.q = e[4];
+  d.rho0 = 1.0; d.s = 0.0; d.e0 = 0.0; d.rho0_c0_c0 = 0.0; d.G0_half = 0.0; d.G0_rho0 = 0.0;
+  d.rhomin = 0.0; d.pmin = -DBL_MAX; d.rhomax = DBL_MAX; d.pmax = DBL_MAX;
+  d.clip_default = 1;
+}
+
+// Independent 1D problems, each with its own material pair (the warm-start
+// training and evaluation sets): W rows {rho_l, u_l, p_l, rho_r, u_r, p_r},
+// E rows {type, gamma, pc, b, q} left then right; out rows {p*, u*, rho*_l,
+// rho*_r}.  One thread per problem, grid-stride.
+__global__ void k_riemann_batch_eos(RiemannPrm rp, int64_t n, const double* __restrict__ W,
+                                    const double* __restrict__ E, const double* __restrict__ warm, double* out,
+                                    int32_t* iters, int32_t* err, double* scratch, int path_cap) {
+  int64_t T = (int64_t)gridDim.x * blockDim.x;
+  int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  Mats mats;
+  ExactRiemannDev rs;
+  init_solver(rs, &mats, rp, scratch, path_cap, tid, T);
+  const double dir[3] = {1.0, 0.0, 0.0};
+  for (int64_t q = tid; q < n; q += T) {
+    make_devmat(&E[q * 10], mats.m[0]);
+    make_devmat(&E[q * 10 + 5], mats.m[1]);
+    const double* w = &W[q * 6];
+    double Vm[5] = {w[0], w[1], 0.0, 0.0, w[2]}, Vp[5] = {w[3], w[4], 0.0, 0.0, w[5]};
+    double Vs[5], Vsm[5], Vsp[5];
+    int oid = 0;
+    rs.warm_p = warm ? warm[q] : 0.0;
+    int e = rs.solve(dir, Vm, 0, Vp, 1, Vs, oid, Vsm, Vsp);
+    out[q * 4 + 0] = Vsm[4];
+    out[q * 4 + 1] = Vsm[1];
+    out[q * 4 + 2] = Vsm[0];
+    out[q * 4 + 3] = Vsp[0];
+    if (iters) iters[q] = rs.evals;
+    if (err) err[q] = e;
+  }
+}
+
 __global__ void k_flux_batch(Params P, int64_t n, const int32_t* __restrict__ dir, const double* __restrict__ Vm,
                              const double* __restrict__ Vp, const int32_t* __restrict__ id, double* F) {
   int64_t q = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
@@ -265,6 +313,11 @@ void launch_riemann_batch(cudaStream_t s, const Params& P, const Mats* md, int64
                           int blocks, int threads, const double* warm) {
   k_riemann_batch<<<blocks, threads, 0, s>>>(md, P.rp, n, Vm, idm, Vp, idp, dir, Vs, id, Vsm, Vsp, iters, err,
                                              scratch, path_cap, warm);
+}
+void launch_riemann_batch_eos(cudaStream_t s, const Params& P, int64_t n, const double* W, const double* E,
+                              const double* warm, double* out, int32_t* iters, int32_t* err, double* scratch,
+                              int path_cap, int blocks, int threads) {
+  k_riemann_batch_eos<<<blocks, threads, 0, s>>>(P.rp, n, W, E, warm, out, iters, err, scratch, path_cap);
 }
 void launch_flux_batch(cudaStream_t s, const Params& P, int64_t n, const int32_t* dir, const double* Vm,
                        const double* Vp, const int32_t* id, double* F) {

@@ -91,6 +91,12 @@ class Solver:
         abi.check(self.lib, self.lib.m2cg_conserved_totals(self.ctx, abi.dptr(t)), "m2cg_conserved_totals")
         return t
 
+    def set_warm_start(self, net):
+        """Warm-start the interface solves with a WarmStartMLP (None: cold start)."""
+        abi.check(self.lib, self.lib.m2cg_set_warm_start(self.ctx, net.h if net is not None else None),
+                  "m2cg_set_warm_start")
+        self._warm_net = net  # the network must outlive its use by the context
+
     def riemann_batch(self, Vm, idm, Vp, idp, dirs):
         n = len(idm)
         Vs, Vsm, Vsp = np.zeros((n, 5)), np.zeros((n, 5)), np.zeros((n, 5))

@@ -932,6 +932,44 @@ void orc_riemann_batch(const m2cg_config* cfg, int64_t n, const double* Vm, cons
   }
 }
 
+// Batched 1D problems with a material pair each (the warm-start data sets):
+// W rows {rho_l, u_l, p_l, rho_r, u_r, p_r}, E rows {type, gamma, pc, b, q}
+// left then right, out rows {p*, u*, rho*_l, rho*_r}; the solver parameters
+// come from cfg.
+void orc_riemann_batch_eos(const m2cg_config* cfg, int64_t n, const double* W, const double* E, const double* warm_p,
+                           double* out, int32_t* iters, int32_t* err) {
+  RiemannParams rp;
+  rp.maxIts_main = cfg->maxits_main; rp.maxIts_bracket = cfg->maxits_bracket; rp.maxIts_shock = cfg->maxits_shock;
+  rp.numSteps_rarefaction = cfg->numsteps_rarefaction; rp.tol_main = cfg->tol_main; rp.tol_shock = cfg->tol_shock;
+  rp.tol_rarefaction = cfg->tol_rarefaction; rp.min_pressure = cfg->min_pressure;
+  rp.failure_threshold = cfg->failure_threshold; rp.pressure_at_failure = cfg->pressure_at_failure;
+#pragma omp parallel
+  {
+    std::vector<Eos> vf(2);
+    ExactRiemann rs(vf, rp);
+#pragma omp for schedule(dynamic, 16)
+    for (int64_t q = 0; q < n; q++) {
+      for (int side = 0; side < 2; side++) {
+        const double* e = &E[q * 10 + side * 5];
+        m2cg_material m;
+        memset(&m, 0, sizeof(m));
+        m.eos = (int32_t)e[0]; m.gamma = e[1]; m.pc = e[2]; m.b = e[3]; m.q = e[4];
+        m.rhomin = 0.0; m.pmin = -DBL_MAX; m.rhomax = DBL_MAX; m.pmax = DBL_MAX;
+        vf[side].setup(m);
+      }
+      const double* w = &W[q * 6];
+      double Vm[5] = {w[0], w[1], 0.0, 0.0, w[2]}, Vp[5] = {w[3], w[4], 0.0, 0.0, w[5]};
+      double dir[3] = {1.0, 0.0, 0.0}, Vs[5], Vsm[5], Vsp[5];
+      int oid = 0;
+      rs.warm_p = warm_p ? warm_p[q] : 0.0;
+      int e = rs.Solve(dir, Vm, 0, Vp, 1, Vs, oid, Vsm, Vsp);
+      out[q * 4 + 0] = Vsm[4]; out[q * 4 + 1] = Vsm[1]; out[q * 4 + 2] = Vsm[0]; out[q * 4 + 3] = Vsp[0];
+      if (iters) iters[q] = rs.evals;
+      if (err) err[q] = e;
+    }
+  }
+}
+
 // Batched numerical fluxes (FluxFcnHLLC.h:196-245, FluxFcnLLF.h:80-111, FluxFcnGenRoe.h:183-213).
 void orc_flux_batch(const m2cg_config* cfg, int64_t n, const int32_t* dir, const double* Vm, const double* Vp,
                     const int32_t* id, double* F) {

@@ -14,6 +14,8 @@ struct RiemannParams {
   int maxIts_main = 200, maxIts_bracket = 100, maxIts_shock = 200, numSteps_rarefaction = 200;
   double tol_main = 1e-5, tol_shock = 1e-12, tol_rarefaction = 1e-8;
   double min_pressure = -1e8, failure_threshold = 0.2, pressure_at_failure = 1e-8;
+  double warm_delta = 1e-5;  // learned warm start (not in the reference)
+  int warm_tries = 3;
 };
 
 class ExactRiemann {
@@ -24,9 +26,13 @@ class ExactRiemann {
   // Number of wave-pair evaluations (bracketing + main loop) in the last solve.
   int evals = 0;
   int main_iters = 0;
-  // Optional warm start: when > 0, replaces the acoustic p0 (used only by the
-  // learned-warm-start study; the reference path passes 0).
+  // Optional warm start (the learned warm start; the reference path passes 0):
+  // when > 0 the starting pair is warm_p (1 -+ P.warm_delta) instead of the
+  // acoustic-theory pair; if that pair is not physical, or P.warm_tries secant
+  // expansions do not bracket the root, the solve restarts cold (SolveOnce
+  // returns 3 to Solve).
   double warm_p = 0.0;
+  bool warm_miss = false;
   // true while running as ExactRiemannSolverNonAdaptive (fixed-step RK4
   // rarefactions, ExactRiemannSolverBase.cpp:2243-2990)
   bool nonadaptive = false;
@@ -39,6 +45,14 @@ class ExactRiemann {
     nonadaptive = false;
     fallbacks = 0;
     int e = SolveOnce(dir, Vm, idl, Vp, idr, Vs, id, Vsm, Vsp);
+    if (e == 3) {  // the warm start did not bracket the root quickly: cold start
+      int ev = evals;
+      double w = warm_p;
+      warm_p = 0.0;
+      e = SolveOnce(dir, Vm, idl, Vp, idr, Vs, id, Vsm, Vsp);
+      evals += ev;
+      warm_p = w;
+    }
     if (e == 1) {
       int ev = evals;
       double w = warm_p;
@@ -89,8 +103,10 @@ class ExactRiemann {
       return 0;
     }
 
+    warm_miss = false;
     bool success = FindInitialInterval(rhol, ul, pl, el, cl, idl, rhor, ur, pr, er, cr, idr,
                                        p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
+    if (warm_miss) return 3;
     if (!success) {  // :150-194 (the caller retries with the non-adaptive solver)
       success = RhoUStar(1, path1_, rhol, ul, pl, p1, idl, rhol0, rhol0 * 1.1, rhol2, ul2, &trans_rare, Vrare_x0);
       success = success && RhoUStar(3, path3_, rhor, ur, pr, p1, idr, rhor0, rhol0 * 1.1, rhor2, ur2, &trans_rare, Vrare_x0);
@@ -236,6 +252,7 @@ class ExactRiemann {
       f0 = ul0 - ur0;
       f1 = ul1 - ur1;
       if (f0 * f1 <= 0.0) return true;
+      if (warm_p > 0.0 && i >= P.warm_tries) { warm_miss = true; return false; }
       if (std::fabs(f0 - f1) > 1e-9) {
         p2 = p1 - f1 * (p1 - p0) / (f1 - f0);
         if (p2 < p0) p2 -= 0.1 * (p1 - p0);
@@ -289,6 +306,7 @@ class ExactRiemann {
     bool success = true;
     int found = Acoustic(rhol, ul, pl, el, cl, idl, rhor, ur, pr, er, cr, idr, p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
     if (found == 2) return true;
+    if (warm_p > 0.0) { warm_miss = true; return false; }
     if (found != 1) {
       dp = (pl != pr) ? std::fabs(pl - pr) : 0.5 * pl;
       for (int i = 0; i < P.maxIts_bracket; i++) {
@@ -336,9 +354,22 @@ class ExactRiemann {
                double& p0, double& rhol0, double& rhor0, double& ul0, double& ur0,
                double& p1, double& rhol1, double& rhor1, double& ul1, double& ur1) {
     int found = 0;
+    if (warm_p > 0.0) {
+      // learned warm start (not in the reference): the starting pair brackets
+      // the prediction, warm_p (1 -+ warm_delta), in place of the acoustic pair
+      p0 = warm_p * (1.0 - P.warm_delta);
+      p1 = warm_p * (1.0 + P.warm_delta);
+      evals++;
+      if (!RhoUStar(1, path1_, rhol, ul, pl, p0, idl, rhol, (p0 > pl) ? rhol * 1.1 : rhol * 0.9, rhol0, ul0, nullptr, nullptr)) return found;
+      if (!RhoUStar(3, path3_, rhor, ur, pr, p0, idr, rhor, (p0 > pr) ? rhor * 1.1 : rhor * 0.9, rhor0, ur0, nullptr, nullptr)) return found;
+      found = 1;
+      evals++;
+      if (!RhoUStar(1, path1_, rhol, ul, pl, p1, idl, rhol, (p1 > pl) ? rhol * 1.1 : rhol * 0.9, rhol1, ul1, nullptr, nullptr)) return found;
+      if (!RhoUStar(3, path3_, rhor, ur, pr, p1, idr, rhor, (p1 > pr) ? rhor * 1.1 : rhor * 0.9, rhor1, ur1, nullptr, nullptr)) return found;
+      return 2;
+    }
     double Cl = rhol * cl, Cr = rhor * cr;
     p0 = (Cr * pl + Cl * pr + Cl * Cr * (ul - ur)) / (Cl + Cr);
-    if (warm_p > 0.0) p0 = warm_p;
     evals++;
     if (!RhoUStar(1, path1_, rhol, ul, pl, p0, idl, rhol, (p0 > pl) ? rhol * 1.1 : rhol * 0.9, rhol0, ul0, nullptr, nullptr)) return found;
     if (!RhoUStar(3, path3_, rhor, ur, pr, p0, idr, rhor, (p0 > pr) ? rhor * 1.1 : rhor * 0.9, rhor0, ur0, nullptr, nullptr)) return found;
