@@ -52,6 +52,10 @@ def parse():
     ap.add_argument("--cpu-size", type=int, default=96)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    # learned warm start: training / test problems of the study (0 disables it)
+    ap.add_argument("--ws-train", type=int, default=1 << 20)
+    ap.add_argument("--ws-test", type=int, default=1 << 17)
+    ap.add_argument("--ws-epochs", type=int, default=60)
     return ap.parse_args()
 
 
@@ -274,6 +278,33 @@ def run_gb300(args):
     for p in (hv, hi, hp):
         lib.m2cg_host_free(p)
 
+    # learned warm start: batch study (interface problems drawn from the
+    # warm-start distribution) and the same step with the network in the loop
+    wsres = None
+    if args.ws_train > 0 and rank == 0:
+        from m2c_gb300 import warmstart as ws
+        res, net = ws.study(n_train=args.ws_train, n_test=args.ws_test, epochs=args.ws_epochs, keep_net=True)
+        s.set_warm_start(net)
+        s.run(args.warmup)
+        w0 = s.counters()
+        lib.m2cg_event_record(ctx, 0)
+        s.run(args.steps)
+        lib.m2cg_event_record(ctx, 1)
+        lib.m2cg_sync(ctx)
+        wms = C.c_float()
+        abi.check(lib, lib.m2cg_event_elapsed(ctx, 0, 1, C.byref(wms)), "elapsed")
+        w1 = s.counters()
+        s.set_warm_start(None)
+        wsolves = w1["riemann_solves"] - w0["riemann_solves"]
+        res["fv_step"] = {"value_warm": cells * stages * args.steps / (wms.value * 1e-3), "unit": UNIT,
+                          "value_cold": value,
+                          "mean_iters_per_solve_warm": (w1["riemann_iterations"] - w0["riemann_iterations"]) /
+                                                       max(wsolves, 1),
+                          "mean_iters_per_solve_cold": iters / max(solves, 1),
+                          "note": "warm steps follow the cold-timed ones (later states, similar face counts)"}
+        net.close()
+        wsres = res
+
     if rank != 0:
         return 0
     cpu = None
@@ -300,6 +331,7 @@ def run_gb300(args):
                        "interface_faces_per_stage": (c1["interface_faces"] - c0["interface_faces"]) /
                                                      max(stages * args.steps, 1),
                        "errors": c1["riemann_errors"] - c0["riemann_errors"], "warm_start": "cold"},
+           "warm_start": wsres,
            "phase_ms_per_step": phase,
            "counters": {k: c1[k] for k in ("clipped_cells", "nonphysical", "swept_cells", "unresolved_cells")}}
     print(json.dumps(out))

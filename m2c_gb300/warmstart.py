@@ -176,8 +176,10 @@ class WarmStartMLP:
         return p, ms.value
 
 
-def study(n_train=1 << 22, n_test=1 << 22, epochs=60, batch=16384, lr=3e-3, seed=2024, tol=1e-10, log=None):
-    """Label a training set, train the network, compare warm and cold starts on a test set."""
+def study(n_train=1 << 22, n_test=1 << 22, epochs=60, batch=16384, lr=3e-3, seed=2024, tol=1e-10, log=None,
+          keep_net=False):
+    """Label a training set, train the network, compare warm and cold starts on
+    a test set.  With keep_net the trained WarmStartMLP is returned as well."""
     say = log or (lambda *a: None)
     solver = BatchSolver(tol)
     Wtr, Etr = sample_problems(n_train, seed)
@@ -197,6 +199,13 @@ def study(n_train=1 << 22, n_test=1 << 22, epochs=60, batch=16384, lr=3e-3, seed
     rel = np.abs(pred[ok] - cold["pstar"][ok]) / cold["pstar"][ok]
     both = (cold["err"] == 0) & (warm["err"] == 0)
     dp = np.abs(warm["pstar"][both] - cold["pstar"][both]) / np.maximum(np.abs(cold["pstar"][both]), 1e-300)
+    # device time on the problems both starts solve: the whole-set time is set
+    # by the few failing solves, which run the reference's MaxIts twice
+    sub_cold = solver.solve(Wte[both], Ete[both])
+    sub_pred, sub_pred_ms = net.predict(Wte[both], Ete[both])
+    sub_warm = solver.solve(Wte[both], Ete[both], warm_p=sub_pred)
+    # the same solver started at the converged root: the bound on any predictor
+    exact = solver.solve(Wte[both], Ete[both], warm_p=np.where(cold["pstar"][both] > 0, cold["pstar"][both], 0.0))
     res = {
         "n_train": int(n_train), "n_test": int(n_test), "tolerance": tol,
         "train_usable": int(keep.sum()), "epochs": epochs, "batch": batch, "lr": lr,
@@ -214,7 +223,16 @@ def study(n_train=1 << 22, n_test=1 << 22, epochs=60, batch=16384, lr=3e-3, seed
         "warm_vs_cold_pstar_rel_median": float(np.median(dp)) if len(dp) else 0.0,
         "warm_vs_cold_pstar_rel_p99": float(np.percentile(dp, 99)) if len(dp) else 0.0,
         "warm_vs_cold_pstar_rel_max": float(dp.max()) if len(dp) else 0.0,
+        "converged_set": {"n": int(both.sum()), "solve_ms_cold": sub_cold["ms"], "solve_ms_warm": sub_warm["ms"],
+                          "predict_ms": sub_pred_ms,
+                          "time_ratio": sub_cold["ms"] / max(sub_warm["ms"] + sub_pred_ms, 1e-30),
+                          "iters_cold_mean": float(sub_cold["iters"].mean()),
+                          "iters_warm_mean": float(sub_warm["iters"].mean()),
+                          "iters_exact_start_mean": float(exact["iters"].mean()),
+                          "solve_ms_exact_start": exact["ms"]},
     }
     solver.close()
+    if keep_net:
+        return res, net
     net.close()
     return res
