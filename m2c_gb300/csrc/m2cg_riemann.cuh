@@ -22,6 +22,7 @@ struct RiemannPrm {
   // secant expansions allowed before a cold restart
   double warm_delta;
   int warm_tries;
+  double warm_gate;  // the prediction is used only where it differs from the acoustic estimate by more
 };
 
 // Status bits returned alongside the reference's error code.
@@ -66,11 +67,13 @@ struct ExactRiemannDev {
   RiemannPrm P;
   PathCache path1, path3;
   int evals;
-  // Learned warm start: with warm_p > 0 the starting pair is
+  // Learned warm start: with warm_p > 0 differing from the acoustic estimate
+  // by more than P.warm_gate (relative), the starting pair is
   // warm_p (1 -+ P.warm_delta) instead of the acoustic-theory pair; if that
   // pair is not physical or P.warm_tries secant expansions do not bracket the
   // root, solve_once returns 3 and solve restarts cold (the reference's path).
   double warm_p;
+  bool warm_used = false;  // this pass started from the prediction
   bool warm_miss = false;
   bool nonadaptive;  // running as the reference's non-adaptive fallback solver
   int fallback;      // 1 if the last solve needed the non-adaptive retry
@@ -427,7 +430,13 @@ struct ExactRiemannDev {
   __device__ __noinline__ int acoustic(double rhol, double ul, double pl, double cl, int idl, double rhor, double ur, double pr,
                         double cr, int idr, double& p0, double& rhol0, double& rhor0, double& ul0, double& ur0,
                         double& p1, double& rhol1, double& rhor1, double& ul1, double& ur1) {
-    if (warm_p > 0.0) {
+    double Cl = rhol * cl, Cr = rhor * cr;
+    p0 = (Cr * pl + Cl * pr + Cl * Cr * (ul - ur)) / (Cl + Cr);
+    // the prediction replaces the acoustic estimate only where the two differ
+    // by more than warm_gate (relative); elsewhere acoustic theory is already
+    // as close as the network
+    warm_used = warm_p > 0.0 && !(fabs(warm_p - p0) <= P.warm_gate * fabs(p0));
+    if (warm_used) {
       // learned warm start: the two starting points bracket the prediction,
       // p_hat (1 -+ warm_delta), in place of the acoustic-theory pair; the
       // bracketing and the secant loop that follow are the reference's
@@ -441,8 +450,6 @@ struct ExactRiemannDev {
       if (!rho_u_star(3, path3, rhor, ur, pr, p1, idr, rhor, (p1 > pr) ? rhor * 1.1 : rhor * 0.9, rhor1, ur1, nullptr, nullptr)) return 1;
       return 2;
     }
-    double Cl = rhol * cl, Cr = rhor * cr;
-    p0 = (Cr * pl + Cl * pr + Cl * Cr * (ul - ur)) / (Cl + Cr);
     evals++;
     if (!rho_u_star(1, path1, rhol, ul, pl, p0, idl, rhol, (p0 > pl) ? rhol * 1.1 : rhol * 0.9, rhol0, ul0, nullptr, nullptr)) return 0;
     if (!rho_u_star(3, path3, rhor, ur, pr, p0, idr, rhor, (p0 > pr) ? rhor * 1.1 : rhor * 0.9, rhor0, ur0, nullptr, nullptr)) return 0;
@@ -463,7 +470,7 @@ struct ExactRiemannDev {
                          double& p1, double& rhol1, double& rhor1, double& ul1, double& ur1) {
     int found = acoustic(rhol, ul, pl, cl, idl, rhor, ur, pr, cr, idr, p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
     if (found == 2) return true;
-    if (warm_p > 0.0) { warm_miss = true; return false; }
+    if (warm_used) { warm_miss = true; return false; }
     bool ok = true;
     double dp;
     if (found != 1) {
@@ -528,7 +535,7 @@ struct ExactRiemannDev {
       f0 = ul0 - ur0;
       f1 = ul1 - ur1;
       if (f0 * f1 <= 0.0) return true;
-      if (warm_p > 0.0 && i >= P.warm_tries) { warm_miss = true; return false; }
+      if (warm_used && i >= P.warm_tries) { warm_miss = true; return false; }
       if (fabs(f0 - f1) > 1e-9) {
         p2 = p1 - f1 * (p1 - p0) / (f1 - f0);
         if (p2 < p0) p2 -= 0.1 * (p1 - p0);
@@ -667,6 +674,7 @@ struct ExactRiemannDev {
       return 0;
     }
     warm_miss = false;
+    warm_used = false;
     bool ok = bracket(rhol, ul, pl, cl, idl, rhor, ur, pr, cr, idr, p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
     if (suspended) return 2;
     if (warm_miss) return 3;

@@ -16,6 +16,7 @@ struct RiemannParams {
   double min_pressure = -1e8, failure_threshold = 0.2, pressure_at_failure = 1e-8;
   double warm_delta = 1e-5;  // learned warm start (not in the reference)
   int warm_tries = 3;
+  double warm_gate = 0.05;
 };
 
 class ExactRiemann {
@@ -27,11 +28,13 @@ class ExactRiemann {
   int evals = 0;
   int main_iters = 0;
   // Optional warm start (the learned warm start; the reference path passes 0):
-  // when > 0 the starting pair is warm_p (1 -+ P.warm_delta) instead of the
+  // when > 0 and off the acoustic estimate by more than P.warm_gate
+  // (relative), the starting pair is warm_p (1 -+ P.warm_delta) instead of the
   // acoustic-theory pair; if that pair is not physical, or P.warm_tries secant
   // expansions do not bracket the root, the solve restarts cold (SolveOnce
   // returns 3 to Solve).
   double warm_p = 0.0;
+  bool warm_used = false;
   bool warm_miss = false;
   // true while running as ExactRiemannSolverNonAdaptive (fixed-step RK4
   // rarefactions, ExactRiemannSolverBase.cpp:2243-2990)
@@ -104,6 +107,7 @@ class ExactRiemann {
     }
 
     warm_miss = false;
+    warm_used = false;
     bool success = FindInitialInterval(rhol, ul, pl, el, cl, idl, rhor, ur, pr, er, cr, idr,
                                        p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
     if (warm_miss) return 3;
@@ -252,7 +256,7 @@ class ExactRiemann {
       f0 = ul0 - ur0;
       f1 = ul1 - ur1;
       if (f0 * f1 <= 0.0) return true;
-      if (warm_p > 0.0 && i >= P.warm_tries) { warm_miss = true; return false; }
+      if (warm_used && i >= P.warm_tries) { warm_miss = true; return false; }
       if (std::fabs(f0 - f1) > 1e-9) {
         p2 = p1 - f1 * (p1 - p0) / (f1 - f0);
         if (p2 < p0) p2 -= 0.1 * (p1 - p0);
@@ -306,7 +310,7 @@ class ExactRiemann {
     bool success = true;
     int found = Acoustic(rhol, ul, pl, el, cl, idl, rhor, ur, pr, er, cr, idr, p0, rhol0, rhor0, ul0, ur0, p1, rhol1, rhor1, ul1, ur1);
     if (found == 2) return true;
-    if (warm_p > 0.0) { warm_miss = true; return false; }
+    if (warm_used) { warm_miss = true; return false; }
     if (found != 1) {
       dp = (pl != pr) ? std::fabs(pl - pr) : 0.5 * pl;
       for (int i = 0; i < P.maxIts_bracket; i++) {
@@ -354,7 +358,12 @@ class ExactRiemann {
                double& p0, double& rhol0, double& rhor0, double& ul0, double& ur0,
                double& p1, double& rhol1, double& rhor1, double& ul1, double& ur1) {
     int found = 0;
-    if (warm_p > 0.0) {
+    double Cl = rhol * cl, Cr = rhor * cr;
+    p0 = (Cr * pl + Cl * pr + Cl * Cr * (ul - ur)) / (Cl + Cr);
+    // warm start only where the prediction differs from the acoustic estimate
+    // by more than warm_gate (relative)
+    warm_used = warm_p > 0.0 && !(std::fabs(warm_p - p0) <= P.warm_gate * std::fabs(p0));
+    if (warm_used) {
       // learned warm start (not in the reference): the starting pair brackets
       // the prediction, warm_p (1 -+ warm_delta), in place of the acoustic pair
       p0 = warm_p * (1.0 - P.warm_delta);
@@ -368,8 +377,6 @@ class ExactRiemann {
       if (!RhoUStar(3, path3_, rhor, ur, pr, p1, idr, rhor, (p1 > pr) ? rhor * 1.1 : rhor * 0.9, rhor1, ur1, nullptr, nullptr)) return found;
       return 2;
     }
-    double Cl = rhol * cl, Cr = rhor * cr;
-    p0 = (Cr * pl + Cl * pr + Cl * Cr * (ul - ur)) / (Cl + Cr);
     evals++;
     if (!RhoUStar(1, path1_, rhol, ul, pl, p0, idl, rhol, (p0 > pl) ? rhol * 1.1 : rhol * 0.9, rhol0, ul0, nullptr, nullptr)) return found;
     if (!RhoUStar(3, path3_, rhor, ur, pr, p0, idr, rhor, (p0 > pr) ? rhor * 1.1 : rhor * 0.9, rhor0, ur0, nullptr, nullptr)) return found;
