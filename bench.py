@@ -284,24 +284,28 @@ def run_gb300(args):
     if args.ws_train > 0 and rank == 0:
         from m2c_gb300 import warmstart as ws
         res, net = ws.study(n_train=args.ws_train, n_test=args.ws_test, epochs=args.ws_epochs, keep_net=True)
-        s.set_warm_start(net)
-        s.run(args.warmup)
-        w0 = s.counters()
-        lib.m2cg_event_record(ctx, 0)
-        s.run(args.steps)
-        lib.m2cg_event_record(ctx, 1)
-        lib.m2cg_sync(ctx)
+        # the same steps from the same initial state, with the network in the loop
+        s2 = Solver(cfg, FluidState(V, ID, phi))
+        s2.set_warm_start(net)
+        s2.run(args.warmup)
+        w0 = s2.counters()
+        lib.m2cg_event_record(s2.ctx, 0)
+        s2.run(args.steps)
+        lib.m2cg_event_record(s2.ctx, 1)
+        lib.m2cg_sync(s2.ctx)
         wms = C.c_float()
-        abi.check(lib, lib.m2cg_event_elapsed(ctx, 0, 1, C.byref(wms)), "elapsed")
-        w1 = s.counters()
-        s.set_warm_start(None)
+        abi.check(lib, lib.m2cg_event_elapsed(s2.ctx, 0, 1, C.byref(wms)), "elapsed")
+        w1 = s2.counters()
+        s2.set_warm_start(None)
+        s2.close()
         wsolves = w1["riemann_solves"] - w0["riemann_solves"]
         res["fv_step"] = {"value_warm": cells * stages * args.steps / (wms.value * 1e-3), "unit": UNIT,
                           "value_cold": value,
                           "mean_iters_per_solve_warm": (w1["riemann_iterations"] - w0["riemann_iterations"]) /
                                                        max(wsolves, 1),
                           "mean_iters_per_solve_cold": iters / max(solves, 1),
-                          "note": "warm steps follow the cold-timed ones (later states, similar face counts)"}
+                          "warm_solves": wsolves, "cold_solves": solves,
+                          "note": "the same steps from the same initial state, cold and with the network"}
         net.close()
         wsres = res
 

@@ -22,7 +22,7 @@ struct RiemannPrm {
   // secant expansions allowed before a cold restart
   double warm_delta;
   int warm_tries;
-  double warm_gate;  // the prediction is used only where it differs from the acoustic estimate by more
+  double warm_gate;  // the prediction is used only where the acoustic jump / pressure exceeds this
 };
 
 // Status bits returned alongside the reference's error code.
@@ -67,8 +67,8 @@ struct ExactRiemannDev {
   RiemannPrm P;
   PathCache path1, path3;
   int evals;
-  // Learned warm start: with warm_p > 0 differing from the acoustic estimate
-  // by more than P.warm_gate (relative), the starting pair is
+  // Learned warm start: with warm_p > 0 on a face whose acoustic pressure
+  // jump exceeds P.warm_gate times the mean pressure, the starting pair is
   // warm_p (1 -+ P.warm_delta) instead of the acoustic-theory pair; if that
   // pair is not physical or P.warm_tries secant expansions do not bracket the
   // root, solve_once returns 3 and solve restarts cold (the reference's path).
@@ -432,10 +432,12 @@ struct ExactRiemannDev {
                         double& p1, double& rhol1, double& rhor1, double& ul1, double& ur1) {
     double Cl = rhol * cl, Cr = rhor * cr;
     p0 = (Cr * pl + Cl * pr + Cl * Cr * (ul - ur)) / (Cl + Cr);
-    // the prediction replaces the acoustic estimate only where the two differ
-    // by more than warm_gate (relative); elsewhere acoustic theory is already
-    // as close as the network
-    warm_used = warm_p > 0.0 && !(fabs(warm_p - p0) <= P.warm_gate * fabs(p0));
+    // the prediction replaces the acoustic estimate only where the acoustic
+    // pressure jump exceeds warm_gate times the impedance-weighted pressure:
+    // the linearization's error grows like the square of that ratio, and
+    // below it acoustic theory is closer than the network
+    const double pbar = (Cr * pl + Cl * pr) / (Cl + Cr);
+    warm_used = warm_p > 0.0 && fabs(p0 - pbar) > P.warm_gate * fabs(pbar);
     if (warm_used) {
       // learned warm start: the two starting points bracket the prediction,
       // p_hat (1 -+ warm_delta), in place of the acoustic-theory pair; the

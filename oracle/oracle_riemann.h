@@ -16,7 +16,7 @@ struct RiemannParams {
   double min_pressure = -1e8, failure_threshold = 0.2, pressure_at_failure = 1e-8;
   double warm_delta = 1e-5;  // learned warm start (not in the reference)
   int warm_tries = 3;
-  double warm_gate = 0.05;
+  double warm_gate = 0.15;
 };
 
 class ExactRiemann {
@@ -28,8 +28,8 @@ class ExactRiemann {
   int evals = 0;
   int main_iters = 0;
   // Optional warm start (the learned warm start; the reference path passes 0):
-  // when > 0 and off the acoustic estimate by more than P.warm_gate
-  // (relative), the starting pair is warm_p (1 -+ P.warm_delta) instead of the
+  // when > 0 on a problem whose acoustic pressure jump exceeds P.warm_gate
+  // times the mean pressure, the starting pair is warm_p (1 -+ P.warm_delta) instead of the
   // acoustic-theory pair; if that pair is not physical, or P.warm_tries secant
   // expansions do not bracket the root, the solve restarts cold (SolveOnce
   // returns 3 to Solve).
@@ -360,9 +360,10 @@ class ExactRiemann {
     int found = 0;
     double Cl = rhol * cl, Cr = rhor * cr;
     p0 = (Cr * pl + Cl * pr + Cl * Cr * (ul - ur)) / (Cl + Cr);
-    // warm start only where the prediction differs from the acoustic estimate
-    // by more than warm_gate (relative)
-    warm_used = warm_p > 0.0 && !(std::fabs(warm_p - p0) <= P.warm_gate * std::fabs(p0));
+    // warm start only where the acoustic pressure jump exceeds warm_gate times
+    // the impedance-weighted pressure
+    const double pbar = (Cr * pl + Cl * pr) / (Cl + Cr);
+    warm_used = warm_p > 0.0 && std::fabs(p0 - pbar) > P.warm_gate * std::fabs(pbar);
     if (warm_used) {
       // learned warm start (not in the reference): the starting pair brackets
       // the prediction, warm_p (1 -+ warm_delta), in place of the acoustic pair
