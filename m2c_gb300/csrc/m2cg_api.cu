@@ -194,7 +194,7 @@ m2cg_status m2cg_fill_params(const m2cg_config& c, m2cg::Params& P) {
   r.min_pressure = c.min_pressure; r.failure_threshold = c.failure_threshold; r.pressure_at_failure = c.pressure_at_failure;
   r.warm_delta = 1e-5;
   r.warm_tries = 3;
-  r.warm_gate = 0.15;
+  r.warm_gate = 0.05;
   // tuning overrides for the learned warm start
   if (const char* e = getenv("M2CG_WARM_GATE")) r.warm_gate = atof(e);
   if (const char* e = getenv("M2CG_WARM_DELTA")) r.warm_delta = atof(e);

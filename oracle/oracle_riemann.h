@@ -16,7 +16,7 @@ struct RiemannParams {
   double min_pressure = -1e8, failure_threshold = 0.2, pressure_at_failure = 1e-8;
   double warm_delta = 1e-5;  // learned warm start (not in the reference)
   int warm_tries = 3;
-  double warm_gate = 0.15;
+  double warm_gate = 0.05;
 };
 
 class ExactRiemann {
