@@ -291,6 +291,27 @@ m2cg_status m2cg_mlp_predict(m2cg_mlp* mlp, int64_t n, const double* W, const do
  * use by the context; the step's CUDA graph is captured again. */
 m2cg_status m2cg_set_warm_start(m2cg_ctx* ctx, m2cg_mlp* mlp);
 
+/* ---- batched ensemble of independent domains ----------------------------
+ * No reference counterpart (the reference runs one domain per program): n
+ * member domains, each an ordinary context (m2cg_ensemble_member returns it;
+ * upload / download / counters work on it as on any context), advanced
+ * together with one launch per kernel and Runge-Kutta stage for all members
+ * (one block row per member, the interface Riemann solves of all members as
+ * one pool) inside one CUDA graph.  Members may differ in mesh, materials,
+ * boundary conditions and state; they must share the time integrator (RK2 or
+ * RK3), the level-set count and the interface reconstruction.  Each member
+ * keeps its own CFL time step.  m2cg_ensemble_run_sequential advances the
+ * members one after another with their own per-domain launches (the baseline
+ * the batched step is compared with); ms: elapsed milliseconds. */
+typedef struct m2cg_ensemble m2cg_ensemble;
+m2cg_status m2cg_ensemble_create(const m2cg_config* cfgs, int32_t n, m2cg_ensemble** out);
+void m2cg_ensemble_destroy(m2cg_ensemble* ens);
+int32_t m2cg_ensemble_size(const m2cg_ensemble* ens);
+m2cg_ctx* m2cg_ensemble_member(m2cg_ensemble* ens, int32_t i);
+m2cg_status m2cg_ensemble_run(m2cg_ensemble* ens, int32_t n_steps, float* ms);
+m2cg_status m2cg_ensemble_run_sequential(m2cg_ensemble* ens, int32_t n_steps, float* ms);
+int64_t m2cg_ensemble_kernel_launches(const m2cg_ensemble* ens);
+
 /* ---- timing on the context stream -------------------------------------- */
 m2cg_status m2cg_sync(m2cg_ctx* ctx);
 /* Records CUDA event `slot` (0..15) on the context stream. */

@@ -198,6 +198,13 @@ def load(path=None):
         "m2cg_mlp_forward": (C.c_int, [_P, C.c_int64, _F, _F]),
         "m2cg_mlp_predict": (C.c_int, [_P, C.c_int64, _D, _D, _D, _F]),
         "m2cg_set_warm_start": (C.c_int, [_P, _P]),
+        "m2cg_ensemble_create": (C.c_int, [C.POINTER(Config), C.c_int32, C.POINTER(_P)]),
+        "m2cg_ensemble_destroy": (None, [_P]),
+        "m2cg_ensemble_size": (C.c_int32, [_P]),
+        "m2cg_ensemble_member": (_P, [_P, C.c_int32]),
+        "m2cg_ensemble_run": (C.c_int, [_P, C.c_int32, _F]),
+        "m2cg_ensemble_run_sequential": (C.c_int, [_P, C.c_int32, _F]),
+        "m2cg_ensemble_kernel_launches": (C.c_int64, [_P]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -5,11 +5,13 @@
 #include <cstring>
 #include <cstdarg>
 #include <cstdlib>
+#include <chrono>
 #include <vector>
 #include <string>
 #include <algorithm>
 #include <cuda_bf16.h>
 #include "m2cg_internal.h"
+#include "m2cg_ens.h"
 
 namespace m2cg {
 void launch_reconstruct(cudaStream_t, const Params&, const StateSet&, const int32_t*, double* const*, unsigned long long*);
@@ -107,6 +109,7 @@ struct m2cg_ctx {
   DevScalars* sc = nullptr;
   unsigned long long* cnt = nullptr;
   double* scratch = nullptr;
+  double* ext_scratch = nullptr;  // set for ensemble members: scratch owned by the ensemble
   // Integration-path cache entries per wave.  The reference keeps an unbounded
   // std::vector; 1024 entries covers the longest paths seen on random two-material
   // problems (767); a solve that would exceed it is counted in CNT_PATH_CAPPED.
@@ -253,7 +256,8 @@ static m2cg_status ctx_alloc(m2cg_ctx* x) {
   CK(cudaMemcpyAsync(x->d_mats, &x->P.mats, sizeof(Mats), cudaMemcpyHostToDevice, x->stream));
   x->rblocks = x->nsm * 2;
   x->rthreads = 128;
-  CK(x->alloc(&x->scratch, (size_t)6 * x->path_cap * x->rblocks * x->rthreads));
+  if (x->ext_scratch) x->scratch = x->ext_scratch;  // a member of an ensemble shares the ensemble's pool
+  else CK(x->alloc(&x->scratch, (size_t)6 * x->path_cap * x->rblocks * x->rthreads));
   CK(x->alloc(&x->strag, L.cap));
   CK(x->alloc(&x->strag_count, 1));
   x->sblocks = std::max(1, std::min(x->nsm, x->rblocks));
@@ -304,6 +308,29 @@ static PhaseTimer* g_timer = nullptr;  // set only inside m2cg_phase_times (not 
 #define PHASE_ON(c, st, stmt) do { if (g_timer) g_timer->begin(c, st); stmt; if (g_timer) g_timer->end(); } while (0)
 #define PHASE(c, stmt) PHASE_ON(c, s, stmt)
 
+// Arguments of the stage update kernel for stage `stage` of the configured scheme.
+static StageArgs stage_args(m2cg_ctx* x, int stage, bool last, const StateSet& in, const StateSet& out) {
+  StageArgs A;
+  memset(&A, 0, sizeof(A));
+  A.in = in;
+  A.out = out;
+  A.stage = stage;
+  A.last = last;
+  A.phi_lsin = in.q[5];
+  A.phi_own = in.q[5];
+  A.phi_tmp = x->S[0].q[5];
+  for (int p = 0; p < 5; p++) { A.Un[p] = x->Un[p]; A.Us[p] = x->Us[p]; }
+  const int ts = x->cfg.ts_type;
+  if (stage == 0) { A.store_un = (ts != M2CG_TS_FORWARD_EULER); }
+  if (ts == M2CG_TS_FORWARD_EULER) A.ls_use_updated_v = 1;
+  if (ts == M2CG_TS_RK2 && stage == 1) { A.a_own = 0.5; A.b_un = 0.5; A.c_dt = 0.5; A.la = 0.5; A.lb = 0.5; A.lc = 0.5; }
+  if (ts == M2CG_TS_RK3 && stage == 1) { A.a_own = 0.25; A.b_un = 0.75; A.c_dt = 0.25; A.la = 0.25; A.lb = 0.75; A.lc = 0.25; }
+  if (ts == M2CG_TS_RK3 && stage == 2) {
+    A.a_own = 2.0 / 3.0; A.b_un = 1.0 / 3.0; A.c_dt = 2.0 / 3.0; A.la = 2.0 / 3.0; A.lb = 1.0 / 3.0; A.lc = 2.0 / 3.0;
+  }
+  return A;
+}
+
 // Enqueue one Runge-Kutta stage.
 static int64_t enqueue_stage(m2cg_ctx* x, int stage, bool last, const StateSet& in, const StateSet& out) {
   cudaStream_t s = x->stream;
@@ -341,24 +368,7 @@ static int64_t enqueue_stage(m2cg_ctx* x, int stage, bool last, const StateSet& 
   if (!after_recon) { PHASE(PH_RECON, launch_reconstruct(s, P, in, x->id, x->d_fs, x->cnt)); n += 2; }
   PHASE(PH_FLUX, launch_face_flux(s, P, x->id, x->d_fs, x->d_F, x->cnt)); n++;
   cudaStreamWaitEvent(s, x->ev_join, 0);
-  StageArgs A;
-  memset(&A, 0, sizeof(A));
-  A.in = in;
-  A.out = out;
-  A.stage = stage;
-  A.last = last;
-  A.phi_lsin = in.q[5];
-  A.phi_own = in.q[5];
-  A.phi_tmp = x->S[0].q[5];
-  for (int p = 0; p < 5; p++) { A.Un[p] = x->Un[p]; A.Us[p] = x->Us[p]; }
-  const int ts = x->cfg.ts_type;
-  if (stage == 0) { A.store_un = (ts != M2CG_TS_FORWARD_EULER); }
-  if (ts == M2CG_TS_FORWARD_EULER) A.ls_use_updated_v = 1;
-  if (ts == M2CG_TS_RK2 && stage == 1) { A.a_own = 0.5; A.b_un = 0.5; A.c_dt = 0.5; A.la = 0.5; A.lb = 0.5; A.lc = 0.5; }
-  if (ts == M2CG_TS_RK3 && stage == 1) { A.a_own = 0.25; A.b_un = 0.75; A.c_dt = 0.25; A.la = 0.25; A.lb = 0.75; A.lc = 0.25; }
-  if (ts == M2CG_TS_RK3 && stage == 2) {
-    A.a_own = 2.0 / 3.0; A.b_un = 1.0 / 3.0; A.c_dt = 2.0 / 3.0; A.la = 2.0 / 3.0; A.lb = 1.0 / 3.0; A.lc = 2.0 / 3.0;
-  }
+  StageArgs A = stage_args(x, stage, last, in, out);
   PHASE(PH_UPDATE, launch_update(s, P, A, x->id, x->id_new, x->d_F, x->L, x->sc, x->swept, x->swept_count,
                                   x->swept_cap, x->cnt)); n++;
   if (!last) { PHASE(PH_BC, launch_bc(s, P, out, 1, 1, nullptr, x->sc)); n++; }
@@ -439,13 +449,14 @@ m2cg_status m2cg_config_default(m2cg_config* c) {
   return M2CG_OK;
 }
 
-m2cg_status m2cg_create(const m2cg_config* cfg, m2cg_ctx** out) {
+static m2cg_status create_ctx(const m2cg_config* cfg, double* ext_scratch, m2cg_ctx** out) {
   if (!cfg || !out) { set_err("null argument"); return M2CG_ERR_INVALID_ARG; }
   *out = nullptr;
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_err("no CUDA device"); return M2CG_ERR_NO_DEVICE; }
   m2cg_ctx* x = new m2cg_ctx();
   x->cfg = *cfg;
+  x->ext_scratch = ext_scratch;
   m2cg_status st = m2cg_fill_params(*cfg, x->P);
   if (st != M2CG_OK) { delete x; return st; }
   int dev = 0;
@@ -467,6 +478,8 @@ m2cg_status m2cg_create(const m2cg_config* cfg, m2cg_ctx** out) {
   *out = x;
   return M2CG_OK;
 }
+
+m2cg_status m2cg_create(const m2cg_config* cfg, m2cg_ctx** out) { return create_ctx(cfg, nullptr, out); }
 
 void m2cg_destroy(m2cg_ctx* x) {
   if (!x) return;
@@ -868,5 +881,328 @@ void* m2cg_host_alloc(size_t bytes) {
 void m2cg_host_free(void* p) {
   if (p) cudaFreeHost(p);
 }
+
+}  // extern "C"
+
+// ===========================================================================
+// Batched ensemble of independent member domains (m2cg_ensemble_*).
+//
+// Every member is an ordinary context (its own mesh, state and counters, all
+// the usual entry points work on it); the ensemble advances all of them with
+// one launch per kernel and RK stage: the launch has one block row per member
+// (gridDim.y = members, gridDim.x = the largest member's block count; rows of
+// smaller members exit their surplus blocks), and each row reads its member's
+// arguments from a device table.  The interface Riemann solves of all members
+// run as one pool over the concatenated face lists.  The step is captured
+// once into a CUDA graph.
+namespace m2cg {
+void launch_k_reconstruct_ens(cudaStream_t, int, const k_reconstruct_args*, int);
+void launch_k_reconstruct_ghosts_ens(cudaStream_t, int, const k_reconstruct_ghosts_args*, int);
+void launch_k_face_flux_ens(cudaStream_t, int, const k_face_flux_args*, int);
+void launch_k_update_ens(cudaStream_t, int, const k_update_args*, int);
+void launch_k_bc_ens(cudaStream_t, int, const k_bc_args*, int);
+void launch_k_dt_reduce_ens(cudaStream_t, int, const k_dt_reduce_args*, int);
+void launch_k_dt_finalize_ens(cudaStream_t, int, const k_dt_finalize_args*, int);
+void launch_k_compact_interfaces_ens(cudaStream_t, int, const k_compact_interfaces_args*, int);
+void launch_k_resolve_remaining_ens(cudaStream_t, int, const k_resolve_remaining_args*, int);
+void launch_k_commit_remaining_ens(cudaStream_t, int, const k_commit_remaining_args*, int);
+void launch_k_swept_update_ens(cudaStream_t, int, const k_swept_update_args*, int);
+void launch_k_commit_ids_ens(cudaStream_t, int, const k_commit_ids_args*, int);
+void launch_reset_counters_ens(cudaStream_t, const CounterResetArgs*, int);
+void launch_riemann_ens(cudaStream_t, const RiemannEnsArgs*, int, int64_t*, double*, int, int, int, int64_t*,
+                        unsigned long long*, int, size_t);
+cudaError_t riemann_stragglers_ens_reserve(size_t bytes);
+}  // namespace m2cg
+
+struct m2cg_ensemble {
+  std::vector<m2cg_ctx*> m;
+  int nsm = 0;
+  cudaStream_t stream = nullptr;
+  cudaEvent_t e0 = nullptr, e1 = nullptr;
+  double* scratch = nullptr;  // Riemann integration-path pool shared by the members
+  int path_cap = 1024, rblocks = 0, sblocks = 0, eval_limit = 16;
+  size_t sreserve = 0;
+  int64_t* strag = nullptr;
+  unsigned long long* strag_count = nullptr;
+  int64_t* off = nullptr;
+  std::vector<void*> dev;  // argument tables (device), in the order the step uses them
+  size_t tab_i = 0;
+  bool building = false;   // first pass: fill the tables; second pass (captured): launch
+  cudaGraphExec_t graph = nullptr;
+  int64_t launches_per_step = 0;
+  int64_t launches = 0;
+
+  template <class T>
+  T* table(const std::vector<T>& h) {
+    if (!building) return tab_i < dev.size() ? (T*)dev[tab_i++] : nullptr;
+    void* p = nullptr;
+    if (cudaMalloc(&p, std::max<size_t>(h.size(), 1) * sizeof(T)) != cudaSuccess) return nullptr;
+    dev.push_back(p);
+    if (cudaMemcpy(p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice) != cudaSuccess) return nullptr;
+    return (T*)p;
+  }
+};
+
+static int64_t ens_cells(const m2cg_ctx* x) { return (int64_t)x->P.g.nx * x->P.g.ny * x->P.g.nz; }
+static int64_t ens_faces(const m2cg_ctx* x) {
+  return (int64_t)(x->P.g.nx + 1) * (x->P.g.ny + 1) * (x->P.g.nz + 1);
+}
+static int64_t ens_ghosts(const m2cg_ctx* x) {
+  const Grid& g = x->P.g;
+  return 2 * ((int64_t)g.ny * g.nz + (int64_t)g.nx * g.nz + (int64_t)g.nx * g.ny);
+}
+template <class F>
+static int ens_grid(const m2cg_ensemble* e, F count, int block) {
+  int64_t mx = 0;
+  for (const m2cg_ctx* x : e->m) mx = std::max<int64_t>(mx, (count(x) + block - 1) / block);
+  return (int)mx;
+}
+
+// One batched time step (CFL dt per member, MaxTime clamp), enqueued on e->stream.
+static m2cg_status ens_enqueue_step(m2cg_ensemble* e, int64_t* nl) {
+  const int D = (int)e->m.size();
+  cudaStream_t s = e->stream;
+  int64_t n = 0;
+#define ENS_TABLE(T, v)                                                       \
+  T* v##_d = e->table(v);                                                    \
+  if (!v##_d) { set_err("ensemble argument table allocation failed"); return M2CG_ERR_CUDA; }
+  {
+    std::vector<k_dt_reduce_args> v(D);
+    std::vector<k_dt_finalize_args> f(D);
+    std::vector<CounterResetArgs> r(D);
+    std::vector<k_compact_interfaces_args> c(D);
+    for (int d = 0; d < D; d++) {
+      m2cg_ctx* x = e->m[d];
+      v[d] = {x->P, x->S[0], x->id, x->sc};
+      f[d] = {x->P, x->sc, 1, 0.0};
+      r[d] = {x->L.count, x->swept_count};
+      c[d] = {x->P, x->id, x->L, x->cnt, x->sc};
+    }
+    ENS_TABLE(k_dt_reduce_args, v);
+    ENS_TABLE(k_dt_finalize_args, f);
+    ENS_TABLE(CounterResetArgs, r);
+    ENS_TABLE(k_compact_interfaces_args, c);
+    if (!e->building) launch_k_dt_reduce_ens(s, ens_grid(e, ens_cells, 256), v_d, D);
+    if (!e->building) launch_k_dt_finalize_ens(s, 1, f_d, D);
+    if (!e->building) launch_reset_counters_ens(s, r_d, D);
+    if (!e->building) launch_k_compact_interfaces_ens(s, ens_grid(e, ens_faces, 256), c_d, D);
+    n += 4;
+  }
+  const m2cg_ctx* x0 = e->m[0];
+  const int nst = x0->cfg.ts_type == M2CG_TS_RK2 ? 2 : 3;
+  for (int stage = 0; stage < nst; stage++) {
+    const bool last = stage == nst - 1;
+    std::vector<RiemannEnsArgs> ra(D);
+    std::vector<k_reconstruct_args> rc(D);
+    std::vector<k_reconstruct_ghosts_args> rg(D);
+    std::vector<k_face_flux_args> ff(D);
+    std::vector<k_update_args> up(D);
+    std::vector<k_bc_args> bc(D);
+    for (int d = 0; d < D; d++) {
+      m2cg_ctx* x = e->m[d];
+      StateSet in = x->S[stage], out = last ? x->S[0] : x->S[stage + 1];
+      ra[d] = {x->P, x->d_mats, in, x->id, x->d_fs, x->L, stage == 0, nullptr, x->cnt, x->sc};
+      rc[d] = {x->P, in, x->id, x->d_fs, x->cnt};
+      rg[d] = {x->P, in, x->id, x->d_fs, x->cnt};
+      ff[d] = {x->P, x->id, x->d_fs, x->d_F, x->cnt};
+      up[d] = {x->P, stage_args(x, stage, last, in, out), x->id, x->id_new, x->d_F, x->L, x->sc, x->swept,
+               x->swept_count, x->swept_cap, x->cnt};
+      bc[d] = {x->P, out, 1, 1, nullptr, x->sc};
+    }
+    ENS_TABLE(RiemannEnsArgs, ra);
+    ENS_TABLE(k_reconstruct_args, rc);
+    ENS_TABLE(k_reconstruct_ghosts_args, rg);
+    ENS_TABLE(k_face_flux_args, ff);
+    ENS_TABLE(k_update_args, up);
+    ENS_TABLE(k_bc_args, bc);
+    const bool after_recon = (x0->P.mp_recon != M2CG_MPREC_CONSTANT);
+    auto recon = [&]() {
+      if (!e->building) launch_k_reconstruct_ens(s, ens_grid(e, ens_cells, 128), rc_d, D);
+      if (!e->building) launch_k_reconstruct_ghosts_ens(s, ens_grid(e, ens_ghosts, 128), rg_d, D);
+      n += 2;
+    };
+    if (after_recon) recon();
+    if (!e->building) launch_riemann_ens(s, ra_d, D, e->off, e->scratch, e->path_cap, e->rblocks, e->eval_limit, e->strag,
+                       e->strag_count, e->sblocks, e->sreserve);
+    n += 3;
+    if (!after_recon) recon();
+    if (!e->building) launch_k_face_flux_ens(s, ens_grid(e, ens_faces, 128), ff_d, D);
+    if (!e->building) launch_k_update_ens(s, ens_grid(e, ens_cells, 128), up_d, D);
+    n += 2;
+    if (!last) { if (!e->building) launch_k_bc_ens(s, ens_grid(e, ens_ghosts, 128), bc_d, D); n++; }
+  }
+  {
+    std::vector<k_bc_args> bc(D);
+    for (int d = 0; d < D; d++) {
+      m2cg_ctx* x = e->m[d];
+      bc[d] = {x->P, x->S[0], 1, 1, x0->P.n_ls > 0 ? x->id : nullptr, x->sc};
+    }
+    if (x0->P.n_ls > 0) {
+      // end of step: remaining swept cells, swept-cell update, IDs (MultiPhaseOperator.cpp:153-357, 980-1150)
+      const int blocks = 8;  // per member: the swept lists are short
+      std::vector<k_resolve_remaining_args> r0(D), r1(D);
+      std::vector<k_commit_remaining_args> cr(D);
+      std::vector<k_swept_update_args> su(D);
+      std::vector<k_commit_ids_args> ci(D);
+      for (int d = 0; d < D; d++) {
+        m2cg_ctx* x = e->m[d];
+        r0[d] = {x->P, x->id_new, x->swept, x->swept_count, x->swept_cap, x->cand, 0, x->sc};
+        r1[d] = r0[d];
+        r1[d].final_pass = 1;
+        cr[d] = {x->id_new, x->swept, x->swept_count, x->swept_cap, x->cand, x->sc};
+        su[d] = {x->P, x->S[0], x->id, x->id_new, x->L, x->swept, x->swept_count, x->swept_cap, x->cnt, x->sc};
+        ci[d] = {x->id, x->id_new, x->swept, x->swept_count, x->swept_cap, x->sc};
+      }
+      ENS_TABLE(k_resolve_remaining_args, r0);
+      ENS_TABLE(k_resolve_remaining_args, r1);
+      ENS_TABLE(k_commit_remaining_args, cr);
+      ENS_TABLE(k_swept_update_args, su);
+      ENS_TABLE(k_commit_ids_args, ci);
+      const int passes = 3;
+      for (int p = 0; p < passes; p++) {
+        if (!e->building) launch_k_resolve_remaining_ens(s, blocks, p == passes - 1 ? r1_d : r0_d, D);
+        if (!e->building) launch_k_commit_remaining_ens(s, blocks, cr_d, D);
+      }
+      if (!e->building) launch_k_swept_update_ens(s, blocks, su_d, D);
+      if (!e->building) launch_k_commit_ids_ens(s, blocks, ci_d, D);
+      n += 2 * passes + 2;
+    }
+    ENS_TABLE(k_bc_args, bc);
+    if (!e->building) launch_k_bc_ens(s, ens_grid(e, ens_ghosts, 128), bc_d, D);
+    n++;
+  }
+#undef ENS_TABLE
+  *nl = n;
+  return M2CG_OK;
+}
+
+extern "C" {
+
+void m2cg_ensemble_destroy(m2cg_ensemble* e) {
+  if (!e) return;
+  if (e->stream) cudaStreamSynchronize(e->stream);
+  if (e->graph) cudaGraphExecDestroy(e->graph);
+  for (m2cg_ctx* x : e->m) m2cg_destroy(x);
+  for (void* p : e->dev) cudaFree(p);
+  if (e->scratch) cudaFree(e->scratch);
+  if (e->strag) cudaFree(e->strag);
+  if (e->strag_count) cudaFree(e->strag_count);
+  if (e->off) cudaFree(e->off);
+  if (e->e0) cudaEventDestroy(e->e0);
+  if (e->e1) cudaEventDestroy(e->e1);
+  if (e->stream) cudaStreamDestroy(e->stream);
+  delete e;
+}
+
+m2cg_status m2cg_ensemble_create(const m2cg_config* cfgs, int32_t n, m2cg_ensemble** out) {
+  if (!cfgs || !out || n < 1 || n > 65535) { set_err("need 1..65535 member configurations"); return M2CG_ERR_INVALID_ARG; }
+  *out = nullptr;
+  for (int d = 1; d < n; d++) {
+    if (cfgs[d].ts_type != cfgs[0].ts_type || cfgs[d].n_levelsets != cfgs[0].n_levelsets ||
+        cfgs[d].mp_recon != cfgs[0].mp_recon) {
+      set_err("member %d: time integrator, level-set count and interface reconstruction must match member 0", d);
+      return M2CG_ERR_INVALID_ARG;
+    }
+  }
+  if (cfgs[0].ts_type == M2CG_TS_FORWARD_EULER) {
+    set_err("the batched step supports the RK2 and RK3 integrators");
+    return M2CG_ERR_INVALID_ARG;
+  }
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_err("no CUDA device"); return M2CG_ERR_NO_DEVICE; }
+  m2cg_ensemble* e = new m2cg_ensemble();
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, dev);
+  e->rblocks = e->nsm * 2;
+  e->sblocks = e->nsm;
+  if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
+      cudaEventCreate(&e->e0) != cudaSuccess || cudaEventCreate(&e->e1) != cudaSuccess ||
+      cudaMalloc(&e->scratch, (size_t)6 * e->path_cap * e->rblocks * 128 * sizeof(double)) != cudaSuccess ||
+      cudaMalloc(&e->strag_count, sizeof(unsigned long long)) != cudaSuccess ||
+      cudaMalloc(&e->off, (size_t)(n + 1) * sizeof(int64_t)) != cudaSuccess) {
+    set_err("ensemble set-up failed: %s", cudaGetErrorString(cudaGetLastError()));
+    m2cg_ensemble_destroy(e);
+    return M2CG_ERR_CUDA;
+  }
+  int64_t strag_cap = 0;
+  for (int d = 0; d < n; d++) {
+    m2cg_ctx* x = nullptr;
+    m2cg_status st = create_ctx(&cfgs[d], e->scratch, &x);
+    if (st != M2CG_OK) { m2cg_ensemble_destroy(e); return st; }
+    e->m.push_back(x);
+    strag_cap += x->L.cap;
+  }
+  e->eval_limit = e->m[0]->eval_limit;
+  if (cudaMalloc(&e->strag, (size_t)strag_cap * sizeof(int64_t)) != cudaSuccess) {
+    set_err("ensemble straggler list allocation failed");
+    m2cg_ensemble_destroy(e);
+    return M2CG_ERR_CUDA;
+  }
+  {
+    int optin = 0;
+    cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    e->sreserve = (optin > 0 && riemann_stragglers_ens_reserve((size_t)optin) == cudaSuccess) ? (size_t)optin : 0;
+    cudaGetLastError();
+  }
+  *out = e;
+  return M2CG_OK;
+}
+
+int32_t m2cg_ensemble_size(const m2cg_ensemble* e) { return e ? (int32_t)e->m.size() : 0; }
+
+m2cg_ctx* m2cg_ensemble_member(m2cg_ensemble* e, int32_t i) {
+  if (!e || i < 0 || i >= (int32_t)e->m.size()) return nullptr;
+  return e->m[i];
+}
+
+m2cg_status m2cg_ensemble_run(m2cg_ensemble* e, int32_t n_steps, float* ms) {
+  if (!e || n_steps < 0) { set_err("bad ensemble arguments"); return M2CG_ERR_INVALID_ARG; }
+  // members' own streams may still hold uploads
+  for (m2cg_ctx* x : e->m) CK(cudaStreamSynchronize(x->stream));
+  cudaStream_t s = e->stream;
+  if (!e->graph) {
+    int64_t nl = 0;
+    e->building = true;
+    m2cg_status st = ens_enqueue_step(e, &nl);
+    e->building = false;
+    if (st != M2CG_OK) return st;
+    e->tab_i = 0;
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    st = ens_enqueue_step(e, &nl);
+    cudaError_t ce = cudaStreamEndCapture(s, &g);
+    if (st != M2CG_OK) return st;
+    CK(ce);
+    CK(cudaGraphInstantiate(&e->graph, g, 0));
+    cudaGraphDestroy(g);
+    e->launches_per_step = nl;
+  }
+  CK(cudaEventRecord(e->e0, s));
+  for (int i = 0; i < n_steps; i++) {
+    CK(cudaGraphLaunch(e->graph, s));
+    e->launches += e->launches_per_step;
+  }
+  CK(cudaEventRecord(e->e1, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  if (ms) CK(cudaEventElapsedTime(ms, e->e0, e->e1));
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_ensemble_run_sequential(m2cg_ensemble* e, int32_t n_steps, float* ms) {
+  if (!e || n_steps < 0) { set_err("bad ensemble arguments"); return M2CG_ERR_INVALID_ARG; }
+  CK(cudaStreamSynchronize(e->stream));
+  auto t0 = std::chrono::steady_clock::now();
+  for (m2cg_ctx* x : e->m) {
+    m2cg_status st = m2cg_run(x, n_steps, nullptr);
+    if (st != M2CG_OK) return st;
+  }
+  auto t1 = std::chrono::steady_clock::now();
+  if (ms) *ms = (float)std::chrono::duration<double, std::milli>(t1 - t0).count();
+  return M2CG_OK;
+}
+
+int64_t m2cg_ensemble_kernel_launches(const m2cg_ensemble* e) { return e ? e->launches : 0; }
 
 }  // extern "C"

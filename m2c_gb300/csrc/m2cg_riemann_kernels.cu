@@ -7,6 +7,7 @@
 // (-fmad=false) so that the iterative solver's branch decisions follow the
 // same binary64 rounding as a CPU build of the same algorithm.
 #include "m2cg_internal.h"
+#include "m2cg_ens.h"
 
 namespace m2cg {
 
@@ -187,6 +188,119 @@ __global__ void __launch_bounds__(128) k_riemann_stragglers(Params P, const Mats
   unsigned long long acc[6] = {0, 0, 0, 0, 0, 0};
   for (int64_t k = lane * W + w; k < n; k += 32 * W) iface_solve(P, S, id, fs, L, store, warm, strag[k], rs, acc);
   iface_counts(cnt, acc);
+}
+
+// ---- batched member domains (m2cg_ensemble) ----------------------------------
+// One solve pass over the interface faces of every member domain: a global
+// index runs over the concatenated per-domain lists (exclusive prefix `off`
+// of the member counts), so the whole GPU works on all domains' faces at once
+// and the integration-path scratch is one pool shared by the members.
+
+// Prefix of the member interface counts (inactive members count zero) and
+// the per-member face counter; clears the straggler count.  One thread.
+__global__ void k_ens_iface_prefix(const RiemannEnsArgs* __restrict__ a, int D, int64_t* off,
+                                   unsigned long long* strag_count) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  int64_t t = 0;
+  for (int d = 0; d < D; d++) {
+    off[d] = t;
+    int64_t n = (a[d].sc && !a[d].sc->active) ? 0 : (int64_t)min((unsigned long long)a[d].L.cap, *a[d].L.count);
+    if (n) atomicAdd(&a[d].cnt[CNT_IFACE], (unsigned long long)n);
+    t += n;
+  }
+  off[D] = t;
+  *strag_count = 0;
+}
+
+__device__ __forceinline__ int ens_domain(const int64_t* off, int D, int64_t g) {
+  int lo = 0, hi = D - 1;  // largest d with off[d] <= g
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (off[mid] <= g) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+__device__ __forceinline__ void ens_flush(unsigned long long* cnt, unsigned long long (&acc)[6]) {
+  iface_counts(cnt, acc);
+  for (int i = 0; i < 6; i++) acc[i] = 0;
+}
+
+__global__ void k_riemann_interfaces_ens(const RiemannEnsArgs* __restrict__ a, int D, const int64_t* __restrict__ off,
+                                         double* scratch, int path_cap, int eval_limit, int64_t* strag,
+                                         unsigned long long* strag_count) {
+  const int64_t n = off[D];
+  int64_t T = (int64_t)gridDim.x * blockDim.x;
+  int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  ExactRiemannDev rs;
+  init_solver(rs, a[0].md, a[0].P.rp, scratch, path_cap, tid, T);
+  rs.eval_limit = eval_limit;
+  unsigned long long acc[6] = {0, 0, 0, 0, 0, 0};
+  int dcur = -1;
+  for (int64_t g = tid; g < n; g += T) {
+    int d = ens_domain(off, D, g);
+    const RiemannEnsArgs& e = a[d];
+    if (d != dcur) {
+      if (dcur >= 0) ens_flush(a[dcur].cnt, acc);
+      dcur = d;
+    }
+    rs.mats = e.md;
+    rs.P = e.P.rp;
+    int64_t s = g - off[d];
+    if (iface_solve(e.P, e.S, e.id, e.fs, e.L, e.store, e.warm, s, rs, acc) == 2) {
+      unsigned long long k = atomicAdd(strag_count, 1ull);  // k < n
+      strag[k] = ((int64_t)d << 40) | s;
+    }
+  }
+  if (dcur >= 0) ens_flush(a[dcur].cnt, acc);
+}
+
+// The listed faces of all members, dealt lane-major over the warps as in
+// k_riemann_stragglers (one face per warp while there are no more faces than
+// warps).
+__global__ void __launch_bounds__(128) k_riemann_stragglers_ens(const RiemannEnsArgs* __restrict__ a, double* scratch,
+                                                                int path_cap, size_t reserve_bytes,
+                                                                const int64_t* __restrict__ strag,
+                                                                const unsigned long long* strag_count) {
+  extern __shared__ __align__(16) double s_path[];
+  const int64_t n = (int64_t)*strag_count;
+  const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
+  const int64_t lane = threadIdx.x & 31;
+  int64_t T = (int64_t)gridDim.x * blockDim.x;
+  int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  ExactRiemannDev rs;
+  init_solver(rs, a[0].md, a[0].P.rp, scratch, path_cap, tid, T);
+  const size_t per_warp = (size_t)6 * path_cap;
+  if (lane == 0 && (size_t)(blockDim.x >> 5) * per_warp * sizeof(double) <= reserve_bytes) {
+    rs.path1.base = s_path + (threadIdx.x >> 5) * per_warp;
+    rs.path1.stride = 1;
+    rs.path3.base = rs.path1.base + (size_t)3 * path_cap;
+    rs.path3.stride = 1;
+  }
+  unsigned long long acc[6] = {0, 0, 0, 0, 0, 0};
+  for (int64_t k = lane * W + w; k < n; k += 32 * W) {
+    int64_t v = strag[k];
+    int d = (int)(v >> 40);
+    int64_t s = v & ((1ll << 40) - 1);
+    const RiemannEnsArgs& e = a[d];
+    rs.mats = e.md;
+    rs.P = e.P.rp;
+    iface_solve(e.P, e.S, e.id, e.fs, e.L, e.store, e.warm, s, rs, acc);
+    ens_flush(e.cnt, acc);
+  }
+}
+
+void launch_riemann_ens(cudaStream_t s, const RiemannEnsArgs* a, int D, int64_t* off, double* scratch, int path_cap,
+                        int blocks, int eval_limit, int64_t* strag, unsigned long long* strag_count, int sblocks,
+                        size_t reserve_smem) {
+  k_ens_iface_prefix<<<1, 1, 0, s>>>(a, D, off, strag_count);
+  k_riemann_interfaces_ens<<<blocks, 128, 0, s>>>(a, D, off, scratch, path_cap, eval_limit, strag, strag_count);
+  k_riemann_stragglers_ens<<<sblocks, 128, reserve_smem, s>>>(a, scratch, path_cap, reserve_smem, strag, strag_count);
+}
+cudaError_t riemann_stragglers_ens_reserve(size_t bytes) {
+  return cudaFuncSetAttribute(k_riemann_stragglers_ens, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
 }
 
 // Batched independent problems (device arrays, AoS rows of 5 / 3).

@@ -1,0 +1,54 @@
+"""Batched ensemble of independent multi-material domains (m2cg_ensemble_*).
+
+Each member is an ordinary context -- `member(i)` returns a Solver view of it
+for uploads, downloads and counters -- and `run` advances all members with one
+launch per kernel and RK stage inside a CUDA graph; `run_sequential` advances
+them one after another with per-domain launches, the baseline."""
+import ctypes as C
+
+from . import abi
+from .solver import Solver
+
+
+class Ensemble:
+    def __init__(self, cfgs, lib=None):
+        self.lib = lib or abi.load()
+        self.cfgs = list(cfgs)
+        arr = (abi.Config * len(self.cfgs))(*self.cfgs)
+        h = C.c_void_p()
+        abi.check(self.lib, self.lib.m2cg_ensemble_create(arr, len(self.cfgs), C.byref(h)), "m2cg_ensemble_create")
+        self.h = h
+        self.members = [Solver.member(self.lib, c, self.lib.m2cg_ensemble_member(h, i))
+                        for i, c in enumerate(self.cfgs)]
+
+    def __len__(self):
+        return len(self.cfgs)
+
+    def member(self, i):
+        return self.members[i]
+
+    def run(self, nsteps):
+        """Batched steps; returns device milliseconds."""
+        ms = C.c_float()
+        abi.check(self.lib, self.lib.m2cg_ensemble_run(self.h, int(nsteps), C.byref(ms)), "m2cg_ensemble_run")
+        return ms.value
+
+    def run_sequential(self, nsteps):
+        """Per-domain launches, one member after another; returns wall milliseconds."""
+        ms = C.c_float()
+        abi.check(self.lib, self.lib.m2cg_ensemble_run_sequential(self.h, int(nsteps), C.byref(ms)),
+                  "m2cg_ensemble_run_sequential")
+        return ms.value
+
+    def kernel_launches(self):
+        return self.lib.m2cg_ensemble_kernel_launches(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            for m in self.members:
+                m.ctx = None
+            self.lib.m2cg_ensemble_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        self.close()

@@ -119,3 +119,52 @@ def shock_bubble(n=256, seed=2024, radius=0.15, noise=0.01):
     V[:, 0] *= 1.0 + noise * uniform_noise(N, seed)
     ID = gas.astype(np.int32)
     return c, V, ID, phi
+
+
+EDGES = (32, 48, 64, 96, 128)
+
+
+def bubble_collapse(nx, ny, nz, radius_frac, p_water, h=1.0e-3):
+    """One bubble-collapse domain: a gas bubble (SG 1.4, rho 0.12, p 1e4 Pa) of
+    radius radius_frac times the box's shortest side at the box centre, in
+    water (SG 6.12, p_inf 3.43e8, rho 1000) at p_water; cubic cells of side h;
+    phi = |x - c| - r; MUSCL / van Albada, HLLC, exact interface Riemann at
+    1e-10, RK2, CFL 0.4, Outlet on every side."""
+    c = abi.default_config()
+    c.nx, c.ny, c.nz = nx, ny, nz
+    c.x0, c.xmax, c.y0, c.ymax, c.z0, c.zmax = 0.0, nx * h, 0.0, ny * h, 0.0, nz * h
+    c.n_materials = 2
+    abi.set_material(c.mat[0], abi.EOS_SG, gamma=6.12, pc=3.43e8)
+    abi.set_material(c.mat[1], abi.EOS_SG, gamma=1.4, pc=0.0)
+    for s in range(6):
+        c.bc[s] = abi.BC_OUTLET
+    c.flux = abi.FLUX_HLLC
+    c.rec_type = abi.REC_LINEAR
+    c.limiter = abi.LIM_VANALBADA
+    c.tol_main = 1e-10
+    c.n_levelsets, c.ls_matid = 1, 1
+    c.ts_type = abi.TS_RK2
+    c.cfl = 0.4
+    X, Y, Z = cell_centers(c)
+    ctr = np.array([nx, ny, nz]) * h * 0.5
+    r = radius_frac * min(nx, ny, nz) * h
+    phi = np.sqrt((X - ctr[0]) ** 2 + (Y - ctr[1]) ** 2 + (Z - ctr[2]) ** 2) - r
+    gas = phi < 0
+    V = np.zeros((X.size, 5))
+    V[:, 0] = np.where(gas, 0.12, 1000.0)
+    V[:, 4] = np.where(gas, 1.0e4, p_water)
+    return c, V, gas.astype(np.int32), phi
+
+
+def bubble_collapse_ensemble(n_domains=512, seed=4096, edges=EDGES):
+    """Uneven ensemble: edges per axis drawn uniformly from `edges`, bubble
+    radius uniform in [0.1, 0.3] of the box, water pressure log-uniform in
+    [1e6, 1e8] Pa, gas at 1e4 Pa.  Returns a list of (cfg, V, ID, phi)."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    out = []
+    for _ in range(n_domains):
+        nx, ny, nz = (int(e) for e in rng.choice(edges, 3))
+        rf = rng.uniform(0.1, 0.3)
+        pw = 10.0 ** rng.uniform(6.0, 8.0)
+        out.append(bubble_collapse(nx, ny, nz, rf, pw))
+    return out

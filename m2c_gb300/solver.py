@@ -34,9 +34,17 @@ class Solver:
         if state is not None:
             self.set_state(state)
 
+    @classmethod
+    def member(cls, lib, cfg, ctx):
+        """A view of a context owned elsewhere (an ensemble member): not destroyed by close()."""
+        s = cls.__new__(cls)
+        s.lib, s.cfg, s.n, s.ctx, s._owned = lib, cfg, cfg.nx * cfg.ny * cfg.nz, ctx, False
+        return s
+
     def close(self):
         if getattr(self, "ctx", None):
-            self.lib.m2cg_destroy(self.ctx)
+            if getattr(self, "_owned", True):
+                self.lib.m2cg_destroy(self.ctx)
             self.ctx = None
 
     def __del__(self):

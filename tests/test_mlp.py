@@ -170,12 +170,15 @@ def test_forward_and_gradients_match_reference():
 
 @gpu
 def test_training_and_warm_start():
-    res = ws.study(n_train=1 << 17, n_test=1 << 14, epochs=30, batch=4096, lr=3e-3, seed=99)
-    assert res["loss_last_epoch"] < 0.2 * res["loss_first_epoch"]
-    assert res["pstar_rel_err_median"] < 0.05
-    # the warm start costs no more evaluations than the cold start ...
-    assert res["iters_warm_mean_converged"] <= 1.02 * res["iters_cold_mean_converged"]
-    # ... and ends where the cold start ends, within the reference's stopping rule
+    """A network trained on 2^20 labelled problems saves evaluations on the
+    problems both starts solve, and the warm-started solve ends where the cold
+    one ends within the reference's stopping rule."""
+    res = ws.study(n_train=1 << 20, n_test=1 << 15, epochs=60, batch=16384, lr=3e-3, seed=99)
+    assert res["loss_last_epoch"] < 0.05 * res["loss_first_epoch"]
+    assert res["pstar_rel_err_median"] < 0.03
+    assert res["iters_warm_mean_converged"] < res["iters_cold_mean_converged"]
+    # the bound for any predictor: the same solver started at the converged root
+    assert res["converged_set"]["iters_exact_start_mean"] < res["iters_warm_mean_converged"]
     assert res["warm_vs_cold_pstar_rel_median"] < 1e-5 and res["warm_vs_cold_pstar_rel_p99"] < 1e-3
     assert res["failed_warm"] <= res["failed_cold"] + 2
 
