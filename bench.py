@@ -56,6 +56,9 @@ def parse():
     ap.add_argument("--ws-train", type=int, default=1 << 20)
     ap.add_argument("--ws-test", type=int, default=1 << 17)
     ap.add_argument("--ws-epochs", type=int, default=60)
+    # batched ensemble of uneven bubble-collapse domains (0 disables it)
+    ap.add_argument("--ens-domains", type=int, default=64)
+    ap.add_argument("--ens-steps", type=int, default=10)
     return ap.parse_args()
 
 
@@ -171,6 +174,40 @@ def run_reference(args):
                    "the m2c binary needs MPI + PETSc, absent on the box"}
     print(json.dumps(out))
     return 0
+
+
+def ensemble_bench(n_domains, steps):
+    """Batched ensemble (edges per axis from {32,48,64,96,128}, bubble radius
+    [0.1,0.3] of the box, water 1e6..1e8 Pa, gas 1e4 Pa, RK2): the same steps
+    from the same initial states, batched (one launch per kernel and stage for
+    all members, device-timed) and with per-domain launches one member after
+    another (wall-timed, each member's own CUDA graph)."""
+    from m2c_gb300 import problems
+    from m2c_gb300.ensemble import Ensemble
+    from m2c_gb300.solver import FluidState
+    doms = problems.bubble_collapse_ensemble(n_domains, seed=4096)
+    cells = sum(c.nx * c.ny * c.nz for c, *_ in doms)
+    ens = Ensemble([d[0] for d in doms])
+    out = {"workload": f"{n_domains} bubble-collapse domains, edges per axis from {{32,48,64,96,128}}, "
+                       f"SG gas / SG water, MUSCL-van Albada, HLLC, exact interface Riemann @1e-10, RK2, CFL 0.4",
+           "domains": n_domains, "cells": cells, "steps": steps}
+    def reset():
+        for i, (c, V, ID, phi) in enumerate(doms):
+            ens.member(i).set_state(FluidState(V, ID, phi))
+
+    for mode in ("batched", "sequential"):
+        run = ens.run if mode == "batched" else ens.run_sequential
+        reset()
+        run(1)  # graph capture
+        reset()
+        l0 = ens.kernel_launches()
+        ms = run(steps)
+        out[mode] = {"ms": ms, "value": cells * 2 * steps / (ms * 1e-3), "unit": UNIT}
+        if mode == "batched":
+            out[mode]["gpu_launches_per_step"] = (ens.kernel_launches() - l0) / max(steps, 1)
+    out["speedup"] = out["sequential"]["ms"] / out["batched"]["ms"]
+    ens.close()
+    return out
 
 
 def run_gb300(args):
@@ -309,6 +346,10 @@ def run_gb300(args):
         net.close()
         wsres = res
 
+    ensres = None
+    if args.ens_domains > 0 and rank == 0:
+        ensres = ensemble_bench(args.ens_domains, args.ens_steps)
+
     if rank != 0:
         return 0
     cpu = None
@@ -336,6 +377,7 @@ def run_gb300(args):
                                                      max(stages * args.steps, 1),
                        "errors": c1["riemann_errors"] - c0["riemann_errors"], "warm_start": "cold"},
            "warm_start": wsres,
+           "ensemble": ensres,
            "phase_ms_per_step": phase,
            "counters": {k: c1[k] for k in ("clipped_cells", "nonphysical", "swept_cells", "unresolved_cells")}}
     print(json.dumps(out))
