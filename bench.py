@@ -59,6 +59,9 @@ def parse():
     # batched ensemble of uneven bubble-collapse domains (0 disables it)
     ap.add_argument("--ens-domains", type=int, default=64)
     ap.add_argument("--ens-steps", type=int, default=10)
+    # large production-shaped run (8 gas bubbles in NASG water, 5e8 Pa shock, RK3): off by default
+    ap.add_argument("--large", type=int, default=0, help="cells per axis of the large run (e.g. 512)")
+    ap.add_argument("--large-steps", type=int, default=10)
     return ap.parse_args()
 
 
@@ -210,6 +213,53 @@ def ensemble_bench(n_domains, steps):
     return out
 
 
+def large_bench(n, steps, warmup=2, ws_train=1 << 20):
+    """n^3 bubble cluster in NASG water hit by a 5e8 Pa shock, RK3: device-timed
+    cell-stage updates/s and the interface-solve share of the step, cold and
+    with the learned warm start, the same steps from the same initial state.
+    The reference reinitializes the level set every 10 steps; this path has no
+    reinitializer yet, so the level set is only advected."""
+    from m2c_gb300 import abi, problems
+    from m2c_gb300 import warmstart as ws
+    from m2c_gb300.solver import FluidState, Solver
+    lib = abi.load()
+    cfg, V, ID, phi = problems.bubble_cluster_shock(n=n)
+    cells = n ** 3
+    s = Solver(cfg, FluidState(V, ID, phi))
+    out = {"workload": f"{n}^3 cluster of 8 SG gas bubbles in NASG water, 5e8 Pa planar shock, MUSCL-van Albada, "
+                       f"HLLC, exact interface Riemann @1e-10, RK3, CFL 0.4 (level set advected, not reinitialized)",
+           "cells": cells, "steps": steps, "stages_per_step": 3}
+    net = None
+    for mode in ("cold", "warm"):
+        if mode == "warm":
+            _, net = ws.study(n_train=ws_train, n_test=1 << 12, epochs=60, keep_net=True)
+            s.set_warm_start(net)
+        s.set_state(FluidState(V, ID, phi))
+        s.run(warmup)
+        c0 = s.counters()
+        lib.m2cg_event_record(s.ctx, 0)
+        s.run(steps)
+        lib.m2cg_event_record(s.ctx, 1)
+        lib.m2cg_sync(s.ctx)
+        ms = C.c_float()
+        abi.check(lib, lib.m2cg_event_elapsed(s.ctx, 0, 1, C.byref(ms)), "elapsed")
+        c1 = s.counters()
+        ph = np.zeros(9)
+        abi.check(lib, lib.m2cg_phase_times(s.ctx, 1, abi.dptr(ph)), "phase_times")
+        solves = c1["riemann_solves"] - c0["riemann_solves"]
+        out[mode] = {"value": cells * 3 * steps / (ms.value * 1e-3), "unit": UNIT, "ms_per_step": ms.value / steps,
+                     "riemann_solves": solves,
+                     "mean_iters_per_solve": (c1["riemann_iterations"] - c0["riemann_iterations"]) / max(solves, 1),
+                     "riemann_first_pass_ms_per_step": float(ph[4]),
+                     "riemann_stragglers_ms_per_step": float(ph[8]),
+                     "interface_faces_per_stage": (c1["interface_faces"] - c0["interface_faces"]) / (3 * steps)}
+    s.set_warm_start(None)
+    s.close()
+    if net is not None:
+        net.close()
+    return out
+
+
 def run_gb300(args):
     rank, world, local = dist_info()
     pg = None
@@ -349,6 +399,10 @@ def run_gb300(args):
     ensres = None
     if args.ens_domains > 0 and rank == 0:
         ensres = ensemble_bench(args.ens_domains, args.ens_steps)
+    largeres = None
+    if args.large > 0 and rank == 0:
+        s.close()  # the large run needs the device memory of the 256^3 context
+        largeres = large_bench(args.large, args.large_steps)
 
     if rank != 0:
         return 0
@@ -378,6 +432,7 @@ def run_gb300(args):
                        "errors": c1["riemann_errors"] - c0["riemann_errors"], "warm_start": "cold"},
            "warm_start": wsres,
            "ensemble": ensres,
+           "large": largeres,
            "phase_ms_per_step": phase,
            "counters": {k: c1[k] for k in ("clipped_cells", "nonphysical", "swept_cells", "unresolved_cells")}}
     print(json.dumps(out))

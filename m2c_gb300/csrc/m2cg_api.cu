@@ -896,18 +896,18 @@ void m2cg_host_free(void* p) {
 // run as one pool over the concatenated face lists.  The step is captured
 // once into a CUDA graph.
 namespace m2cg {
-void launch_k_reconstruct_ens(cudaStream_t, int, const k_reconstruct_args*, int);
-void launch_k_reconstruct_ghosts_ens(cudaStream_t, int, const k_reconstruct_ghosts_args*, int);
-void launch_k_face_flux_ens(cudaStream_t, int, const k_face_flux_args*, int);
-void launch_k_update_ens(cudaStream_t, int, const k_update_args*, int);
-void launch_k_bc_ens(cudaStream_t, int, const k_bc_args*, int);
-void launch_k_dt_reduce_ens(cudaStream_t, int, const k_dt_reduce_args*, int);
-void launch_k_dt_finalize_ens(cudaStream_t, int, const k_dt_finalize_args*, int);
-void launch_k_compact_interfaces_ens(cudaStream_t, int, const k_compact_interfaces_args*, int);
-void launch_k_resolve_remaining_ens(cudaStream_t, int, const k_resolve_remaining_args*, int);
-void launch_k_commit_remaining_ens(cudaStream_t, int, const k_commit_remaining_args*, int);
-void launch_k_swept_update_ens(cudaStream_t, int, const k_swept_update_args*, int);
-void launch_k_commit_ids_ens(cudaStream_t, int, const k_commit_ids_args*, int);
+void launch_k_reconstruct_ens(cudaStream_t, int64_t, const k_reconstruct_args*, const int64_t*, int);
+void launch_k_reconstruct_ghosts_ens(cudaStream_t, int64_t, const k_reconstruct_ghosts_args*, const int64_t*, int);
+void launch_k_face_flux_ens(cudaStream_t, int64_t, const k_face_flux_args*, const int64_t*, int);
+void launch_k_update_ens(cudaStream_t, int64_t, const k_update_args*, const int64_t*, int);
+void launch_k_bc_ens(cudaStream_t, int64_t, const k_bc_args*, const int64_t*, int);
+void launch_k_dt_reduce_ens(cudaStream_t, int64_t, const k_dt_reduce_args*, const int64_t*, int);
+void launch_k_dt_finalize_ens(cudaStream_t, int64_t, const k_dt_finalize_args*, const int64_t*, int);
+void launch_k_compact_interfaces_ens(cudaStream_t, int64_t, const k_compact_interfaces_args*, const int64_t*, int);
+void launch_k_resolve_remaining_ens(cudaStream_t, int64_t, const k_resolve_remaining_args*, const int64_t*, int);
+void launch_k_commit_remaining_ens(cudaStream_t, int64_t, const k_commit_remaining_args*, const int64_t*, int);
+void launch_k_swept_update_ens(cudaStream_t, int64_t, const k_swept_update_args*, const int64_t*, int);
+void launch_k_commit_ids_ens(cudaStream_t, int64_t, const k_commit_ids_args*, const int64_t*, int);
 void launch_reset_counters_ens(cudaStream_t, const CounterResetArgs*, int);
 void launch_riemann_ens(cudaStream_t, const RiemannEnsArgs*, int, int64_t*, double*, int, int, int, int64_t*,
                         unsigned long long*, int, size_t);
@@ -958,6 +958,22 @@ static int ens_grid(const m2cg_ensemble* e, F count, int block) {
   return (int)mx;
 }
 
+// Exclusive prefix of the members' block counts for a batched launch; returns
+// the device table (built on the first pass) and the total in *total.
+template <class F>
+static int64_t* ens_boff(m2cg_ensemble* e, F count, int block, int64_t* total) {
+  const int D = (int)e->m.size();
+  std::vector<int64_t> b(D + 1);
+  int64_t t = 0;
+  for (int d = 0; d < D; d++) {
+    b[d] = t;
+    t += (count(e->m[d]) + block - 1) / block;
+  }
+  b[D] = t;
+  *total = t;
+  return e->table(b);
+}
+
 // One batched time step (CFL dt per member, MaxTime clamp), enqueued on e->stream.
 static m2cg_status ens_enqueue_step(m2cg_ensemble* e, int64_t* nl) {
   const int D = (int)e->m.size();
@@ -982,10 +998,10 @@ static m2cg_status ens_enqueue_step(m2cg_ensemble* e, int64_t* nl) {
     ENS_TABLE(k_dt_finalize_args, f);
     ENS_TABLE(CounterResetArgs, r);
     ENS_TABLE(k_compact_interfaces_args, c);
-    if (!e->building) launch_k_dt_reduce_ens(s, ens_grid(e, ens_cells, 256), v_d, D);
-    if (!e->building) launch_k_dt_finalize_ens(s, 1, f_d, D);
+    { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_cells, 256, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_dt_reduce_ens(s, nb_, v_d, bo_, D); }
+    { int64_t nb_; int64_t* bo_ = ens_boff(e, [](const m2cg_ctx*) { return (int64_t)1; }, 1, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_dt_finalize_ens(s, nb_, f_d, bo_, D); }
     if (!e->building) launch_reset_counters_ens(s, r_d, D);
-    if (!e->building) launch_k_compact_interfaces_ens(s, ens_grid(e, ens_faces, 256), c_d, D);
+    { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_faces, 256, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_compact_interfaces_ens(s, nb_, c_d, bo_, D); }
     n += 4;
   }
   const m2cg_ctx* x0 = e->m[0];
@@ -1017,8 +1033,8 @@ static m2cg_status ens_enqueue_step(m2cg_ensemble* e, int64_t* nl) {
     ENS_TABLE(k_bc_args, bc);
     const bool after_recon = (x0->P.mp_recon != M2CG_MPREC_CONSTANT);
     auto recon = [&]() {
-      if (!e->building) launch_k_reconstruct_ens(s, ens_grid(e, ens_cells, 128), rc_d, D);
-      if (!e->building) launch_k_reconstruct_ghosts_ens(s, ens_grid(e, ens_ghosts, 128), rg_d, D);
+      { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_cells, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_reconstruct_ens(s, nb_, rc_d, bo_, D); }
+      { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_ghosts, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_reconstruct_ghosts_ens(s, nb_, rg_d, bo_, D); }
       n += 2;
     };
     if (after_recon) recon();
@@ -1026,10 +1042,10 @@ static m2cg_status ens_enqueue_step(m2cg_ensemble* e, int64_t* nl) {
                        e->strag_count, e->sblocks, e->sreserve);
     n += 3;
     if (!after_recon) recon();
-    if (!e->building) launch_k_face_flux_ens(s, ens_grid(e, ens_faces, 128), ff_d, D);
-    if (!e->building) launch_k_update_ens(s, ens_grid(e, ens_cells, 128), up_d, D);
+    { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_faces, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_face_flux_ens(s, nb_, ff_d, bo_, D); }
+    { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_cells, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_update_ens(s, nb_, up_d, bo_, D); }
     n += 2;
-    if (!last) { if (!e->building) launch_k_bc_ens(s, ens_grid(e, ens_ghosts, 128), bc_d, D); n++; }
+    if (!last) { { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_ghosts, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_bc_ens(s, nb_, bc_d, bo_, D); } n++; }
   }
   {
     std::vector<k_bc_args> bc(D);
@@ -1060,15 +1076,15 @@ static m2cg_status ens_enqueue_step(m2cg_ensemble* e, int64_t* nl) {
       ENS_TABLE(k_commit_ids_args, ci);
       const int passes = 3;
       for (int p = 0; p < passes; p++) {
-        if (!e->building) launch_k_resolve_remaining_ens(s, blocks, p == passes - 1 ? r1_d : r0_d, D);
-        if (!e->building) launch_k_commit_remaining_ens(s, blocks, cr_d, D);
+        { int64_t nb_; int64_t* bo_ = ens_boff(e, [&](const m2cg_ctx*) { return (int64_t)blocks; }, 1, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_resolve_remaining_ens(s, nb_, p == passes - 1 ? r1_d : r0_d, bo_, D); }
+        { int64_t nb_; int64_t* bo_ = ens_boff(e, [&](const m2cg_ctx*) { return (int64_t)blocks; }, 1, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_commit_remaining_ens(s, nb_, cr_d, bo_, D); }
       }
-      if (!e->building) launch_k_swept_update_ens(s, blocks, su_d, D);
-      if (!e->building) launch_k_commit_ids_ens(s, blocks, ci_d, D);
+      { int64_t nb_; int64_t* bo_ = ens_boff(e, [&](const m2cg_ctx*) { return (int64_t)blocks; }, 1, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_swept_update_ens(s, nb_, su_d, bo_, D); }
+      { int64_t nb_; int64_t* bo_ = ens_boff(e, [&](const m2cg_ctx*) { return (int64_t)blocks; }, 1, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_commit_ids_ens(s, nb_, ci_d, bo_, D); }
       n += 2 * passes + 2;
     }
     ENS_TABLE(k_bc_args, bc);
-    if (!e->building) launch_k_bc_ens(s, ens_grid(e, ens_ghosts, 128), bc_d, D);
+    { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_ghosts, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_bc_ens(s, nb_, bc_d, bo_, D); }
     n++;
   }
 #undef ENS_TABLE

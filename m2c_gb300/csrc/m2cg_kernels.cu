@@ -10,6 +10,18 @@
 
 namespace m2cg {
 
+// Member owning flat block b of a batched launch: largest d with boff[d] <= b.
+__device__ __forceinline__ int ens_member(const int64_t* __restrict__ boff, int D, int64_t b) {
+  int lo = 0, hi = D - 1;
+  while (lo < hi) {
+    int mid = (lo + hi + 1) >> 1;
+    if (boff[mid] <= b) lo = mid;
+    else hi = mid - 1;
+  }
+  return lo;
+}
+
+
 __device__ __forceinline__ void atomic_inc(unsigned long long* c, unsigned long long v = 1ull) {
   atomicAdd(c, v);
 }
@@ -30,9 +42,9 @@ __device__ __forceinline__ bool real_cell(const Grid& g, int64_t t, int& i, int&
 // K1: MUSCL reconstruction of the six face states of every real cell
 // (Reconstructor.cpp:426-782) followed by CheckReconstructedStates
 // (SpaceOperator.cpp:2446-2484).  fs[f*5+p]: f = vl, vr, vb, vt, vk, vf.
-__device__ __forceinline__ void k_reconstruct_body(const Params& P, const StateSet& S, const int32_t* __restrict__ id, double* const* fs, unsigned long long* cnt) {
+__device__ __forceinline__ void k_reconstruct_body(const Params& P, const StateSet& S, const int32_t* __restrict__ id, double* const* fs, unsigned long long* cnt, unsigned bx_, unsigned gx_) {
   int i, j, k;
-  if (!real_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
+  if (!real_cell(P.g, (int64_t)bx_ * blockDim.x + threadIdx.x, i, j, k)) return;
   const Grid& g = P.g;
   int64_t c = g.at(i, j, k);
   double q[5];
@@ -96,11 +108,13 @@ __device__ __forceinline__ void k_reconstruct_body(const Params& P, const StateS
     for (int p = 0; p < 5; p++) fs[f * 5 + p][c] = face[f][p];
 }
 __global__ void __launch_bounds__(128) k_reconstruct(Params P, StateSet S, const int32_t* __restrict__ id,
-                                                     double* const* fs, unsigned long long* cnt) { k_reconstruct_body(P, S, id, fs, cnt); }
-// batched: block row blockIdx.y runs member domain blockIdx.y
-__global__ void __launch_bounds__(128) k_reconstruct_ens(const k_reconstruct_args* __restrict__ ea) {
-  const k_reconstruct_args& e = ea[blockIdx.y];
-  k_reconstruct_body(e.P, e.S, e.id, e.fs, e.cnt);
+                                                     double* const* fs, unsigned long long* cnt) { k_reconstruct_body(P, S, id, fs, cnt, blockIdx.x, gridDim.x); }
+// batched: the launch's blocks are the members' blocks back to back
+// (boff: exclusive prefix of the members' block counts)
+__global__ void __launch_bounds__(128) k_reconstruct_ens(const k_reconstruct_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
+  const int d = ens_member(boff, D, blockIdx.x);
+  const k_reconstruct_args& e = ea[d];
+  k_reconstruct_body(e.P, e.S, e.id, e.fs, e.cnt, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
 }
 
 
@@ -137,9 +151,9 @@ __device__ __forceinline__ bool ghost_face_cell(const Grid& g, int64_t t, int& s
 // K1b: face states of the face-ghost cells by boundary condition
 // (Reconstructor.cpp:807-889), then the boundary branch of
 // CheckReconstructedStates (SpaceOperator.cpp:2486-2535).
-__device__ __forceinline__ void k_reconstruct_ghosts_body(const Params& P, const StateSet& S, const int32_t* __restrict__ id, double* const* fs, unsigned long long* cnt) {
+__device__ __forceinline__ void k_reconstruct_ghosts_body(const Params& P, const StateSet& S, const int32_t* __restrict__ id, double* const* fs, unsigned long long* cnt, unsigned bx_, unsigned gx_) {
   int side, i, j, k, ii, jj, kk;
-  if (!ghost_face_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, side, i, j, k, ii, jj, kk)) return;
+  if (!ghost_face_cell(P.g, (int64_t)bx_ * blockDim.x + threadIdx.x, side, i, j, k, ii, jj, kk)) return;
   const Grid& g = P.g;
   int64_t c = g.at(i, j, k), im = g.at(ii, jj, kk);
   int inward = side ^ 1, src = side;
@@ -166,11 +180,13 @@ __device__ __forceinline__ void k_reconstruct_ghosts_body(const Params& P, const
   for (int p = 0; p < 5; p++) fs[inward * 5 + p][c] = t[p];
 }
 __global__ void k_reconstruct_ghosts(Params P, StateSet S, const int32_t* __restrict__ id, double* const* fs,
-                                     unsigned long long* cnt) { k_reconstruct_ghosts_body(P, S, id, fs, cnt); }
-// batched: block row blockIdx.y runs member domain blockIdx.y
-__global__ void k_reconstruct_ghosts_ens(const k_reconstruct_ghosts_args* __restrict__ ea) {
-  const k_reconstruct_ghosts_args& e = ea[blockIdx.y];
-  k_reconstruct_ghosts_body(e.P, e.S, e.id, e.fs, e.cnt);
+                                     unsigned long long* cnt) { k_reconstruct_ghosts_body(P, S, id, fs, cnt, blockIdx.x, gridDim.x); }
+// batched: the launch's blocks are the members' blocks back to back
+// (boff: exclusive prefix of the members' block counts)
+__global__ void k_reconstruct_ghosts_ens(const k_reconstruct_ghosts_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
+  const int d = ens_member(boff, D, blockIdx.x);
+  const k_reconstruct_ghosts_args& e = ea[d];
+  k_reconstruct_ghosts_body(e.P, e.S, e.id, e.fs, e.cnt, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
 }
 
 
@@ -184,9 +200,9 @@ __device__ __forceinline__ bool num_flux(const Params& P, int dir, const double*
 // ---------------------------------------------------------------------------
 // K2: numerical flux of every same-material face (SpaceOperator.cpp:1692-1701,
 // 1852-1861, 2011-2020).  The thread of cell c owns the faces at its minus side.
-__device__ __forceinline__ void k_face_flux_body(const Params& P, const int32_t* __restrict__ id, double* const* fs, double* const* F, unsigned long long* cnt) {
+__device__ __forceinline__ void k_face_flux_body(const Params& P, const int32_t* __restrict__ id, double* const* fs, double* const* F, unsigned long long* cnt, unsigned bx_, unsigned gx_) {
   const Grid& g = P.g;
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t t = (int64_t)bx_ * blockDim.x + threadIdx.x;
   int64_t ex = g.nx + 1, ey = g.ny + 1;
   int64_t n = ex * ey * (g.nz + 1);
   if (t >= n) return;
@@ -213,11 +229,13 @@ __device__ __forceinline__ void k_face_flux_body(const Params& P, const int32_t*
   if (bad) atomic_inc(&cnt[CNT_BAD], bad);
 }
 __global__ void __launch_bounds__(128) k_face_flux(Params P, const int32_t* __restrict__ id, double* const* fs, double* const* F,
-                            unsigned long long* cnt) { k_face_flux_body(P, id, fs, F, cnt); }
-// batched: block row blockIdx.y runs member domain blockIdx.y
-__global__ void __launch_bounds__(128) k_face_flux_ens(const k_face_flux_args* __restrict__ ea) {
-  const k_face_flux_args& e = ea[blockIdx.y];
-  k_face_flux_body(e.P, e.id, e.fs, e.F, e.cnt);
+                            unsigned long long* cnt) { k_face_flux_body(P, id, fs, F, cnt, blockIdx.x, gridDim.x); }
+// batched: the launch's blocks are the members' blocks back to back
+// (boff: exclusive prefix of the members' block counts)
+__global__ void __launch_bounds__(128) k_face_flux_ens(const k_face_flux_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
+  const int d = ens_member(boff, D, blockIdx.x);
+  const k_face_flux_args& e = ea[d];
+  k_face_flux_body(e.P, e.id, e.fs, e.F, e.cnt, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
 }
 
 
@@ -265,9 +283,9 @@ __device__ __forceinline__ double ls_residual(const Params& P, const double* __r
 // (TimeIntegrator.cpp:355-369, 409-417, 565-579, 617-631, 667-676), the
 // level-set stage update and, on the final stage, the sign-change detection of
 // MultiPhaseOperator::UpdateMaterialIDByLevelSet (MultiPhaseOperator.cpp:177-222).
-__device__ __forceinline__ void k_update_body(const Params& P, const StageArgs& A, const int32_t* __restrict__ id, int32_t* __restrict__ id_new, double* const* F, const IfaceList& L, const DevScalars* __restrict__ sc, int64_t* __restrict__ swept, unsigned long long* swept_count, int64_t swept_cap, unsigned long long* cnt) {
+__device__ __forceinline__ void k_update_body(const Params& P, const StageArgs& A, const int32_t* __restrict__ id, int32_t* __restrict__ id_new, double* const* F, const IfaceList& L, const DevScalars* __restrict__ sc, int64_t* __restrict__ swept, unsigned long long* swept_count, int64_t swept_cap, unsigned long long* cnt, unsigned bx_, unsigned gx_) {
   int i, j, k;
-  if (!real_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
+  if (!real_cell(P.g, (int64_t)bx_ * blockDim.x + threadIdx.x, i, j, k)) return;
   if (!sc->active && !A.residual_only) return;
   const Grid& g = P.g;
   int64_t c = g.at(i, j, k);
@@ -372,11 +390,13 @@ __device__ __forceinline__ void k_update_body(const Params& P, const StageArgs& 
 __global__ void k_update(Params P, StageArgs A, const int32_t* __restrict__ id, int32_t* __restrict__ id_new,
                          double* const* F, IfaceList L, const DevScalars* __restrict__ sc,
                          int64_t* __restrict__ swept, unsigned long long* swept_count, int64_t swept_cap,
-                         unsigned long long* cnt) { k_update_body(P, A, id, id_new, F, L, sc, swept, swept_count, swept_cap, cnt); }
-// batched: block row blockIdx.y runs member domain blockIdx.y
-__global__ void k_update_ens(const k_update_args* __restrict__ ea) {
-  const k_update_args& e = ea[blockIdx.y];
-  k_update_body(e.P, e.A, e.id, e.id_new, e.F, e.L, e.sc, e.swept, e.swept_count, e.swept_cap, e.cnt);
+                         unsigned long long* cnt) { k_update_body(P, A, id, id_new, F, L, sc, swept, swept_count, swept_cap, cnt, blockIdx.x, gridDim.x); }
+// batched: the launch's blocks are the members' blocks back to back
+// (boff: exclusive prefix of the members' block counts)
+__global__ void k_update_ens(const k_update_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
+  const int d = ens_member(boff, D, blockIdx.x);
+  const k_update_args& e = ea[d];
+  k_update_body(e.P, e.A, e.id, e.id_new, e.F, e.L, e.sc, e.swept, e.swept_count, e.swept_cap, e.cnt, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
 }
 
 
@@ -392,9 +412,9 @@ __global__ void k_ls_residual(Params P, StateSet S, double* __restrict__ out) {
 // ---------------------------------------------------------------------------
 // Boundary conditions on the face-ghost cells: SpaceOperator.cpp:738-821 (V),
 // LevelSetOperator.cpp:408-508 (phi), MultiPhaseOperator.cpp:919-942 (ID).
-__device__ __forceinline__ void k_bc_body(const Params& P, const StateSet& S, int do_v, int do_phi, int32_t* id, const DevScalars* sc) {
+__device__ __forceinline__ void k_bc_body(const Params& P, const StateSet& S, int do_v, int do_phi, int32_t* id, const DevScalars* sc, unsigned bx_, unsigned gx_) {
   int side, i, j, k, ii, jj, kk;
-  if (!ghost_face_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, side, i, j, k, ii, jj, kk)) return;
+  if (!ghost_face_cell(P.g, (int64_t)bx_ * blockDim.x + threadIdx.x, side, i, j, k, ii, jj, kk)) return;
   if (sc && !sc->active) return;
   const Grid& g = P.g;
   int64_t c = g.at(i, j, k), im = g.at(ii, jj, kk);
@@ -439,11 +459,13 @@ __device__ __forceinline__ void k_bc_body(const Params& P, const StateSet& S, in
   }
   if (id) id[c] = id[im];
 }
-__global__ void k_bc(Params P, StateSet S, int do_v, int do_phi, int32_t* id, const DevScalars* sc) { k_bc_body(P, S, do_v, do_phi, id, sc); }
-// batched: block row blockIdx.y runs member domain blockIdx.y
-__global__ void k_bc_ens(const k_bc_args* __restrict__ ea) {
-  const k_bc_args& e = ea[blockIdx.y];
-  k_bc_body(e.P, e.S, e.do_v, e.do_phi, e.id, e.sc);
+__global__ void k_bc(Params P, StateSet S, int do_v, int do_phi, int32_t* id, const DevScalars* sc) { k_bc_body(P, S, do_v, do_phi, id, sc, blockIdx.x, gridDim.x); }
+// batched: the launch's blocks are the members' blocks back to back
+// (boff: exclusive prefix of the members' block counts)
+__global__ void k_bc_ens(const k_bc_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
+  const int d = ens_member(boff, D, blockIdx.x);
+  const k_bc_args& e = ea[d];
+  k_bc_body(e.P, e.S, e.do_v, e.do_phi, e.id, e.sc, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
 }
 
 
@@ -451,10 +473,10 @@ __global__ void k_bc_ens(const k_bc_args* __restrict__ ea) {
 // CFL time step: FindExtremeValuesOfFlowVariables + ComputeTimeStepSize
 // (SpaceOperator.cpp:1223-1330).  Warp-shuffle min, then one atomicMin per block
 // on the bit pattern of the positive minimum.
-__device__ __forceinline__ void k_dt_reduce_body(const Params& P, const StateSet& S, const int32_t* __restrict__ id, DevScalars* sc) {
+__device__ __forceinline__ void k_dt_reduce_body(const Params& P, const StateSet& S, const int32_t* __restrict__ id, DevScalars* sc, unsigned bx_, unsigned gx_) {
   int i, j, k;
   double m = DBL_MAX;
-  if (real_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) {
+  if (real_cell(P.g, (int64_t)bx_ * blockDim.x + threadIdx.x, i, j, k)) {
     const Grid& g = P.g;
     int64_t c = g.at(i, j, k);
     const DevMat& M = P.mats.m[id[c]];
@@ -480,17 +502,19 @@ __device__ __forceinline__ void k_dt_reduce_body(const Params& P, const StateSet
     if (lane == 0 && m < DBL_MAX) atomicMin(&sc->min_dx_over_lambda, (unsigned long long)__double_as_longlong(m));
   }
 }
-__global__ void k_dt_reduce(Params P, StateSet S, const int32_t* __restrict__ id, DevScalars* sc) { k_dt_reduce_body(P, S, id, sc); }
-// batched: block row blockIdx.y runs member domain blockIdx.y
-__global__ void k_dt_reduce_ens(const k_dt_reduce_args* __restrict__ ea) {
-  const k_dt_reduce_args& e = ea[blockIdx.y];
-  k_dt_reduce_body(e.P, e.S, e.id, e.sc);
+__global__ void k_dt_reduce(Params P, StateSet S, const int32_t* __restrict__ id, DevScalars* sc) { k_dt_reduce_body(P, S, id, sc, blockIdx.x, gridDim.x); }
+// batched: the launch's blocks are the members' blocks back to back
+// (boff: exclusive prefix of the members' block counts)
+__global__ void k_dt_reduce_ens(const k_dt_reduce_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
+  const int d = ens_member(boff, D, blockIdx.x);
+  const k_dt_reduce_args& e = ea[d];
+  k_dt_reduce_body(e.P, e.S, e.id, e.sc, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
 }
 
 
 // dt, cfl and the MaxTime clamp of Main.cpp:653-681, kept on the device.
 // mode 0: query (dt and cfl only); 1: CFL-driven step; 2: step with a given dt.
-__device__ __forceinline__ void k_dt_finalize_body(const Params& P, DevScalars* sc, int mode, double fixed_dt) {
+__device__ __forceinline__ void k_dt_finalize_body(const Params& P, DevScalars* sc, int mode, double fixed_dt, unsigned bx_, unsigned gx_) {
   double m = __longlong_as_double((long long)sc->min_dx_over_lambda);
   sc->min_dx_over_lambda = 0x7fefffffffffffffull;  // DBL_MAX for the next reduction
   double dt, cfl;
@@ -509,11 +533,13 @@ __device__ __forceinline__ void k_dt_finalize_body(const Params& P, DevScalars* 
   sc->time = t + dt;
   sc->steps += 1;
 }
-__global__ void k_dt_finalize(Params P, DevScalars* sc, int mode, double fixed_dt) { k_dt_finalize_body(P, sc, mode, fixed_dt); }
-// batched: block row blockIdx.y runs member domain blockIdx.y
-__global__ void k_dt_finalize_ens(const k_dt_finalize_args* __restrict__ ea) {
-  const k_dt_finalize_args& e = ea[blockIdx.y];
-  k_dt_finalize_body(e.P, e.sc, e.mode, e.fixed_dt);
+__global__ void k_dt_finalize(Params P, DevScalars* sc, int mode, double fixed_dt) { k_dt_finalize_body(P, sc, mode, fixed_dt, blockIdx.x, gridDim.x); }
+// batched: the launch's blocks are the members' blocks back to back
+// (boff: exclusive prefix of the members' block counts)
+__global__ void k_dt_finalize_ens(const k_dt_finalize_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
+  const int d = ens_member(boff, D, blockIdx.x);
+  const k_dt_finalize_args& e = ea[d];
+  k_dt_finalize_body(e.P, e.sc, e.mode, e.fixed_dt, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
 }
 
 
@@ -523,11 +549,11 @@ __global__ void k_dt_finalize_ens(const k_dt_finalize_args* __restrict__ ea) {
 // level-set material (MultiPhaseOperator.cpp:236-340).  Jacobi passes: each
 // pass decides from the previous pass's IDs; the reference resolves in
 // lexicographic order within a pass.
-__device__ __forceinline__ void k_resolve_remaining_body(const Params& P, int32_t* id_new, const int64_t* swept, const unsigned long long* count, int64_t cap, int32_t* cand_out, int final_pass, const DevScalars* sc) {
+__device__ __forceinline__ void k_resolve_remaining_body(const Params& P, int32_t* id_new, const int64_t* swept, const unsigned long long* count, int64_t cap, int32_t* cand_out, int final_pass, const DevScalars* sc, unsigned bx_, unsigned gx_) {
   if (!sc->active) return;
   int64_t n = (int64_t)min((unsigned long long)cap, *count);
   const Grid& g = P.g;
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t s = (int64_t)bx_ * blockDim.x + threadIdx.x; s < n; s += (int64_t)gx_ * blockDim.x) {
     int64_t c = swept[s];
     int cur = id_new[c];
     if (cur >= 0) { cand_out[s] = cur; continue; }
@@ -549,38 +575,42 @@ __device__ __forceinline__ void k_resolve_remaining_body(const Params& P, int32_
   }
 }
 __global__ void k_resolve_remaining(Params P, int32_t* id_new, const int64_t* swept, const unsigned long long* count,
-                                    int64_t cap, int32_t* cand_out, int final_pass, const DevScalars* sc) { k_resolve_remaining_body(P, id_new, swept, count, cap, cand_out, final_pass, sc); }
-// batched: block row blockIdx.y runs member domain blockIdx.y
-__global__ void k_resolve_remaining_ens(const k_resolve_remaining_args* __restrict__ ea) {
-  const k_resolve_remaining_args& e = ea[blockIdx.y];
-  k_resolve_remaining_body(e.P, e.id_new, e.swept, e.count, e.cap, e.cand_out, e.final_pass, e.sc);
+                                    int64_t cap, int32_t* cand_out, int final_pass, const DevScalars* sc) { k_resolve_remaining_body(P, id_new, swept, count, cap, cand_out, final_pass, sc, blockIdx.x, gridDim.x); }
+// batched: the launch's blocks are the members' blocks back to back
+// (boff: exclusive prefix of the members' block counts)
+__global__ void k_resolve_remaining_ens(const k_resolve_remaining_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
+  const int d = ens_member(boff, D, blockIdx.x);
+  const k_resolve_remaining_args& e = ea[d];
+  k_resolve_remaining_body(e.P, e.id_new, e.swept, e.count, e.cap, e.cand_out, e.final_pass, e.sc, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
 }
 
 
-__device__ __forceinline__ void k_commit_remaining_body(int32_t* id_new, const int64_t* swept, const unsigned long long* count, int64_t cap, const int32_t* cand, const DevScalars* sc) {
+__device__ __forceinline__ void k_commit_remaining_body(int32_t* id_new, const int64_t* swept, const unsigned long long* count, int64_t cap, const int32_t* cand, const DevScalars* sc, unsigned bx_, unsigned gx_) {
   if (!sc->active) return;
   int64_t n = (int64_t)min((unsigned long long)cap, *count);
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x)
+  for (int64_t s = (int64_t)bx_ * blockDim.x + threadIdx.x; s < n; s += (int64_t)gx_ * blockDim.x)
     id_new[swept[s]] = cand[s];
 }
 __global__ void k_commit_remaining(int32_t* id_new, const int64_t* swept, const unsigned long long* count, int64_t cap,
-                                   const int32_t* cand, const DevScalars* sc) { k_commit_remaining_body(id_new, swept, count, cap, cand, sc); }
-// batched: block row blockIdx.y runs member domain blockIdx.y
-__global__ void k_commit_remaining_ens(const k_commit_remaining_args* __restrict__ ea) {
-  const k_commit_remaining_args& e = ea[blockIdx.y];
-  k_commit_remaining_body(e.id_new, e.swept, e.count, e.cap, e.cand, e.sc);
+                                   const int32_t* cand, const DevScalars* sc) { k_commit_remaining_body(id_new, swept, count, cap, cand, sc, blockIdx.x, gridDim.x); }
+// batched: the launch's blocks are the members' blocks back to back
+// (boff: exclusive prefix of the members' block counts)
+__global__ void k_commit_remaining_ens(const k_commit_remaining_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
+  const int d = ens_member(boff, D, blockIdx.x);
+  const k_commit_remaining_args& e = ea[d];
+  k_commit_remaining_body(e.id_new, e.swept, e.count, e.cap, e.cand, e.sc, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
 }
 
 
 // UpdateStateVariablesByRiemannSolutions / LocalUpdateByRiemannSolutions
 // (MultiPhaseOperator.cpp:980-1150) or by extrapolation (1155-1274) for every
 // swept cell whose ID changed; then ClipDensityAndPressure (TimeIntegrator.cpp:800).
-__device__ __forceinline__ void k_swept_update_body(const Params& P, const StateSet& S, const int32_t* __restrict__ id_old, const int32_t* __restrict__ id_new, const IfaceList& L, const int64_t* swept, const unsigned long long* count, int64_t cap, unsigned long long* cnt, const DevScalars* sc) {
+__device__ __forceinline__ void k_swept_update_body(const Params& P, const StateSet& S, const int32_t* __restrict__ id_old, const int32_t* __restrict__ id_new, const IfaceList& L, const int64_t* swept, const unsigned long long* count, int64_t cap, unsigned long long* cnt, const DevScalars* sc, unsigned bx_, unsigned gx_) {
   if (!sc->active) return;
   int64_t n = (int64_t)min((unsigned long long)cap, *count);
   const Grid& g = P.g;
   const int64_t st[3] = {1, g.sy, g.sz};
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x) {
+  for (int64_t s = (int64_t)bx_ * blockDim.x + threadIdx.x; s < n; s += (int64_t)gx_ * blockDim.x) {
     int64_t c = swept[s];
     int myid = id_new[c];
     if (myid == id_old[c]) continue;
@@ -659,36 +689,40 @@ __device__ __forceinline__ void k_swept_update_body(const Params& P, const State
 }
 __global__ void k_swept_update(Params P, StateSet S, const int32_t* __restrict__ id_old, const int32_t* __restrict__ id_new,
                                IfaceList L, const int64_t* swept, const unsigned long long* count, int64_t cap,
-                               unsigned long long* cnt, const DevScalars* sc) { k_swept_update_body(P, S, id_old, id_new, L, swept, count, cap, cnt, sc); }
-// batched: block row blockIdx.y runs member domain blockIdx.y
-__global__ void k_swept_update_ens(const k_swept_update_args* __restrict__ ea) {
-  const k_swept_update_args& e = ea[blockIdx.y];
-  k_swept_update_body(e.P, e.S, e.id_old, e.id_new, e.L, e.swept, e.count, e.cap, e.cnt, e.sc);
+                               unsigned long long* cnt, const DevScalars* sc) { k_swept_update_body(P, S, id_old, id_new, L, swept, count, cap, cnt, sc, blockIdx.x, gridDim.x); }
+// batched: the launch's blocks are the members' blocks back to back
+// (boff: exclusive prefix of the members' block counts)
+__global__ void k_swept_update_ens(const k_swept_update_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
+  const int d = ens_member(boff, D, blockIdx.x);
+  const k_swept_update_args& e = ea[d];
+  k_swept_update_body(e.P, e.S, e.id_old, e.id_new, e.L, e.swept, e.count, e.cap, e.cnt, e.sc, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
 }
 
 
-__device__ __forceinline__ void k_commit_ids_body(int32_t* id, const int32_t* id_new, const int64_t* swept, const unsigned long long* count, int64_t cap, const DevScalars* sc) {
+__device__ __forceinline__ void k_commit_ids_body(int32_t* id, const int32_t* id_new, const int64_t* swept, const unsigned long long* count, int64_t cap, const DevScalars* sc, unsigned bx_, unsigned gx_) {
   if (!sc->active) return;
   int64_t n = (int64_t)min((unsigned long long)cap, *count);
-  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < n; s += (int64_t)gridDim.x * blockDim.x)
+  for (int64_t s = (int64_t)bx_ * blockDim.x + threadIdx.x; s < n; s += (int64_t)gx_ * blockDim.x)
     id[swept[s]] = id_new[swept[s]];
 }
 __global__ void k_commit_ids(int32_t* id, const int32_t* id_new, const int64_t* swept, const unsigned long long* count,
-                             int64_t cap, const DevScalars* sc) { k_commit_ids_body(id, id_new, swept, count, cap, sc); }
-// batched: block row blockIdx.y runs member domain blockIdx.y
-__global__ void k_commit_ids_ens(const k_commit_ids_args* __restrict__ ea) {
-  const k_commit_ids_args& e = ea[blockIdx.y];
-  k_commit_ids_body(e.id, e.id_new, e.swept, e.count, e.cap, e.sc);
+                             int64_t cap, const DevScalars* sc) { k_commit_ids_body(id, id_new, swept, count, cap, sc, blockIdx.x, gridDim.x); }
+// batched: the launch's blocks are the members' blocks back to back
+// (boff: exclusive prefix of the members' block counts)
+__global__ void k_commit_ids_ens(const k_commit_ids_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
+  const int d = ens_member(boff, D, blockIdx.x);
+  const k_commit_ids_args& e = ea[d];
+  k_commit_ids_body(e.id, e.id_new, e.swept, e.count, e.cap, e.sc, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
 }
 
 
 // ---------------------------------------------------------------------------
 // Interface-face compaction: every face whose two cells carry different IDs
 // (SpaceOperator.cpp:1613, 1772, 1931) gets a slot in the work list.
-__device__ __forceinline__ void k_compact_interfaces_body(const Params& P, const int32_t* __restrict__ id, const IfaceList& L, unsigned long long* cnt, const DevScalars* sc) {
+__device__ __forceinline__ void k_compact_interfaces_body(const Params& P, const int32_t* __restrict__ id, const IfaceList& L, unsigned long long* cnt, const DevScalars* sc, unsigned bx_, unsigned gx_) {
   if (sc && !sc->active) return;
   const Grid& g = P.g;
-  int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
+  int64_t t = (int64_t)bx_ * blockDim.x + threadIdx.x;
   int64_t ex = g.nx + 1, ey = g.ny + 1;
   int64_t n = ex * ey * (g.nz + 1);
   bool valid = t < n;
@@ -727,11 +761,13 @@ __device__ __forceinline__ void k_compact_interfaces_body(const Params& P, const
   }
 }
 __global__ void k_compact_interfaces(Params P, const int32_t* __restrict__ id, IfaceList L, unsigned long long* cnt,
-                                     const DevScalars* sc) { k_compact_interfaces_body(P, id, L, cnt, sc); }
-// batched: block row blockIdx.y runs member domain blockIdx.y
-__global__ void k_compact_interfaces_ens(const k_compact_interfaces_args* __restrict__ ea) {
-  const k_compact_interfaces_args& e = ea[blockIdx.y];
-  k_compact_interfaces_body(e.P, e.id, e.L, e.cnt, e.sc);
+                                     const DevScalars* sc) { k_compact_interfaces_body(P, id, L, cnt, sc, blockIdx.x, gridDim.x); }
+// batched: the launch's blocks are the members' blocks back to back
+// (boff: exclusive prefix of the members' block counts)
+__global__ void k_compact_interfaces_ens(const k_compact_interfaces_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
+  const int d = ens_member(boff, D, blockIdx.x);
+  const k_compact_interfaces_args& e = ea[d];
+  k_compact_interfaces_body(e.P, e.id, e.L, e.cnt, e.sc, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
 }
 
 
@@ -854,14 +890,14 @@ void launch_pack(cudaStream_t s, const Params& P, const StateSet& S, const int32
   k_pack<<<nblk(n, 256), 256, 0, s>>>(P, S, id, Vh, idh, phih, R, Rh, rphi, rphih);
 }
 
-// ---- batched launchers: grid (gx, D), block row d = member d --------------------
+// ---- batched launchers: the members' blocks back to back ---------------------------
 __global__ void k_reset_counters_ens(const CounterResetArgs* __restrict__ ea) {
   const CounterResetArgs& e = ea[blockIdx.y];
   if (threadIdx.x == 0) { *e.a = 0; *e.b = 0; }
 }
 #define M2CG_ENS_LAUNCHER(K, B)                                                                        \
-  void launch_##K##_ens(cudaStream_t s, int gx, const K##_args* t, int D) {                           \
-    if (gx > 0 && D > 0) K##_ens<<<dim3((unsigned)gx, (unsigned)D), B, 0, s>>>(t);                    \
+  void launch_##K##_ens(cudaStream_t s, int64_t blocks, const K##_args* t, const int64_t* boff, int D) { \
+    if (blocks > 0 && D > 0) K##_ens<<<(unsigned)blocks, B, 0, s>>>(t, boff, D);                       \
   }
 M2CG_ENS_LAUNCHER(k_reconstruct, 128)
 M2CG_ENS_LAUNCHER(k_reconstruct_ghosts, 128)

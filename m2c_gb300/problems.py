@@ -168,3 +168,64 @@ def bubble_collapse_ensemble(n_domains=512, seed=4096, edges=EDGES):
         pw = 10.0 ** rng.uniform(6.0, 8.0)
         out.append(bubble_collapse(nx, ny, nz, rf, pw))
     return out
+
+
+def nasg_post_shock(rho1, p1, p2, gamma, pinf, b):
+    """Post-shock density and velocity behind a right-moving shock of pressure
+    p2 into still Noble-Abel stiffened gas (q = 0) at (rho1, p1).  With
+    e = (p + gamma pinf)(v - b) / (gamma - 1), v = 1/rho, the Hugoniot
+    e2 - e1 + (p1 + p2)(v2 - v1) / 2 = 0 is linear in v2; u2 = sqrt((p2 - p1)(v1 - v2))."""
+    v1 = 1.0 / rho1
+    g1 = gamma - 1.0
+    a = (p2 + gamma * pinf) / g1 + 0.5 * (p2 + p1)
+    rhs = (p1 + gamma * pinf) * (v1 - b) / g1 + b * (p2 + gamma * pinf) / g1 + 0.5 * (p2 + p1) * v1
+    v2 = rhs / a
+    return 1.0 / v2, float(np.sqrt((p2 - p1) * (v1 - v2)))
+
+
+def bubble_cluster_shock(n=512, seed=512, n_bubbles=8, p_shock=5.0e8):
+    """Large production-shaped run: n^3 cells on [0,1]^3, n_bubbles gas bubbles
+    (SG 1.4, rho 1.2, p 1e5) with seeded centres in [0.35,0.8] x [0.25,0.75]^2 and
+    radii uniform in [0.04, 0.1], in NASG water (gamma 1.19, pinf 6.2e8,
+    b 6.61e-4, rho 1000, p 1e5); water for x < 0.1 carries the post-shock state
+    of a p_shock shock (Hugoniot above).  phi = min_i(|x - c_i| - r_i).  MUSCL /
+    van Albada, HLLC, exact interface Riemann at 1e-10, RK3, CFL 0.4; Inlet at
+    x0 (post-shock state), Outlet at xmax, Symmetry on y and z."""
+    rng = np.random.Generator(np.random.PCG64(seed))
+    ctr = np.column_stack([rng.uniform(0.35, 0.8, n_bubbles), rng.uniform(0.25, 0.75, n_bubbles),
+                           rng.uniform(0.25, 0.75, n_bubbles)])
+    rad = rng.uniform(0.04, 0.1, n_bubbles)
+    c = abi.default_config()
+    c.nx = c.ny = c.nz = n
+    c.x0, c.xmax, c.y0, c.ymax, c.z0, c.zmax = 0.0, 1.0, 0.0, 1.0, 0.0, 1.0
+    c.n_materials = 2
+    abi.set_material(c.mat[0], abi.EOS_NASG, gamma=1.19, pc=6.2e8, b=6.61e-4, q=0.0)
+    abi.set_material(c.mat[1], abi.EOS_SG, gamma=1.4, pc=0.0)
+    rho_s, u_s = nasg_post_shock(1000.0, 1.0e5, p_shock, 1.19, 6.2e8, 6.61e-4)
+    c.bc[0] = abi.BC_INLET
+    c.bc[1] = abi.BC_OUTLET
+    for s in range(2, 6):
+        c.bc[s] = abi.BC_SYMMETRY
+    for p, v in enumerate((rho_s, u_s, 0.0, 0.0, p_shock)):
+        c.inlet[p] = v
+    c.flux = abi.FLUX_HLLC
+    c.rec_type = abi.REC_LINEAR
+    c.limiter = abi.LIM_VANALBADA
+    c.tol_main = 1e-10
+    c.n_levelsets, c.ls_matid = 1, 1
+    c.ts_type = abi.TS_RK3
+    c.cfl = 0.4
+    h = 1.0 / n
+    x = 0.5 * h + np.arange(n) * h
+    phi = np.full((n, n, n), np.inf)
+    for (cx, cy, cz), r in zip(ctr, rad):
+        d = np.sqrt((x[None, None, :] - cx) ** 2 + (x[None, :, None] - cy) ** 2 + (x[:, None, None] - cz) ** 2) - r
+        np.minimum(phi, d, out=phi)
+    phi = phi.ravel()
+    gas = phi < 0
+    shocked = np.broadcast_to(x[None, None, :] < 0.1, (n, n, n)).ravel() & ~gas
+    V = np.zeros((n * n * n, 5))
+    V[:, 0] = np.where(gas, 1.2, np.where(shocked, rho_s, 1000.0))
+    V[:, 1] = np.where(shocked, u_s, 0.0)
+    V[:, 4] = np.where(gas, 1.0e5, np.where(shocked, p_shock, 1.0e5))
+    return c, V, gas.astype(np.int32), phi

@@ -51,6 +51,18 @@ def sample_problems(n, seed):
     return np.ascontiguousarray(W[:n]), np.ascontiguousarray(E[:n])
 
 
+def acoustic_estimate(W, E):
+    """Acoustic-theory star pressure (ExactRiemannSolverBase.cpp:1107-1116) and
+    the acoustic pressure jump relative to the impedance-weighted pressure."""
+    rl, ul, pl, rr, ur, pr = (W[:, i] for i in range(6))
+    c2l = E[:, 1] * (pl + E[:, 2]) / (rl * (1.0 - E[:, 3] * rl))
+    c2r = E[:, 6] * (pr + E[:, 7]) / (rr * (1.0 - E[:, 8] * rr))
+    Cl, Cr = rl * np.sqrt(c2l), rr * np.sqrt(c2r)
+    pbar = (Cr * pl + Cl * pr) / (Cl + Cr)
+    p0 = pbar + Cl * Cr * (ul - ur) / (Cl + Cr)
+    return p0, np.abs(p0 - pbar) / np.abs(pbar)
+
+
 def solver_config(tol=1e-10):
     c = abi.default_config()
     c.nx = c.ny = c.nz = 1
@@ -197,6 +209,10 @@ def study(n_train=1 << 22, n_test=1 << 22, epochs=60, batch=16384, lr=3e-3, seed
     warm = solver.solve(Wte, Ete, warm_p=pred)
     ok = (cold["err"] == 0) & (cold["pstar"] > 0)
     rel = np.abs(pred[ok] - cold["pstar"][ok]) / cold["pstar"][ok]
+    # the method without the network: the acoustic estimate the reference starts from
+    p_ac, jump = acoustic_estimate(Wte, Ete)
+    rel_ac = np.abs(p_ac[ok] - cold["pstar"][ok]) / cold["pstar"][ok]
+    strong = jump[ok] > 0.05
     both = (cold["err"] == 0) & (warm["err"] == 0)
     dp = np.abs(warm["pstar"][both] - cold["pstar"][both]) / np.maximum(np.abs(cold["pstar"][both]), 1e-300)
     # device time on the problems both starts solve: the whole-set time is set
@@ -212,6 +228,11 @@ def study(n_train=1 << 22, n_test=1 << 22, epochs=60, batch=16384, lr=3e-3, seed
         "loss_first_epoch": float(loss[0]), "loss_last_epoch": float(loss[-1]), "train_s": train_ms / 1e3,
         "pstar_rel_err_median": float(np.median(rel)), "pstar_rel_err_p90": float(np.percentile(rel, 90)),
         "pstar_rel_err_p99": float(np.percentile(rel, 99)),
+        "acoustic_rel_err_median": float(np.median(rel_ac)),
+        # problems whose acoustic pressure jump exceeds 5 % of p_ref, where the solver uses the network
+        "strong_fraction": float(strong.mean()),
+        "pstar_rel_err_median_strong": float(np.median(rel[strong])) if strong.any() else 0.0,
+        "acoustic_rel_err_median_strong": float(np.median(rel_ac[strong])) if strong.any() else 0.0,
         "iters_cold_mean": float(cold["iters"].mean()), "iters_warm_mean": float(warm["iters"].mean()),
         "iters_ratio": float(cold["iters"].mean() / max(warm["iters"].mean(), 1e-30)),
         # problems both starts solve (failures run to MaxIts twice either way)
