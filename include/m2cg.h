@@ -120,7 +120,12 @@ typedef struct {
   double max_time;             /* MaxTime */
   /* Learned warm start for the interface Riemann solve (no reference counterpart) */
   int32_t warm_start;          /* 0 = cold start (reference), 1 = MLP warm start */
-  int32_t pad3_;
+  /* LevelSet[0].Reinitialization (IoData.cpp:1421-1429): full domain, first layer FIXED */
+  int32_t reinit_frequency;    /* Frequency: every that many steps (<= 0: never, the default) */
+  int32_t reinit_max_its;      /* MaxIts (30) */
+  int32_t pad4_;
+  double reinit_cfl;           /* CFL (0.8) */
+  double reinit_tol;           /* ConvergenceTolerance (2e-4) */
 } m2cg_config;
 
 /* Per-step counters (the reference prints these as warnings; SpaceOperator.cpp:681-683,
@@ -191,6 +196,27 @@ m2cg_status m2cg_advance(m2cg_ctx* ctx, double dt);
 m2cg_status m2cg_run(m2cg_ctx* ctx, int32_t n_steps, m2cg_counters* counters);
 
 m2cg_status m2cg_get_counters(m2cg_ctx* ctx, m2cg_counters* counters);
+
+/* Level-set reinitialization statistics of a context (summed over its calls). */
+typedef struct {
+  int64_t calls;               /* reinitializations that found an interface and ran */
+  int64_t iterations;          /* pseudo-time RK3 iterations, summed over attempts */
+  int64_t retries;             /* restarts with CFL / 1.5 (LevelSetReinitializer.cpp:157-174) */
+  int64_t failures;            /* gave up below CFL 0.02 (the reference stops the program) */
+  int64_t loop_bodies;         /* executions of the device loop body */
+  double cfl;                  /* current pseudo-time CFL (kept reduced after a retry) */
+  double last_residual;        /* max |grad phi| - 1 of the last iteration's first sub-stage */
+  double last_change;          /* largest relative change of the last completed iteration */
+} m2cg_reinit_stats;
+
+/* LevelSetOperator::Reinitialize with must_do (LevelSetOperator.cpp:1338-1361):
+ * one full-domain reinitialization of the level set now, first layer FIXED
+ * (LevelSetReinitializer.cpp:76-176), with the context's MaxIts / CFL /
+ * ConvergenceTolerance.  The stepping (m2cg_run, m2cg_advance) calls the same
+ * after every reinit_frequency-th step (TimeIntegrator.cpp:756-768).  stats
+ * (optional) receives the context's totals. */
+m2cg_status m2cg_reinitialize(m2cg_ctx* ctx, m2cg_reinit_stats* stats);
+m2cg_status m2cg_get_reinit_stats(m2cg_ctx* ctx, m2cg_reinit_stats* stats);
 
 /* Conserved totals sum(U * vol) over real cells: mass, momentum x/y/z, energy. */
 m2cg_status m2cg_conserved_totals(m2cg_ctx* ctx, double totals[5]);

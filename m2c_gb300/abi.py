@@ -62,7 +62,8 @@ class Config(C.Structure):
                 ("n_levelsets", C.c_int32), ("ls_matid", C.c_int32), ("ls_bc", C.c_int32 * 6),
                 ("ts_type", C.c_int32), ("max_its", C.c_int32),
                 ("cfl", C.c_double), ("timestep", C.c_double), ("max_time", C.c_double),
-                ("warm_start", C.c_int32), ("pad3_", C.c_int32)]
+                ("warm_start", C.c_int32), ("reinit_frequency", C.c_int32), ("reinit_max_its", C.c_int32),
+                ("pad4_", C.c_int32), ("reinit_cfl", C.c_double), ("reinit_tol", C.c_double)]
 
 
 class Counters(C.Structure):
@@ -72,6 +73,15 @@ class Counters(C.Structure):
                 ("swept_cells", C.c_int64), ("unresolved_cells", C.c_int64), ("steps", C.c_int64),
                 ("time", C.c_double), ("dt", C.c_double), ("cfl", C.c_double),
                 ("riemann_fallbacks", C.c_int64), ("path_capped", C.c_int64)]
+
+    def as_dict(self):
+        return {name: getattr(self, name) for name, _ in self._fields_}
+
+
+class ReinitStats(C.Structure):
+    _fields_ = [("calls", C.c_int64), ("iterations", C.c_int64), ("retries", C.c_int64), ("failures", C.c_int64),
+                ("loop_bodies", C.c_int64), ("cfl", C.c_double), ("last_residual", C.c_double),
+                ("last_change", C.c_double)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -111,6 +121,7 @@ def default_config():
     c.timestep = -1.0
     c.max_time = 1e10
     c.warm_start = 0
+    c.reinit_frequency, c.reinit_max_its, c.reinit_cfl, c.reinit_tol = -1, 30, 0.8, 2.0e-4
     return c
 
 
@@ -173,6 +184,8 @@ def load(path=None):
         "m2cg_advance": (C.c_int, [_P, C.c_double]),
         "m2cg_run": (C.c_int, [_P, C.c_int32, C.POINTER(Counters)]),
         "m2cg_get_counters": (C.c_int, [_P, C.POINTER(Counters)]),
+        "m2cg_reinitialize": (C.c_int, [_P, C.POINTER(ReinitStats)]),
+        "m2cg_get_reinit_stats": (C.c_int, [_P, C.POINTER(ReinitStats)]),
         "m2cg_conserved_totals": (C.c_int, [_P, _D]),
         "m2cg_riemann_batch": (C.c_int, [_P, C.c_int64, _D, _I, _D, _I, _D, _D, _I, _D, _D, _I, _I]),
         "m2cg_flux_batch": (C.c_int, [_P, C.c_int64, _I, _D, _D, _I, _D]),

@@ -16,6 +16,7 @@ OUT = os.path.join(HERE, "lib")
 BUILD = os.path.join(HERE, "_build")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler", "-O2",
+          "-Xcompiler", "-Werror=return-type",
           "-I", os.path.join(HERE, "..", "include")]
 UNITS = {
     "m2cg_kernels.cu": [],
@@ -23,6 +24,7 @@ UNITS = {
     "m2cg_api.cu": [],
     "m2cg_noalloc.cu": ["-fmad=false"],
     "m2cg_mlp.cu": [],
+    "m2cg_reinit.cu": ["-fmad=false"],
 }
 
 

@@ -20,6 +20,7 @@ void launch_update(cudaStream_t, const Params&, const StageArgs&, const int32_t*
                    const IfaceList&, const DevScalars*, int64_t*, unsigned long long*, int64_t, unsigned long long*);
 void launch_ls_residual(cudaStream_t, const Params&, const StateSet&, double*);
 void launch_bc(cudaStream_t, const Params&, const StateSet&, int, int, int32_t*, const DevScalars*);
+cudaError_t reinit_build_graph(cudaStream_t, const ReinitArgs&, int, int, cudaGraphExec_t*);
 void launch_dt(cudaStream_t, const Params&, const StateSet&, const int32_t*, DevScalars*, int, double);
 void launch_compact(cudaStream_t, const Params&, const int32_t*, const IfaceList&, unsigned long long*,
                     const DevScalars*);
@@ -141,6 +142,12 @@ struct m2cg_ctx {
   int64_t launches = 0;
   int64_t launches_per_step = 0;
   cudaGraphExec_t graph_exec = nullptr;
+  // level-set reinitialization: sub-stage states, backup, sign, first-layer
+  // tags, device loop state and the two loop graphs (gated on the step
+  // number for the stepping, ungated for m2cg_reinitialize)
+  ReinitArgs ri = {};
+  cudaGraphExec_t ri_gated = nullptr, ri_now = nullptr;
+  long long ri_bodies_seen = 0;
   // batch buffers
   std::vector<void*> batch;
   int64_t batch_n = 0;
@@ -446,6 +453,61 @@ m2cg_status m2cg_config_default(m2cg_config* c) {
   c->ts_type = M2CG_TS_RK2; c->max_its = 0x7fffffff;
   c->cfl = 0.5; c->timestep = -1.0; c->max_time = 1e10;
   c->warm_start = 0;
+  c->reinit_frequency = -1;  // IoData.cpp:1423-1428
+  c->reinit_max_its = 30;
+  c->reinit_cfl = 0.8;
+  c->reinit_tol = 2.0e-4;
+  return M2CG_OK;
+}
+
+// Buffers and loop graphs of the level-set reinitialization (allocated once).
+static m2cg_status reinit_prepare(m2cg_ctx* x) {
+  if (x->ri_now) return M2CG_OK;
+  if (x->P.n_ls == 0) { set_err("no level set configured"); return M2CG_ERR_INVALID_ARG; }
+  if (x->cfg.reinit_cfl <= 0.0 || !(x->cfg.reinit_tol >= 0.0)) {
+    set_err("reinitialization CFL must be positive and the tolerance non-negative");
+    return M2CG_ERR_INVALID_ARG;
+  }
+  ReinitArgs& a = x->ri;
+  const Grid& g = x->P.g;
+  a.g = g;
+  for (int s = 0; s < 6; s++) a.ls_bc[s] = x->P.ls_bc[s];
+  a.lo[0] = x->cfg.x0; a.lo[1] = x->cfg.y0; a.lo[2] = x->cfg.z0;
+  a.rh[0] = 1.0 / g.dx; a.rh[1] = 1.0 / g.dy; a.rh[2] = 1.0 / g.dz;
+  a.hmin = std::min(g.dx, std::min(g.dy, g.dz));
+  a.tol = x->cfg.reinit_tol;
+  a.max_its = x->cfg.reinit_max_its;
+  a.freq = x->cfg.reinit_frequency;
+  a.phi = x->S[0].q[5];
+  CK(x->alloc(&a.phi1, (size_t)g.ntot));
+  CK(x->alloc(&a.phi2, (size_t)g.ntot));
+  CK(x->alloc(&a.bk, (size_t)g.ntot));
+  CK(x->alloc(&a.sign, (size_t)g.ntot));
+  CK(x->alloc(&a.tag, (size_t)g.ntot));
+  CK(x->alloc(&a.st, 1));
+  a.sc = x->sc;
+  CK(cudaMemsetAsync(a.phi1, 0, g.ntot * sizeof(double), x->stream));
+  CK(cudaMemsetAsync(a.phi2, 0, g.ntot * sizeof(double), x->stream));
+  CK(cudaMemsetAsync(a.tag, 0, g.ntot, x->stream));
+  ReinitState h;
+  memset(&h, 0, sizeof(h));
+  h.cfl = x->cfg.reinit_cfl;
+  CK(cudaMemcpyAsync(a.st, &h, sizeof(h), cudaMemcpyHostToDevice, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  CK(reinit_build_graph(x->stream, a, x->nsm, 1, &x->ri_gated));
+  CK(reinit_build_graph(x->stream, a, x->nsm, 0, &x->ri_now));
+  return M2CG_OK;
+}
+
+// Kernel launches of the reinitialization graphs since the last call: gate +
+// preparation per graph launch, seven per loop body.
+static m2cg_status reinit_account(m2cg_ctx* x, int64_t graph_launches) {
+  if (!x->ri.st) return M2CG_OK;
+  ReinitState h;
+  CK(cudaMemcpyAsync(&h, x->ri.st, sizeof(h), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  x->launches += 2 * graph_launches + 7 * (h.bodies - x->ri_bodies_seen);
+  x->ri_bodies_seen = h.bodies;
   return M2CG_OK;
 }
 
@@ -474,6 +536,7 @@ static m2cg_status create_ctx(const m2cg_config* cfg, double* ext_scratch, m2cg_
     return M2CG_ERR_CUDA;
   }
   st = ctx_alloc(x);
+  if (st == M2CG_OK && x->P.n_ls > 0 && cfg->reinit_frequency > 0) st = reinit_prepare(x);
   if (st != M2CG_OK) { m2cg_destroy(x); return st; }
   *out = x;
   return M2CG_OK;
@@ -485,6 +548,8 @@ void m2cg_destroy(m2cg_ctx* x) {
   if (!x) return;
   if (x->stream) cudaStreamSynchronize(x->stream);
   if (x->graph_exec) cudaGraphExecDestroy(x->graph_exec);
+  if (x->ri_gated) cudaGraphExecDestroy(x->ri_gated);
+  if (x->ri_now) cudaGraphExecDestroy(x->ri_now);
   for (void* p : x->allocs) cudaFree(p);
   for (void* p : x->batch) cudaFree(p);
   if (x->batch_scratch) cudaFree(x->batch_scratch);
@@ -614,9 +679,45 @@ m2cg_status m2cg_levelset_residual(m2cg_ctx* x, double* Rphi) {
 m2cg_status m2cg_advance(m2cg_ctx* x, double dt) {
   if (!x || !(dt > 0)) { set_err("bad argument"); return M2CG_ERR_INVALID_ARG; }
   x->launches += enqueue_step(x, 2, dt);
+  int64_t ri = 0;
+  if (x->ri_gated) {   // the graph's gate checks the step number on the device
+    CK(cudaGraphLaunch(x->ri_gated, x->stream));
+    ri = 1;
+  }
   CK(cudaStreamSynchronize(x->stream));
   CK(cudaGetLastError());
+  return reinit_account(x, ri);
+}
+
+m2cg_status m2cg_get_reinit_stats(m2cg_ctx* x, m2cg_reinit_stats* out) {
+  if (!x || !out) { set_err("null argument"); return M2CG_ERR_INVALID_ARG; }
+  memset(out, 0, sizeof(*out));
+  out->cfl = x->cfg.reinit_cfl;
+  if (!x->ri.st) return M2CG_OK;
+  ReinitState h;
+  CK(cudaMemcpyAsync(&h, x->ri.st, sizeof(h), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  out->calls = h.calls;
+  out->iterations = h.iterations;
+  out->retries = h.retries;
+  out->failures = h.failures;
+  out->loop_bodies = h.bodies;
+  out->cfl = h.cfl;
+  out->last_residual = h.last_res;
+  out->last_change = h.last_dphi;
   return M2CG_OK;
+}
+
+m2cg_status m2cg_reinitialize(m2cg_ctx* x, m2cg_reinit_stats* stats) {
+  if (!x) { set_err("null context"); return M2CG_ERR_INVALID_ARG; }
+  m2cg_status st = reinit_prepare(x);
+  if (st != M2CG_OK) return st;
+  CK(cudaGraphLaunch(x->ri_now, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  CK(cudaGetLastError());
+  st = reinit_account(x, 1);
+  if (st != M2CG_OK) return st;
+  return stats ? m2cg_get_reinit_stats(x, stats) : M2CG_OK;
 }
 
 m2cg_status m2cg_get_counters(m2cg_ctx* x, m2cg_counters* c) {
@@ -680,12 +781,27 @@ m2cg_status m2cg_run(m2cg_ctx* x, int32_t n_steps, m2cg_counters* counters) {
     CK(cudaGraphInstantiate(&x->graph_exec, g, cudaGraphInstantiateFlagUseNodePriority));
     cudaGraphDestroy(g);
   }
+  // reinitialization after every reinit_frequency-th step: the host picks the
+  // steps from the device's step count at entry; the graph's gate re-checks
+  // it on the device (a step past MaxTime is not taken and not counted)
+  long long step0 = 0;
+  const int freq = x->ri_gated ? x->cfg.reinit_frequency : 0;
+  if (freq > 0) {
+    CK(cudaMemcpyAsync(&step0, &x->sc->steps, sizeof(step0), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  int64_t ri = 0;
   for (int i = 0; i < n_steps; i++) {
     CK(cudaGraphLaunch(x->graph_exec, s));
     x->launches += x->launches_per_step;
+    if (freq > 0 && (step0 + i + 1) % freq == 0) {
+      CK(cudaGraphLaunch(x->ri_gated, s));
+      ri++;
+    }
   }
   CK(cudaStreamSynchronize(s));
   CK(cudaGetLastError());
+  if (ri) { m2cg_status st = reinit_account(x, ri); if (st != M2CG_OK) return st; }
   if (counters) return m2cg_get_counters(x, counters);
   return M2CG_OK;
 }
@@ -1032,16 +1148,17 @@ static m2cg_status ens_enqueue_step(m2cg_ensemble* e, int64_t* nl) {
     ENS_TABLE(k_update_args, up);
     ENS_TABLE(k_bc_args, bc);
     const bool after_recon = (x0->P.mp_recon != M2CG_MPREC_CONSTANT);
-    auto recon = [&]() {
+    auto recon = [&]() -> m2cg_status {
       { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_cells, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_reconstruct_ens(s, nb_, rc_d, bo_, D); }
       { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_ghosts, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_reconstruct_ghosts_ens(s, nb_, rg_d, bo_, D); }
       n += 2;
+      return M2CG_OK;
     };
-    if (after_recon) recon();
+    if (after_recon) { m2cg_status st = recon(); if (st != M2CG_OK) return st; }
     if (!e->building) launch_riemann_ens(s, ra_d, D, e->off, e->scratch, e->path_cap, e->rblocks, e->eval_limit, e->strag,
                        e->strag_count, e->sblocks, e->sreserve);
     n += 3;
-    if (!after_recon) recon();
+    if (!after_recon) { m2cg_status st = recon(); if (st != M2CG_OK) return st; }
     { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_faces, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_face_flux_ens(s, nb_, ff_d, bo_, D); }
     { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_cells, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_update_ens(s, nb_, up_d, bo_, D); }
     n += 2;
@@ -1123,6 +1240,12 @@ m2cg_status m2cg_ensemble_create(const m2cg_config* cfgs, int32_t n, m2cg_ensemb
   if (cfgs[0].ts_type == M2CG_TS_FORWARD_EULER) {
     set_err("the batched step supports the RK2 and RK3 integrators");
     return M2CG_ERR_INVALID_ARG;
+  }
+  for (int d = 0; d < n; d++) {
+    if (cfgs[d].n_levelsets > 0 && cfgs[d].reinit_frequency > 0) {
+      set_err("member %d: the batched step does not reinitialize level sets (reinit_frequency must be <= 0)", d);
+      return M2CG_ERR_INVALID_ARG;
+    }
   }
   int ndev = 0;
   if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) { set_err("no CUDA device"); return M2CG_ERR_NO_DEVICE; }

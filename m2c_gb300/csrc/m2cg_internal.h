@@ -18,6 +18,36 @@ struct Grid {
   M2CG_DEV int64_t at(int i, int j, int k) const { return ((int64_t)(k + 1) * py + (j + 1)) * px + (i + 1); }
 };
 
+// Face-ghost cells: position and image (SpaceOperator.cpp:493-519).
+M2CG_DEV bool ghost_face_cell(const Grid& g, int64_t t, int& side, int& i, int& j, int& k,
+                                                int& ii, int& jj, int& kk) {
+  int64_t nyz = (int64_t)g.ny * g.nz, nxz = (int64_t)g.nx * g.nz, nxy = (int64_t)g.nx * g.ny;
+  if (t < 2 * nyz) {
+    side = (int)(t / nyz); int64_t r = t % nyz;
+    k = (int)(r / g.ny); j = (int)(r % g.ny);
+    i = side == 0 ? -1 : g.nx;
+    ii = side == 0 ? 0 : g.nx - 1; jj = j; kk = k;
+    return true;
+  }
+  t -= 2 * nyz;
+  if (t < 2 * nxz) {
+    side = 2 + (int)(t / nxz); int64_t r = t % nxz;
+    k = (int)(r / g.nx); i = (int)(r % g.nx);
+    j = side == 2 ? -1 : g.ny;
+    jj = side == 2 ? 0 : g.ny - 1; ii = i; kk = k;
+    return true;
+  }
+  t -= 2 * nxz;
+  if (t < 2 * nxy) {
+    side = 4 + (int)(t / nxy); int64_t r = t % nxy;
+    j = (int)(r / g.nx); i = (int)(r % g.nx);
+    k = side == 4 ? -1 : g.nz;
+    kk = side == 4 ? 0 : g.nz - 1; ii = i; jj = j;
+    return true;
+  }
+  return false;
+}
+
 // Device counter slots (int64).
 enum {
   CNT_IFACE = 0, CNT_RERR, CNT_RITER, CNT_RSOLVE, CNT_CLIPCELL, CNT_CLIPFACE, CNT_BAD, CNT_SWEPT, CNT_UNRES,
@@ -69,6 +99,42 @@ struct IfaceList {
   int32_t* slot[3];    // per-cell slot of the face at the cell's minus side in each direction
   unsigned long long* count;
   int64_t cap;
+};
+
+// Level-set reinitialization (full domain, first layer held fixed): device
+// state of the pseudo-time loop, written by the one-thread control kernel
+// between the sub-stage launches and read by every launch of the loop body.
+struct ReinitState {
+  unsigned long long res_bits;   // max |grad phi| - 1 over untagged cells (first sub-stage), as bits
+  unsigned long long dphi_bits;  // max relative change of the iteration, as bits
+  unsigned int detected;         // an interior first-layer node exists
+  int run;                       // the loop is running
+  int restore;                   // the next first sub-stage restarts from the backup
+  int iter;                      // iteration of the current attempt
+  int body_runs;                 // loop-body executions of the current call (bounded)
+  int pad;
+  double cfl;                    // pseudo-time CFL; reduced by 1.5 per retry and kept
+  long long calls, iterations, retries, failures, bodies;
+  double last_res, last_dphi;
+};
+
+struct ReinitArgs {
+  Grid g;
+  int ls_bc[6];
+  double lo[3];        // domain origin: cell centres at lo + 0.5 h + i h
+  double rh[3];        // 1/dx, 1/dy, 1/dz
+  double hmin;         // min(dx, dy, dz)
+  double tol;
+  int max_its;
+  int freq;            // gate: every freq-th completed step (<= 0: no gate)
+  double* phi;         // the level set (ghosted), updated in place
+  double* phi1;        // sub-stage states
+  double* phi2;
+  double* bk;          // backup for a retry
+  double* sign;        // smoothed sign of the input
+  uint8_t* tag;        // first-layer nodes (held fixed)
+  ReinitState* st;
+  const DevScalars* sc;
 };
 
 struct StageArgs {

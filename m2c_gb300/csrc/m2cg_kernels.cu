@@ -118,35 +118,6 @@ __global__ void __launch_bounds__(128) k_reconstruct_ens(const k_reconstruct_arg
 }
 
 
-// Face-ghost cells: position and image (SpaceOperator.cpp:493-519).
-__device__ __forceinline__ bool ghost_face_cell(const Grid& g, int64_t t, int& side, int& i, int& j, int& k,
-                                                int& ii, int& jj, int& kk) {
-  int64_t nyz = (int64_t)g.ny * g.nz, nxz = (int64_t)g.nx * g.nz, nxy = (int64_t)g.nx * g.ny;
-  if (t < 2 * nyz) {
-    side = (int)(t / nyz); int64_t r = t % nyz;
-    k = (int)(r / g.ny); j = (int)(r % g.ny);
-    i = side == 0 ? -1 : g.nx;
-    ii = side == 0 ? 0 : g.nx - 1; jj = j; kk = k;
-    return true;
-  }
-  t -= 2 * nyz;
-  if (t < 2 * nxz) {
-    side = 2 + (int)(t / nxz); int64_t r = t % nxz;
-    k = (int)(r / g.nx); i = (int)(r % g.nx);
-    j = side == 2 ? -1 : g.ny;
-    jj = side == 2 ? 0 : g.ny - 1; ii = i; kk = k;
-    return true;
-  }
-  t -= 2 * nxz;
-  if (t < 2 * nxy) {
-    side = 4 + (int)(t / nxy); int64_t r = t % nxy;
-    j = (int)(r / g.nx); i = (int)(r % g.nx);
-    k = side == 4 ? -1 : g.nz;
-    kk = side == 4 ? 0 : g.nz - 1; ii = i; jj = j;
-    return true;
-  }
-  return false;
-}
 
 // K1b: face states of the face-ghost cells by boundary condition
 // (Reconstructor.cpp:807-889), then the boundary branch of

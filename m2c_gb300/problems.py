@@ -189,8 +189,10 @@ def bubble_cluster_shock(n=512, seed=512, n_bubbles=8, p_shock=5.0e8):
     radii uniform in [0.04, 0.1], in NASG water (gamma 1.19, pinf 6.2e8,
     b 6.61e-4, rho 1000, p 1e5); water for x < 0.1 carries the post-shock state
     of a p_shock shock (Hugoniot above).  phi = min_i(|x - c_i| - r_i).  MUSCL /
-    van Albada, HLLC, exact interface Riemann at 1e-10, RK3, CFL 0.4; Inlet at
-    x0 (post-shock state), Outlet at xmax, Symmetry on y and z."""
+    van Albada, HLLC, exact interface Riemann at 1e-10, RK3, CFL 0.4, level set
+    reinitialized every 10 steps (full domain, first layer fixed, MaxIts 30,
+    CFL 0.8, tolerance 2e-4); Inlet at x0 (post-shock state), Outlet at xmax,
+    Symmetry on y and z."""
     rng = np.random.Generator(np.random.PCG64(seed))
     ctr = np.column_stack([rng.uniform(0.35, 0.8, n_bubbles), rng.uniform(0.25, 0.75, n_bubbles),
                            rng.uniform(0.25, 0.75, n_bubbles)])
@@ -215,6 +217,7 @@ def bubble_cluster_shock(n=512, seed=512, n_bubbles=8, p_shock=5.0e8):
     c.n_levelsets, c.ls_matid = 1, 1
     c.ts_type = abi.TS_RK3
     c.cfl = 0.4
+    c.reinit_frequency = 10
     h = 1.0 / n
     x = 0.5 * h + np.arange(n) * h
     phi = np.full((n, n, n), np.inf)

@@ -94,6 +94,19 @@ class Solver:
         abi.check(self.lib, self.lib.m2cg_get_counters(self.ctx, C.byref(c)), "m2cg_get_counters")
         return c.as_dict()
 
+    def Reinitialize(self):
+        """LevelSetOperator::Reinitialize with must_do (LevelSetOperator.cpp:1338-1361):
+        one full-domain reinitialization now, first layer FIXED; returns the
+        context's reinitialization totals."""
+        st = abi.ReinitStats()
+        abi.check(self.lib, self.lib.m2cg_reinitialize(self.ctx, C.byref(st)), "m2cg_reinitialize")
+        return st.as_dict()
+
+    def reinit_stats(self):
+        st = abi.ReinitStats()
+        abi.check(self.lib, self.lib.m2cg_get_reinit_stats(self.ctx, C.byref(st)), "m2cg_get_reinit_stats")
+        return st.as_dict()
+
     def conserved_totals(self):
         t = np.zeros(5)
         abi.check(self.lib, self.lib.m2cg_conserved_totals(self.ctx, abi.dptr(t)), "m2cg_conserved_totals")

@@ -26,6 +26,7 @@ def _load_oracle():
         "orc_residual": (None, [_P, _D]),
         "orc_levelset_residual": (None, [_P, _D]),
         "orc_compute_dt": (None, [_P, _D, _D]),
+        "orc_reinitialize": (C.c_int, [_P, _D]),
         "orc_advance": (None, [_P, C.c_double]),
         "orc_run": (C.c_int, [_P, C.c_int]),
         "orc_counters": (None, [_P, C.POINTER(Counters)]),
@@ -99,6 +100,13 @@ class OracleSim:
         R = np.zeros(self.n)
         lib().orc_levelset_residual(self.h, dptr(R))
         return R
+
+    def reinitialize(self):
+        """One full-domain reinitialization; returns (found_interface, stats dict)."""
+        st = np.zeros(5)
+        r = lib().orc_reinitialize(self.h, dptr(st))
+        return bool(r), dict(calls=int(st[0]), iterations=int(st[1]), retries=int(st[2]), failures=int(st[3]),
+                             cfl=float(st[4]))
 
     def compute_dt(self):
         dt, cfl = C.c_double(), C.c_double()

@@ -14,7 +14,7 @@ def build():
     deps = [src] + [os.path.join(HERE, h) for h in ("oracle_eos_flux.h", "oracle_riemann.h")]
     if os.path.exists(lib) and os.path.getmtime(lib) > max(os.path.getmtime(d) for d in deps):
         return lib
-    cmd = ["g++", "-std=c++17", "-O2", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", lib + ".tmp", src]
+    cmd = ["g++", "-std=c++17", "-O2", "-Werror=return-type", "-ffp-contract=off", "-fopenmp", "-fPIC", "-shared", "-o", lib + ".tmp", src]
     r = subprocess.run(cmd, capture_output=True, text=True)
     if r.returncode != 0:
         raise RuntimeError(f"oracle build failed:\n{r.stderr[-4000:]}")

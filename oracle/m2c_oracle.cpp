@@ -84,6 +84,12 @@ struct Oracle {
   void P2C(const std::vector<double>& v, const std::vector<int>& id, std::vector<double>& u);
   void C2P(const std::vector<double>& u, const std::vector<int>& id, std::vector<double>& v);
   void EndOfStep(std::vector<double>& phi0);
+  // level-set reinitialization (full domain, first layer FIXED)
+  double reinit_cfl = 0.8;
+  int reinit_retries = 0, reinit_failures = 0, reinit_calls = 0, reinit_iters = 0;
+  bool Reinitialize();
+  double ReinitResidual(const std::vector<double>& phi, const std::vector<char>& tag, const std::vector<double>& sign,
+                        std::vector<double>& R, double cfl);
   bool NumFlux(int dir, const double* Vm, const double* Vp, int id, double* F);
 };
 
@@ -628,6 +634,125 @@ void Oracle::Advance(double dt) {
   cnt.steps++;
 }
 
+// LevelSetReinitializer.cpp:960-1041 (ComputeResidualFullDomain): first-order
+// Godunov upwind |grad phi| - 1 on the interior, R = -dt S (|grad phi| - 1)
+// with dt = cfl min(dx, dy, dz) (scaled back where |res| > 1), first-layer
+// nodes held (R = 0).  Returns the largest |res| over the other nodes.
+double Oracle::ReinitResidual(const std::vector<double>& phi, const std::vector<char>& tag,
+                              const std::vector<double>& sign, std::vector<double>& R, double cfl) {
+  const double xlo[3] = {cfg.x0, cfg.y0, cfg.z0}, h[3] = {dx, dy, dz};
+  auto coord = [&](int d, int i) { return xlo[d] + 0.5 * h[d] + i * h[d]; };  // MeshGenerator.cpp:166-171
+  double max_res = 0.0;
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < NX; i++) {
+        size_t c = idx(i, j, k);
+        if (tag[c]) { R[c] = 0.0; continue; }
+        double hmin = std::min(dx, std::min(dy, dz));
+        double dt = cfl * hmin;
+        double p = phi[c];
+        double a = (p - phi[idx(i - 1, j, k)]) / (coord(0, i) - coord(0, i - 1));
+        double b = (phi[idx(i + 1, j, k)] - p) / (coord(0, i + 1) - coord(0, i));
+        double cc = (p - phi[idx(i, j - 1, k)]) / (coord(1, j) - coord(1, j - 1));
+        double d = (phi[idx(i, j + 1, k)] - p) / (coord(1, j + 1) - coord(1, j));
+        double e = (p - phi[idx(i, j, k - 1)]) / (coord(2, k) - coord(2, k - 1));
+        double f = (phi[idx(i, j, k + 1)] - p) / (coord(2, k + 1) - coord(2, k));
+        double ap = std::max(a, 0.0), am = std::min(a, 0.0), bp = std::max(b, 0.0), bm = std::min(b, 0.0);
+        double cp = std::max(cc, 0.0), cm = std::min(cc, 0.0), dp = std::max(d, 0.0), dm = std::min(d, 0.0);
+        double ep = std::max(e, 0.0), em = std::min(e, 0.0), fp = std::max(f, 0.0), fm = std::min(f, 0.0);
+        double res;
+        if (p >= 0) res = std::sqrt(std::max(ap * ap, bm * bm) + std::max(cp * cp, dm * dm) + std::max(ep * ep, fm * fm)) - 1.0;
+        else res = std::sqrt(std::max(am * am, bp * bp) + std::max(cm * cm, dp * dp) + std::max(em * em, fp * fp)) - 1.0;
+        if (std::fabs(res) <= 1.0) R[c] = -dt * sign[c] * res;
+        else R[c] = -dt * sign[c] * res / std::fabs(res);
+        max_res = std::max(max_res, std::fabs(res));
+      }
+  return max_res;
+}
+
+// LevelSetReinitializer.cpp:76-176 (ReinitializeFullDomain) with the default
+// first-layer treatment FIXED (IoData.cpp:1428): tag the first layer
+// (:304-437), sign function with eps = 1 (:601-623), RK3 in pseudo time until
+// the residual or the largest relative change drops below the tolerance;
+// after MaxIts without it, accept if the change is below 0.02, else restart
+// from the input with CFL / 1.5 (the CFL stays reduced for later calls), and
+// give up below CFL 0.02 (the reference stops the program; counted here).
+bool Oracle::Reinitialize() {
+  std::vector<char> tag(N(), 0);
+  bool detected = false;
+  for (int k = -1; k <= NZ; k++)
+    for (int j = -1; j <= NY; j++)
+      for (int i = -1; i <= NX; i++) {
+        if (nface_ghost(i, j, k) > 1) continue;  // edge and corner ghosts are not populated
+        double p = Phi[idx(i, j, k)];
+        bool t = (i - 1 >= -1 && p * Phi[idx(i - 1, j, k)] <= 0) || (i + 1 <= NX && p * Phi[idx(i + 1, j, k)] <= 0) ||
+                 (j - 1 >= -1 && p * Phi[idx(i, j - 1, k)] <= 0) || (j + 1 <= NY && p * Phi[idx(i, j + 1, k)] <= 0) ||
+                 (k - 1 >= -1 && p * Phi[idx(i, j, k - 1)] <= 0) || (k + 1 <= NZ && p * Phi[idx(i, j, k + 1)] <= 0);
+        // neighbours that are edge ghosts are not populated either; a face ghost's neighbours along the
+        // face are edge ghosts, whose values the reference leaves untouched (zero here)
+        tag[idx(i, j, k)] = t;
+        if (t && !outside(i, j, k)) detected = true;
+      }
+  if (!detected) return false;
+  reinit_calls++;
+  std::vector<double> sign(N(), 0.0);
+  double factor = 1.0 * std::min(dx, std::min(dy, dz));
+  for (int k = -1; k <= NZ; k++)
+    for (int j = -1; j <= NY; j++)
+      for (int i = -1; i <= NX; i++) {
+        size_t c = idx(i, j, k);
+        sign[c] = Phi[c] / std::sqrt(Phi[c] * Phi[c] + factor * factor);
+      }
+  auto axpby = [&](std::vector<double>& x, double a, double b, const std::vector<double>& y) {
+    for (int k = 0; k < NZ; k++)
+      for (int j = 0; j < NY; j++)
+        for (int i = 0; i < NX; i++) {
+          size_t c = idx(i, j, k);
+          x[c] = a * x[c] + b * y[c];
+        }
+  };
+  std::vector<double> Phibk = Phi, Phi0(N(), 0.0), Phi1(N(), 0.0), R(N(), 0.0);
+  const int maxIts = cfg.reinit_max_its;
+  const double tol = cfg.reinit_tol;
+  while (true) {
+    double dphi_max = 0.0;
+    int iter;
+    for (iter = 0; iter < maxIts; iter++) {
+      axpby(Phi0, 0.0, 1.0, Phi);
+      double residual = ReinitResidual(Phi, tag, sign, R, reinit_cfl);
+      if (residual < tol) break;
+      axpby(Phi1, 0.0, 1.0, Phi);
+      axpby(Phi1, 1.0, 1.0, R);
+      ApplyLSBC(Phi1);
+      ReinitResidual(Phi1, tag, sign, R, reinit_cfl);
+      axpby(Phi1, 0.25, 0.75, Phi);
+      axpby(Phi1, 1.0, 0.25, R);
+      ApplyLSBC(Phi1);
+      ReinitResidual(Phi1, tag, sign, R, reinit_cfl);
+      axpby(Phi, 1.0 / 3.0, 2.0 / 3.0, Phi1);
+      axpby(Phi, 1.0, 2.0 / 3.0, R);
+      ApplyLSBC(Phi);
+      dphi_max = 0.0;  // CalculateMaximumRelativeErrorFullDomain (:1966-1991)
+      for (int k = 0; k < NZ; k++)
+        for (int j = 0; j < NY; j++)
+          for (int i = 0; i < NX; i++) {
+            size_t c = idx(i, j, k);
+            double e = std::fabs(Phi[c] - Phi0[c]);
+            if (Phi[c] != 0) e /= std::fabs(Phi[c]);
+            dphi_max = std::max(dphi_max, e);
+          }
+      if (dphi_max < tol) break;
+    }
+    reinit_iters += iter;
+    if (iter < maxIts) return true;
+    if (dphi_max < 0.02) return true;
+    if (reinit_cfl < 0.02) { reinit_failures++; return true; }
+    reinit_cfl /= 1.5;
+    reinit_retries++;
+    Phi = Phibk;
+  }
+}
+
 // TimeIntegrator.cpp:720-843 with MultiPhaseOperator.cpp:153-357, 947-1274.
 void Oracle::EndOfStep(std::vector<double>& phi0) {
   std::vector<int> IDn = ID;
@@ -679,6 +804,9 @@ void Oracle::EndOfStep(std::vector<double>& phi0) {
     }
   }
   UpdateIDGhosts(ID);
+  // level-set reinitialization at the user frequency (TimeIntegrator.cpp:756-768,
+  // LevelSetOperator.cpp:1338-1361, Utils.cpp:337-357 with frequency_dt unset)
+  if (cfg.reinit_frequency > 0 && time_step % cfg.reinit_frequency == 0) Reinitialize();
   // UpdateStateVariablesAfterInterfaceMotion
   std::vector<std::array<int, 3>> unresolved;
   std::vector<double> Vold = V;
@@ -776,6 +904,7 @@ extern "C" {
 void* orc_create(const m2cg_config* cfg) {
   Oracle* o = new Oracle();
   o->setup(*cfg);
+  o->reinit_cfl = cfg->reinit_cfl;
   return o;
 }
 void orc_destroy(void* h) { delete (Oracle*)h; }
@@ -843,6 +972,19 @@ void orc_levelset_residual(void* h, double* Rout) {
   for (int k = 0; k < o->NZ; k++)
     for (int j = 0; j < o->NY; j++)
       for (int i = 0; i < o->NX; i++, n++) Rout[n] = R[o->idx(i, j, k)];
+}
+
+// One full-domain reinitialization of the level set now (the call the
+// stepping makes every reinit_frequency steps); returns 1 if an interface was
+// found.  stats (optional): {calls, iterations, retries, failures, cfl}.
+int orc_reinitialize(void* h, double* stats) {
+  Oracle* o = (Oracle*)h;
+  int r = o->Reinitialize() ? 1 : 0;
+  if (stats) {
+    stats[0] = o->reinit_calls; stats[1] = o->reinit_iters; stats[2] = o->reinit_retries;
+    stats[3] = o->reinit_failures; stats[4] = o->reinit_cfl;
+  }
+  return r;
 }
 
 void orc_compute_dt(void* h, double* dt, double* cfl) {

@@ -1,0 +1,193 @@
+"""Level-set reinitialization (full domain, first layer FIXED;
+LevelSetReinitializer.cpp:76-176, 960-1041).
+
+The reference's reinitializer runs on PETSc distributed arrays and cannot be
+compiled here without PETSc, so the oracle's restatement is checked through
+the properties the method guarantees: a signed distance is (nearly) a fixed
+point, a field with the same zero set but the wrong slope is driven to
+|grad phi| = 1, first-layer nodes and every sign are kept, no interface means
+no work, and MaxIts without convergence takes the CFL / 1.5 retry.  The GPU
+path is then held to the oracle: the level set within 1e-10 of max|phi| and
+identical iteration / retry counts."""
+import numpy as np
+import pytest
+
+from helpers import rel_linf
+from m2c_gb300 import abi, problems
+from oracle import binding as ob
+
+
+def sphere_case(n=32, distort="smooth", **kw):
+    """Sphere of radius 0.15 (shock-bubble geometry) with the level set's zero
+    set kept and its slope changed: "smooth" between 0.2 and 1.8, "strong"
+    between about 0.2 and 3 with a jump across the interface (the relative
+    change stays above 0.02 and the CFL / 1.5 retries run), None for the
+    signed distance itself."""
+    c, V, ID, phi = problems.shock_bubble(n=n, **kw)
+    X, Y, Z = problems.cell_centers(c)
+    if distort == "smooth":
+        phi = phi * (1.0 + 0.8 * np.sin(3.0 * X + 2.0 * Y))
+    elif distort == "strong":
+        phi = phi * (1.0 + 2.0 * (X - 0.5) ** 2 + 0.5 * Y) * np.where(phi > 0, 2.5, 0.4)
+    return c, V, ID, phi
+
+
+def grad_norm(phi, c):
+    P = phi.reshape(c.nz, c.ny, c.nx)
+    h = 1.0 / c.nx
+    gz, gy, gx = np.gradient(P, h)
+    return np.sqrt(gx * gx + gy * gy + gz * gz).ravel()
+
+
+def first_layer(phi, c):
+    P = phi.reshape(c.nz, c.ny, c.nx)
+    t = np.zeros(P.shape, bool)
+    for ax in range(3):
+        for sh in (1, -1):
+            Q = np.roll(P, sh, axis=ax)
+            m = P * Q <= 0
+            idx = [slice(None)] * 3
+            idx[ax] = 0 if sh == 1 else -1   # wrapped neighbour: not a neighbour
+            m[tuple(idx)] = False
+            t |= m
+    return t.ravel()
+
+
+def oracle_reinit(c, V, ID, phi):
+    o = ob.OracleSim(c)
+    o.upload(V, ID, phi)
+    found, st = o.reinitialize()
+    return o, found, st, o.download()[2]
+
+
+def test_oracle_distance_is_nearly_fixed():
+    c, V, ID, phi = sphere_case(distort=None)
+    _, found, st, out = oracle_reinit(c, V, ID, phi)
+    h = 1.0 / c.nx
+    assert found and st["calls"] == 1 and st["retries"] == 0
+    # first-order upwind slopes of a sphere's distance are O(h / r) short of 1
+    # (r = 5 cells here), so the field steepens slightly away from the fixed layer
+    near = np.abs(phi) < 2 * h
+    assert np.abs(out - phi)[near].max() < 0.25 * h
+    assert np.abs(out - phi).max() < h
+
+
+def test_oracle_restores_unit_slope_and_keeps_first_layer_and_signs():
+    c, V, ID, phi = sphere_case()
+    _, found, st, out = oracle_reinit(c, V, ID, phi)
+    h = 1.0 / c.nx
+    fl = first_layer(phi, c)
+    assert found and st["failures"] == 0 and st["retries"] == 0
+    np.testing.assert_allclose(out[fl], phi[fl], rtol=1e-14, atol=0)
+    assert np.all(np.sign(out) == np.sign(phi))
+    band = (np.abs(out) > 2.5 * h) & (np.abs(out) < 6 * h)
+    before, after = np.median(np.abs(grad_norm(phi, c)[band] - 1)), np.median(np.abs(grad_norm(out, c)[band] - 1))
+    assert after < 0.06 and after < 0.15 * before, (before, after)
+
+
+def test_oracle_no_interface_is_a_no_op():
+    c, V, ID, phi = sphere_case(distort=None)
+    phi = np.abs(phi) + 0.01
+    o = ob.OracleSim(c)
+    o.upload(V, np.zeros_like(ID), phi)
+    found, st = o.reinitialize()
+    assert not found and st["calls"] == 0
+    np.testing.assert_array_equal(o.download()[2], phi)
+
+
+@pytest.mark.parametrize("max_its", [2, 30])
+def test_oracle_retry_reduces_cfl(max_its):
+    c, V, ID, phi = sphere_case(n=24, distort="strong")
+    c.reinit_max_its = max_its
+    _, found, st, out = oracle_reinit(c, V, ID, phi)
+    assert found and st["retries"] >= 1
+    assert st["cfl"] == pytest.approx(0.8 / 1.5 ** st["retries"], rel=1e-15)
+    assert np.all(np.sign(out) == np.sign(phi))
+
+
+def test_oracle_stepping_reinitializes_at_the_frequency():
+    c, V, ID, phi = problems.shock_bubble(n=16)
+    c.reinit_frequency = 2
+    o = ob.OracleSim(c)
+    o.upload(V, ID, phi)
+    o.run(5)
+    _, st = o.reinitialize()   # one explicit call on top of the steps' two
+    assert st["calls"] == 3
+
+
+# ---------------------------------------------------------------------------
+# GPU against the oracle
+
+
+def _gpu_reinit(c, V, ID, phi):
+    from m2c_gb300.solver import FluidState, Solver
+    s = Solver(c, FluidState(V, ID, phi))
+    st = s.Reinitialize()
+    return s, st, s.get_state().Phi
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("shape", [(32, 32, 32), (40, 24, 20)])
+def test_gpu_reinit_matches_oracle(shape):
+    c, V, ID, phi = sphere_case(n=32)
+    if shape != (32, 32, 32):
+        c, V, ID, phi = problems.shock_bubble(n=8)
+        c.nx, c.ny, c.nz = shape
+        c.ymax, c.zmax = 0.8, 0.6
+        X, Y, Z = problems.cell_centers(c)
+        phi = (np.sqrt((X - 0.45) ** 2 + (Y - 0.4) ** 2 + (Z - 0.3) ** 2) - 0.2) * (1.0 + 3.0 * Z)
+        V = np.tile([1000.0, 0.0, 0.0, 0.0, 1.0e5], (phi.size, 1))
+        ID = (phi < 0).astype(np.int32)
+        c.ls_bc[0], c.ls_bc[1] = abi.LSBC_LINEAR_EXTRAPOLATION, abi.LSBC_NON_NEGATIVE
+        c.ls_bc[4] = abi.LSBC_LINEAR_EXTRAPOLATION
+    _, found, sto, po = oracle_reinit(c, V, ID, phi)
+    _, stg, pg = _gpu_reinit(c, V, ID, phi)
+    assert found
+    for k in ("calls", "iterations", "retries", "failures"):
+        assert stg[k] == sto[k], (k, stg, sto)
+    assert stg["cfl"] == sto["cfl"]
+    assert rel_linf(pg, po) < 1e-10
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("max_its", [2, 30])
+def test_gpu_reinit_retry_matches_oracle(max_its):
+    c, V, ID, phi = sphere_case(n=24, distort="strong")
+    c.reinit_max_its = max_its
+    _, _, sto, po = oracle_reinit(c, V, ID, phi)
+    _, stg, pg = _gpu_reinit(c, V, ID, phi)
+    assert sto["retries"] >= 1
+    for k in ("calls", "iterations", "retries", "failures"):
+        assert stg[k] == sto[k], (k, stg, sto)
+    assert stg["cfl"] == sto["cfl"]
+    assert rel_linf(pg, po) < 1e-10
+
+
+@pytest.mark.gpu
+def test_gpu_reinit_without_interface_is_a_no_op():
+    c, V, ID, phi = sphere_case(n=16, distort=None)
+    phi = np.abs(phi) + 0.01
+    _, st, pg = _gpu_reinit(c, V, np.zeros_like(ID), phi)
+    assert st["calls"] == 0
+    np.testing.assert_array_equal(pg, phi)
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("ts", [abi.TS_RK2, abi.TS_RK3])
+def test_gpu_steps_with_reinit_match_oracle(ts):
+    from m2c_gb300.solver import FluidState, Solver
+    c, V, ID, phi = problems.shock_bubble(n=24)
+    c.ts_type = ts
+    c.reinit_frequency = 2
+    s = Solver(c, FluidState(V, ID, phi))
+    o = ob.OracleSim(c)
+    o.upload(V, ID, phi)
+    cnt = s.run(6)
+    o.run(6)
+    g = s.get_state()
+    Vo, IDo, phio = o.download()
+    assert cnt["steps"] == 6
+    assert s.reinit_stats()["calls"] == o.reinitialize()[1]["calls"] - 1 == 3
+    assert rel_linf(g.Phi, phio) < 1e-8
+    assert np.all(rel_linf(g.V, Vo)[[0, 4]] < 1e-8)
+    np.testing.assert_array_equal(g.ID, IDo)
