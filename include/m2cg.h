@@ -121,7 +121,8 @@ typedef struct {
   /* Learned warm start for the interface Riemann solve (no reference counterpart) */
   int32_t warm_start;          /* 0 = cold start (reference), 1 = MLP warm start */
   /* LevelSet[0].Reinitialization (IoData.cpp:1421-1429): full domain, first layer FIXED */
-  int32_t reinit_frequency;    /* Frequency: every that many steps (<= 0: never, the default) */
+  int32_t reinit_frequency;    /* Frequency: every that many steps (<= 0: never, the default;
+                                  FrequencyDt, the time-interval trigger, is not offered) */
   int32_t reinit_max_its;      /* MaxIts (30) */
   int32_t pad4_;
   double reinit_cfl;           /* CFL (0.8) */
@@ -355,6 +356,12 @@ m2cg_status m2cg_event_elapsed(m2cg_ctx* ctx, int32_t slot0, int32_t slot1, floa
 m2cg_status m2cg_phase_times(m2cg_ctx* ctx, int32_t n_steps, double ms[M2CG_N_PHASES]);
 /* Kernel launches issued on this context since creation (all kernels are this library's). */
 int64_t     m2cg_kernel_launches(m2cg_ctx* ctx);
+/* No reference counterpart (measurement helper): binary64 FMA throughput of
+ * this GPU -- eight independent FMA chains per thread, 8 blocks of 256 threads
+ * per SM, `iters` FMAs per chain (1 .. 2^22) -- in thread-level FMAs per second;
+ * ms (optional) receives the timed kernel's duration.  The FP64-pipe roofline's
+ * denominator. */
+m2cg_status m2cg_fp64_peak(int32_t iters, double* dfma_per_s, float* ms);
 /* Page-locked host memory for fast upload / download (NULL on failure). */
 void*       m2cg_host_alloc(size_t bytes);
 void        m2cg_host_free(void* ptr);

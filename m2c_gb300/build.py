@@ -25,6 +25,7 @@ UNITS = {
     "m2cg_noalloc.cu": ["-fmad=false"],
     "m2cg_mlp.cu": [],
     "m2cg_reinit.cu": ["-fmad=false"],
+    "m2cg_peak.cu": [],
 }
 
 
