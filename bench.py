@@ -36,9 +36,16 @@ sys.path.insert(0, ROOT)
 METRIC = "FP64 cell-stage updates/s (1 GB300) + Newton iters/interface, MLP vs cold start @1e-10"
 UNIT = "cell-stage/s"
 MEASURED_PEAKS = os.path.join(ROOT, "MEASURED_PEAKS.json")
-# FP64 fused multiply-add rate measured on this machine's GB300 with a dependent-chain
-# microbenchmark (1.91 DFMA/clk/SM at 2070 MHz, 152 SMs): 601.6e9 DFMA/s.
-FP64_DFMA_PER_S = 601.6e9
+# FP64-pipe instructions per cell of each stage kernel (warp instructions x 32 /
+# cells), binary64 FLOPs per cell (2 DFMA + DMUL + DADD, active lanes), and DRAM
+# bytes per cell, from the ncu capture of the 128^3 case in
+# profiles/fp64_stage_kernels_shock_bubble_128.txt; the counts per cell do not
+# depend on the grid size (the same code path runs on every cell or face).
+FP64_PROFILE = {
+    "reconstruct": {"fp64_pipe_inst_per_cell": 279.7, "fp64_flop_per_cell": 131.1, "dram_bytes_per_cell": 269.0},
+    "face_flux": {"fp64_pipe_inst_per_cell": 617.5, "fp64_flop_per_cell": 706.8, "dram_bytes_per_cell": 363.0},
+    "update": {"fp64_pipe_inst_per_cell": 104.5, "fp64_flop_per_cell": 122.6, "dram_bytes_per_cell": 293.9},
+}
 
 
 def parse():
@@ -52,6 +59,8 @@ def parse():
     ap.add_argument("--cpu-size", type=int, default=96)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
+    # level-set reinitialization every F steps in the main workload (0: off, the BASELINE shape)
+    ap.add_argument("--reinit", type=int, default=0)
     # learned warm start: training / test problems of the study (0 disables it)
     ap.add_argument("--ws-train", type=int, default=1 << 20)
     ap.add_argument("--ws-test", type=int, default=1 << 17)
@@ -289,6 +298,8 @@ def run_gb300(args):
     from m2c_gb300.solver import FluidState, Solver
     lib = abi.load()
     cfg, V, ID, phi = problems.shock_bubble(n=args.size)
+    if args.reinit > 0:
+        cfg.reinit_frequency = args.reinit
     cells = cfg.nx * cfg.ny * cfg.nz
     stages = 2
     s = Solver(cfg, FluidState(V, ID, phi))
@@ -343,9 +354,30 @@ def run_gb300(args):
     pk, pk_kind = peaks()
     per_launch_ms = phase[dom] / stages
     achieved_gbs = alg_bytes[dom] * cells / (per_launch_ms * 1e-3) / 1e9
+    prof = FP64_PROFILE.get(dom)
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
-            "frac": achieved_gbs / pk["hbm_gbs"], "traffic": None, "peak_source": pk_kind,
+            "frac": achieved_gbs / pk["hbm_gbs"],
+            "traffic": prof["dram_bytes_per_cell"] * cells if prof else None, "peak_source": pk_kind,
             "alg_bytes_per_cell": alg_bytes[dom], "launch_ms": per_launch_ms}
+    # the binding bound of the stage kernels: GB300's FP64 pipe.  Peak = binary64
+    # FMAs/s of this GPU measured now (m2cg_fp64_peak); achieved = the kernel's
+    # FP64-pipe instructions per launch (per-cell count from the ncu profile x
+    # cells) / its event-timed duration.
+    dfma = C.c_double()
+    fp64 = None
+    if lib.m2cg_fp64_peak(1 << 15, C.byref(dfma), None) == 0 and prof:
+        inst = prof["fp64_pipe_inst_per_cell"] * cells / (per_launch_ms * 1e-3)
+        flops = prof["fp64_flop_per_cell"] * cells / (per_launch_ms * 1e-3)
+        fp64 = {"bound": "fp64", "kernel": dom, "achieved": inst / 1e9, "peak": dfma.value / 1e9,
+                "unit": "G FP64-pipe inst/s", "frac": inst / dfma.value,
+                "flop_rate_tflops": flops / 1e12, "flop_peak_tflops": 2 * dfma.value / 1e12,
+                "fp64_pipe_inst_per_cell": prof["fp64_pipe_inst_per_cell"],
+                "fp64_flop_per_cell": prof["fp64_flop_per_cell"],
+                "peak_source": "measured now: m2cg_fp64_peak (independent binary64 FMA chains)",
+                "counts_source": "ncu, profiles/fp64_stage_kernels_shock_bubble_128.txt"}
+    elif dfma.value > 0:
+        fp64 = {"bound": "fp64", "peak": dfma.value / 1e9, "unit": "G FP64-pipe inst/s", "achieved": None,
+                "frac": None, "peak_source": "measured now: m2cg_fp64_peak"}
 
     # e2e through the C ABI with host buffers
     e2e_steps = args.e2e_steps or max(2, min(args.steps, 5))
@@ -428,17 +460,18 @@ def run_gb300(args):
         cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port",
                "sample": f"oracle CPU restatement, shock-bubble {args.cpu_size}^3, {args.cpu_steps} RK2 steps "
                          f"({tcpu:.1f} s)"}
-    # FP64 pipe view of the whole stage (from the fp64 op counts in profiles/)
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": f"shock-bubble {args.size}^3, SG/SG, MUSCL-van Albada, HLLC, exact interface "
                                   f"Riemann @1e-10, RK2, CFL 0.4", "cells": cells, "stages_per_step": stages,
                       "l2": "inputs larger than L2 (state 52 B/cell x 16.8M cells = 0.87 GB per copy)",
+                      "reinit_frequency": args.reinit if args.reinit > 0 else None,
                       "parallelism": "replicas" if world > 1 else "single"},
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nb_v + nb_i + nb_p,
                    "d2h_bytes_per_step": nb_v + nb_i + nb_p, "steps": e2e_steps},
            "roofline": roof,
+           "roofline_fp64": fp64,
            "cpu_baseline": cpu,
            "gpu_launches": int(launches),
            "clocks": clk,

@@ -14,9 +14,13 @@
 //
 // Compiled without floating-point contraction: the stage combinations, the sign
 // function and the ghost extrapolation follow the reference's operation order
-// in plain binary64.  The one-sided differences are multiplied by 1/h where the
-// reference divides by the difference of the two cell-centre coordinates; the
-// two agree to the rounding of those coordinates.
+// in plain binary64.  The residual is written for GB300's FP64 pipe, which
+// bounds this loop: the one-sided differences are multiplied by 1/h where the
+// reference divides by the difference of two cell-centre coordinates (equal to
+// h up to the rounding of those coordinates), signs flip and maxima are taken
+// on the integer pipe through the bit patterns, and the square root and the
+// relative change use a refined hardware reciprocal (square root) estimate.
+// The result differs from the reference's operation order by a few ulps.
 #include <algorithm>
 #include "m2cg_internal.h"
 
@@ -40,17 +44,41 @@ M2CG_DEV double max_with_zero(double x, double y) {
   return __longlong_as_double(m > 0 ? m : 0);
 }
 
+// x with its sign bit xor-ed with sb (0 or the sign bit): an exact negation
+// when sb is set, on the integer pipe.
+M2CG_DEV double flip(double x, long long sb) { return __longlong_as_double(__double_as_longlong(x) ^ sb); }
+
+// sqrt(x) for x >= 0 as x * rsqrt(x), the reciprocal square root from the
+// hardware estimate refined by Newton's iteration (one step, cubic term).
+M2CG_DEV double sqrt_nr(double x) {
+  if (!(x > 1e-300)) return sqrt(x);   // zero, subnormal (the estimate flushes it), NaN
+  double y;
+  asm("rsqrt.approx.ftz.f64 %0, %1;" : "=d"(y) : "d"(x));
+  const double e = fma(-x, y * y, 1.0);
+  y = fma(y * e, fma(e, 0.375, 0.5), y);
+  return x * y;
+}
+
+// 1/x for x > 0 from the hardware estimate refined by Newton's iteration.
+M2CG_DEV double rcp_nr(double x) {
+  double r;
+  asm("rcp.approx.ftz.f64 %0, %1;" : "=d"(r) : "d"(x));
+  const double e = fma(-x, r, 1.0);
+  return fma(r, fma(e, e, e), r);
+}
+
 // |grad phi| - 1 by Godunov's upwind rule (LevelSetReinitializer.cpp:1009-1026).
 // For phi >= 0 the x term is max(max(a,0)^2, min(b,0)^2) with a, b the backward
 // and forward differences; it equals (max(p - p_{i-1}, p - p_{i+1}, 0) / h)^2.
-// For phi < 0 the differences change sign.  Multiplying by +-1 is exact.
+// For phi < 0 the differences change sign (phi = -0 counts as >= 0, as there).
 M2CG_DEV double ri_res(const double* __restrict__ q, int64_t c, int64_t sy, int64_t sz, const double* rh) {
   const double p = q[c];
-  const double s = p >= 0.0 ? 1.0 : -1.0;
-  const double gx = max_with_zero(s * (p - q[c - 1]), s * (p - q[c + 1])) * rh[0];
-  const double gy = max_with_zero(s * (p - q[c - sy]), s * (p - q[c + sy])) * rh[1];
-  const double gz = max_with_zero(s * (p - q[c - sz]), s * (p - q[c + sz])) * rh[2];
-  return sqrt(gx * gx + gy * gy + gz * gz) - 1.0;
+  const long long pb = __double_as_longlong(p);
+  const long long sb = (pb < 0 && pb != (long long)0x8000000000000000ull) ? (long long)0x8000000000000000ull : 0ll;
+  const double gx = max_with_zero(flip(p - q[c - 1], sb), flip(p - q[c + 1], sb)) * rh[0];
+  const double gy = max_with_zero(flip(p - q[c - sy], sb), flip(p - q[c + sy], sb)) * rh[1];
+  const double gz = max_with_zero(flip(p - q[c - sz], sb), flip(p - q[c + sz], sb)) * rh[2];
+  return sqrt_nr(fma(gz, gz, fma(gy, gy, gx * gx))) - 1.0;
 }
 
 // Block maximum of non-negative bit patterns, one atomic per block.
@@ -156,7 +184,9 @@ __global__ void __launch_bounds__(RI_THREADS) k_ri_stage(ReinitArgs a) {
         const double nw = ((1.0 / 3.0) * old + (2.0 / 3.0) * src[c]) + (2.0 / 3.0) * R;
         out[c] = nw;
         double e = fabs(nw - old);
-        if (nw != 0.0) e /= fabs(nw);
+        const double anw = fabs(nw);
+        if (anw > 1e-300) e *= rcp_nr(anw);
+        else if (nw != 0.0) e /= anw;
         const unsigned long long b = as_bits(e);
         mx = b > mx ? b : mx;
       }
