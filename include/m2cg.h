@@ -53,7 +53,9 @@ enum { M2CG_FLUX_ROE = 0, M2CG_FLUX_LLF = 1, M2CG_FLUX_HLLC = 2 };
 enum { M2CG_REC_CONSTANT = 0, M2CG_REC_LINEAR = 1 };
 enum { M2CG_LIM_NONE = 0, M2CG_LIM_GENERALIZED_MINMOD = 1, M2CG_LIM_VANALBADA = 2 };
 enum { M2CG_SLOPE_ZERO = 0, M2CG_SLOPE_NONZERO = 1 };
-enum { M2CG_VAR_PRIMITIVE = 0 };
+/* Reconstruction.VariableType (IoData.cpp:1300-1304). */
+enum { M2CG_VAR_PRIMITIVE = 0, M2CG_VAR_CONSERVATIVE = 1, M2CG_VAR_PRIMITIVE_CHARACTERISTIC = 2,
+       M2CG_VAR_CONSERVATIVE_CHARACTERISTIC = 3 };
 /* Multiphase (MultiPhaseData, IoData.h:893-903). */
 enum { M2CG_MPFLUX_EXACT = 0, M2CG_MPFLUX_NUMERICAL = 1, M2CG_MPFLUX_LLF = 2 };
 enum { M2CG_MPREC_CONSTANT = 0, M2CG_MPREC_LINEAR = 1 };
@@ -94,7 +96,7 @@ typedef struct {
   int32_t flux;                /* Flux: M2CG_FLUX_* (default HLLC) */
   int32_t rec_type;            /* Reconstruction.Type (default Linear) */
   int32_t limiter;             /* Reconstruction.Limiter (default GeneralizedMinMod) */
-  int32_t rec_var;             /* Reconstruction.VariableType (Primitive only) */
+  int32_t rec_var;             /* Reconstruction.VariableType: M2CG_VAR_* (default Primitive) */
   int32_t slope_near_interface;/* Reconstruction.SlopeNearInterface (default NonZero) */
   int32_t pad2_;
   double minmod_coeff;         /* GeneralizedMinModCoefficient (1.2) */
@@ -176,6 +178,15 @@ m2cg_status m2cg_download_state(m2cg_ctx* ctx, double* V, int32_t* id, double* p
 
 /* SpaceOperator::ComputeTimeStepSize (SpaceOperator.cpp:1298-1330). */
 m2cg_status m2cg_compute_dt(m2cg_ctx* ctx, double* dt, double* cfl);
+
+/* The state with its ghost layer, as the reference's ghosted local arrays hold
+ * it after the boundary conditions (SpaceOperator.cpp:738-821; edge and corner
+ * ghosts are not populated, as there): (nx+2) x (ny+2) x (nz+2) cells, i
+ * fastest, real cell (i,j,k) at ((k+1)(ny+2) + j+1)(nx+2) + i+1.  V: 5 planes of
+ * that size (rho, u, v, w, p); id, phi: one plane each (phi ignored without a
+ * level set).  Any pointer may be NULL.  Used by probes and line plots
+ * (ProbeOutput.cpp:360-597, 848-886), which interpolate across the boundary. */
+m2cg_status m2cg_download_ghosted(m2cg_ctx* ctx, double* V, int32_t* id, double* phi);
 
 /* SpaceOperator::ComputeResidual on the current state with the stored
  * Riemann solutions refreshed (SpaceOperator.cpp:2573-2641, first RK stage).

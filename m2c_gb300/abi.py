@@ -22,6 +22,7 @@ FLUX_ROE, FLUX_LLF, FLUX_HLLC = 0, 1, 2
 REC_CONSTANT, REC_LINEAR = 0, 1
 LIM_NONE, LIM_GENERALIZED_MINMOD, LIM_VANALBADA = 0, 1, 2
 SLOPE_ZERO, SLOPE_NONZERO = 0, 1
+VAR_PRIMITIVE, VAR_CONSERVATIVE, VAR_PRIMITIVE_CHARACTERISTIC, VAR_CONSERVATIVE_CHARACTERISTIC = 0, 1, 2, 3
 MPFLUX_EXACT, MPFLUX_NUMERICAL, MPFLUX_LLF = 0, 1, 2
 MPREC_CONSTANT, MPREC_LINEAR = 0, 1
 PHASECHANGE_RIEMANN, PHASECHANGE_EXTRAPOLATION = 0, 1
@@ -186,6 +187,7 @@ def load(path=None):
         "m2cg_get_counters": (C.c_int, [_P, C.POINTER(Counters)]),
         "m2cg_reinitialize": (C.c_int, [_P, C.POINTER(ReinitStats)]),
         "m2cg_fp64_peak": (C.c_int, [C.c_int32, _D, C.POINTER(C.c_float)]),
+        "m2cg_download_ghosted": (C.c_int, [_P, _D, _I, _D]),
         "m2cg_get_reinit_stats": (C.c_int, [_P, C.POINTER(ReinitStats)]),
         "m2cg_conserved_totals": (C.c_int, [_P, _D]),
         "m2cg_riemann_batch": (C.c_int, [_P, C.c_int64, _D, _I, _D, _I, _D, _D, _I, _D, _D, _I, _I]),

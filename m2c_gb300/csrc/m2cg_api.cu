@@ -168,7 +168,7 @@ struct m2cg_ctx {
 m2cg_status m2cg_fill_params(const m2cg_config& c, m2cg::Params& P) {
   if (c.nx < 1 || c.ny < 1 || c.nz < 1) { set_err("mesh dimensions must be >= 1"); return M2CG_ERR_INVALID_ARG; }
   if (c.n_materials < 1 || c.n_materials > M2CG_MAX_MATERIALS) { set_err("n_materials out of range"); return M2CG_ERR_INVALID_ARG; }
-  if (c.rec_var != M2CG_VAR_PRIMITIVE) { set_err("only primitive-variable reconstruction is supported"); return M2CG_ERR_INVALID_ARG; }
+  if (c.rec_var < M2CG_VAR_PRIMITIVE || c.rec_var > M2CG_VAR_CONSERVATIVE_CHARACTERISTIC) { set_err("bad reconstruction variable type"); return M2CG_ERR_INVALID_ARG; }
   if (c.n_levelsets < 0 || c.n_levelsets > 1) { set_err("at most one level set is supported"); return M2CG_ERR_INVALID_ARG; }
   if (c.n_levelsets == 1 && (c.ls_matid < 0 || c.ls_matid >= c.n_materials)) { set_err("ls_matid out of range"); return M2CG_ERR_INVALID_ARG; }
   if (c.ts_type < 0 || c.ts_type > 2) { set_err("bad ts_type"); return M2CG_ERR_INVALID_ARG; }
@@ -193,6 +193,7 @@ m2cg_status m2cg_fill_params(const m2cg_config& c, m2cg::Params& P) {
     d.clip_default = (s.rhomin == 0.0 && s.pmin == -DBL_MAX && s.rhomax == DBL_MAX && s.pmax == DBL_MAX);
   }
   P.flux = c.flux; P.rec_type = c.rec_type; P.limiter = c.limiter; P.slope_zero = (c.slope_near_interface == M2CG_SLOPE_ZERO);
+  P.rec_var = c.rec_var;
   P.mp_flux = c.mp_flux; P.mp_recon = c.mp_recon; P.mp_phasechange = c.mp_phasechange; P.mp_pcdir = c.mp_phasechange_dir;
   P.minmod_coeff = c.minmod_coeff; P.roe_delta = c.roe_delta;
   for (int s = 0; s < 6; s++) { P.bc[s] = c.bc[s]; P.ls_bc[s] = c.ls_bc[s]; }
@@ -605,6 +606,19 @@ m2cg_status m2cg_download_state(m2cg_ctx* x, double* V, int32_t* id, double* phi
   if (phi) CK(cudaMemcpyAsync(phi, x->stage_phi, n * sizeof(double), cudaMemcpyDeviceToHost, s));
   CK(cudaStreamSynchronize(s));
   CK(cudaGetLastError());
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_download_ghosted(m2cg_ctx* x, double* V, int32_t* id, double* phi) {
+  if (!x) { set_err("null context"); return M2CG_ERR_INVALID_ARG; }
+  cudaStream_t s = x->stream;
+  const size_t n = (size_t)x->P.g.ntot;
+  if (V)
+    for (int p = 0; p < 5; p++)
+      CK(cudaMemcpyAsync(V + (size_t)p * n, x->S[0].q[p], n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  if (id) CK(cudaMemcpyAsync(id, x->id, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+  if (phi && x->P.n_ls > 0) CK(cudaMemcpyAsync(phi, x->S[0].q[5], n * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
   return M2CG_OK;
 }
 
@@ -1242,6 +1256,10 @@ m2cg_status m2cg_ensemble_create(const m2cg_config* cfgs, int32_t n, m2cg_ensemb
     return M2CG_ERR_INVALID_ARG;
   }
   for (int d = 0; d < n; d++) {
+    if (cfgs[d].rec_var != M2CG_VAR_PRIMITIVE) {
+      set_err("member %d: the batched step reconstructs primitive variables only", d);
+      return M2CG_ERR_INVALID_ARG;
+    }
     if (cfgs[d].n_levelsets > 0 && cfgs[d].reinit_frequency > 0) {
       set_err("member %d: the batched step does not reinitialize level sets (reinit_frequency must be <= 0)", d);
       return M2CG_ERR_INVALID_ARG;

@@ -68,6 +68,7 @@ struct Params {
   Mats mats;
   int n_mat;
   int flux, rec_type, limiter, slope_zero;
+  int rec_var;          // M2CG_VAR_*: variables whose differences are limited
   int mp_flux, mp_recon, mp_phasechange, mp_pcdir;
   double minmod_coeff, roe_delta;
   int bc[6];

@@ -38,6 +38,30 @@ __device__ __forceinline__ bool real_cell(const Grid& g, int64_t t, int& i, int&
   return true;
 }
 
+// CheckReconstructedStates (SpaceOperator.cpp:2446-2484): a face state that
+// clipping would change reverts to the cell value; then the six face states
+// are stored.
+__device__ __forceinline__ void store_faces(const DevMat& M, const double* q, double (*face)[5], double* const* fs,
+                                            int64_t c, unsigned long long* cnt) {
+  int nclip = 0, nbad = 0;
+#pragma unroll
+  for (int f = 0; f < 6; f++) {
+    double t[5] = {face[f][0], face[f][1], face[f][2], face[f][3], face[f][4]};
+    if (eos_clip_fast(M, t)) {
+#pragma unroll
+      for (int p = 0; p < 5; p++) face[f][p] = q[p];
+      nclip++;
+    }
+    nbad += eos_bad5_fast(M, face[f]);
+  }
+  if (nclip) atomic_inc(&cnt[CNT_CLIPFACE], nclip);
+  if (nbad) atomic_inc(&cnt[CNT_BAD], nbad);
+#pragma unroll
+  for (int f = 0; f < 6; f++)
+#pragma unroll
+    for (int p = 0; p < 5; p++) fs[f * 5 + p][c] = face[f][p];
+}
+
 // ---------------------------------------------------------------------------
 // K1: MUSCL reconstruction of the six face states of every real cell
 // (Reconstructor.cpp:426-782) followed by CheckReconstructedStates
@@ -88,24 +112,7 @@ __device__ __forceinline__ void k_reconstruct_body(const Params& P, const StateS
       }
     }
   }
-  // CheckReconstructedStates: clip -> revert to the cell value
-  int nclip = 0, nbad = 0;
-#pragma unroll
-  for (int f = 0; f < 6; f++) {
-    double t[5] = {face[f][0], face[f][1], face[f][2], face[f][3], face[f][4]};
-    if (eos_clip_fast(M, t)) {
-#pragma unroll
-      for (int p = 0; p < 5; p++) face[f][p] = q[p];
-      nclip++;
-    }
-    nbad += eos_bad5_fast(M, face[f]);
-  }
-  if (nclip) atomic_inc(&cnt[CNT_CLIPFACE], nclip);
-  if (nbad) atomic_inc(&cnt[CNT_BAD], nbad);
-#pragma unroll
-  for (int f = 0; f < 6; f++)
-#pragma unroll
-    for (int p = 0; p < 5; p++) fs[f * 5 + p][c] = face[f][p];
+  store_faces(M, q, face, fs, c, cnt);
 }
 __global__ void __launch_bounds__(128) k_reconstruct(Params P, StateSet S, const int32_t* __restrict__ id,
                                                      double* const* fs, unsigned long long* cnt) { k_reconstruct_body(P, S, id, fs, cnt, blockIdx.x, gridDim.x); }
@@ -118,6 +125,188 @@ __global__ void __launch_bounds__(128) k_reconstruct_ens(const k_reconstruct_arg
 }
 
 
+
+// ---------------------------------------------------------------------------
+// K1 for the other reconstruction variable types (Reconstructor.cpp:335-918):
+// conservative differences (each cell's U with its own material), or primitive
+// / conservative differences projected on the characteristic fields of the
+// cell's state in each direction (FluxFcnBase.h:308-517), limited, projected
+// back; conservative face states convert back to primitive.  A nonphysical face
+// state restarts the cell in primitive variables, where the first nonphysical
+// face reverts to the cell value (Reconstructor.cpp:722-778).
+
+// The EOS quantities and eigenvector products of the characteristic basis at V0.
+struct CharBasis {
+  double e0, c0, dpdrho0, Gamma0, kin0, alpha0, beta0, H0;
+};
+__device__ __forceinline__ void char_basis(const DevMat& M, const double* V0, CharBasis& b) {
+  b.e0 = eos_e(M, V0[0], V0[4]);
+  b.c0 = sqrt(eos_c2(M, V0[0], b.e0));
+  b.dpdrho0 = eos_dpdrho(M, V0[0], b.e0);
+  b.Gamma0 = eos_Gamma(M, V0[0]);
+  b.kin0 = 0.5 * (V0[1] * V0[1] + V0[2] * V0[2] + V0[3] * V0[3]);
+  b.alpha0 = V0[0] * b.Gamma0 / (V0[4] * b.Gamma0 + V0[0] * b.dpdrho0);
+  b.beta0 = (b.e0 - b.kin0 + V0[4] / V0[0]) * b.alpha0;
+  b.H0 = b.e0 + b.kin0 + V0[4] / V0[0];
+}
+// dW = R0^-1 x in direction d (rows: the u-c wave, three transverse / entropy
+// fields, the u+c wave)
+__device__ __forceinline__ void char_left(const CharBasis& b, const double* V0, int d, const double* x, double* w) {
+  const double un = V0[1 + d], ic = 1.0 / b.c0, a = b.alpha0;
+  double s = 0.0;
+#pragma unroll
+  for (int j = 0; j < 3; j++) s += a * V0[1 + j] * x[1 + j];
+  w[0] = 0.5 * (1.0 - b.beta0 + un * ic) * x[0] - 0.5 * s - 0.5 * ic * x[1 + d] + 0.5 * a * x[4];
+  w[4] = 0.5 * (1.0 - b.beta0 - un * ic) * x[0] - 0.5 * s + 0.5 * ic * x[1 + d] + 0.5 * a * x[4];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    if (i == d) w[1 + i] = (b.beta0 + un - V0[1 + i]) * x[0] + s - a * x[4];
+    else w[1 + i] = -V0[1 + i] * x[0] + x[1 + i];
+  }
+}
+// x = R0 dW in direction d
+__device__ __forceinline__ void char_right(const CharBasis& b, const double* V0, int d, const double* w, double* x) {
+  const double un = V0[1 + d];
+  const double param = b.e0 + b.kin0 - b.dpdrho0 / b.Gamma0 - un;
+  x[0] = w[0] + w[1 + d] + w[4];
+#pragma unroll
+  for (int i = 0; i < 3; i++) {
+    // row 1+i of R0: (V_i - c n_i, delta_ij + V_i n_j - n_i n_j, V_i + c n_i)
+    if (i == d) x[1 + i] = V0[1 + i] * (w[0] + w[4]) + b.c0 * (w[4] - w[0]) + V0[1 + i] * w[1 + d];
+    else x[1 + i] = V0[1 + i] * (w[0] + w[4]) + w[1 + i] + V0[1 + i] * w[1 + d];
+  }
+  double t4 = (b.H0 - un * b.c0) * w[0] + (b.H0 + un * b.c0) * w[4];
+#pragma unroll
+  for (int j = 0; j < 3; j++) t4 += (V0[1 + j] + (j == d ? param : 0.0)) * w[1 + j];
+  x[4] = t4;
+}
+
+template <int VT>
+__device__ __forceinline__ void reconstruct_var_cell(const Params& P, const StateSet& S, const int32_t* __restrict__ id,
+                                                     int64_t c, const double* q, int myid, double (*face)[5]) {
+  const Grid& g = P.g;
+  const DevMat& M = P.mats.m[myid];
+  const int64_t st[3] = {1, g.sy, g.sz};
+  CharBasis b;
+  if (VT == M2CG_VAR_PRIMITIVE_CHARACTERISTIC || VT == M2CG_VAR_CONSERVATIVE_CHARACTERISTIC) char_basis(M, q, b);
+  int vt = VT;
+  for (int pass = 0; pass < 2; pass++) {
+    const bool cons = (vt == M2CG_VAR_CONSERVATIVE || vt == M2CG_VAR_CONSERVATIVE_CHARACTERISTIC);
+    double w[5];
+    if (cons) prim_to_cons(M, q, w);
+    else {
+#pragma unroll
+      for (int p = 0; p < 5; p++) w[p] = q[p];
+    }
+    double sig[3][5];
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      double wm[5], wp[5], dq0[5], dq1[5];
+#pragma unroll
+      for (int p = 0; p < 5; p++) { wm[p] = S.q[p][c - st[d]]; wp[p] = S.q[p][c + st[d]]; }
+      if (cons) {
+        double t[5];
+        prim_to_cons(P.mats.m[id[c - st[d]]], wm, t);
+#pragma unroll
+        for (int p = 0; p < 5; p++) wm[p] = t[p];
+        prim_to_cons(P.mats.m[id[c + st[d]]], wp, t);
+#pragma unroll
+        for (int p = 0; p < 5; p++) wp[p] = t[p];
+      }
+#pragma unroll
+      for (int p = 0; p < 5; p++) { dq0[p] = w[p] - wm[p]; dq1[p] = wp[p] - w[p]; }
+      if (vt == M2CG_VAR_PRIMITIVE_CHARACTERISTIC) {
+        // Q0: primitive -> conservative differential at q (FluxFcnBase.h:322-330)
+        const double q51 = b.e0 + b.kin0 - b.dpdrho0 / b.Gamma0;
+        double t0[5], t1[5];
+        t0[0] = dq0[0]; t1[0] = dq1[0];
+#pragma unroll
+        for (int i = 1; i < 4; i++) { t0[i] = q[i] * dq0[0] + q[0] * dq0[i]; t1[i] = q[i] * dq1[0] + q[0] * dq1[i]; }
+        t0[4] = q51 * dq0[0] + q[0] * q[1] * dq0[1] + q[0] * q[2] * dq0[2] + q[0] * q[3] * dq0[3] + dq0[4] / b.Gamma0;
+        t1[4] = q51 * dq1[0] + q[0] * q[1] * dq1[1] + q[0] * q[2] * dq1[2] + q[0] * q[3] * dq1[3] + dq1[4] / b.Gamma0;
+        char_left(b, q, d, t0, dq0);
+        char_left(b, q, d, t1, dq1);
+      } else if (vt == M2CG_VAR_CONSERVATIVE_CHARACTERISTIC) {
+        double t0[5], t1[5];
+        char_left(b, q, d, dq0, t0);
+        char_left(b, q, d, dq1, t1);
+#pragma unroll
+        for (int p = 0; p < 5; p++) { dq0[p] = t0[p]; dq1[p] = t1[p]; }
+      }
+#pragma unroll
+      for (int p = 0; p < 5; p++) {
+        double s;
+        if (P.limiter == M2CG_LIM_VANALBADA) s = van_albada_fast(dq0[p], dq1[p]);
+        else if (P.limiter == M2CG_LIM_GENERALIZED_MINMOD) s = gen_minmod(P.minmod_coeff, dq0[p], dq1[p]);
+        else s = 0.5 * (dq0[p] + dq1[p]);
+        sig[d][p] = s;
+      }
+      if (vt == M2CG_VAR_PRIMITIVE_CHARACTERISTIC) {
+        // R0 then Q0^-1 (FluxFcnBase.h:392-419)
+        double t[5];
+        char_right(b, q, d, sig[d], t);
+        const double ir = 1.0 / q[0];
+        sig[d][0] = t[0];
+#pragma unroll
+        for (int i = 1; i < 4; i++) sig[d][i] = -q[i] * ir * t[0] + t[i] * ir;
+        sig[d][4] = ((-b.e0 + b.kin0) * b.Gamma0 + b.dpdrho0) * t[0] -
+                    b.Gamma0 * (q[1] * t[1] + q[2] * t[2] + q[3] * t[3] - t[4]);
+      } else if (vt == M2CG_VAR_CONSERVATIVE_CHARACTERISTIC) {
+        double t[5];
+        char_right(b, q, d, sig[d], t);
+#pragma unroll
+        for (int p = 0; p < 5; p++) sig[d][p] = t[p];
+      }
+      if (P.slope_zero && (id[c - st[d]] != myid || id[c + st[d]] != myid)) {
+#pragma unroll
+        for (int p = 0; p < 5; p++) sig[d][p] = 0.0;
+      }
+    }
+#pragma unroll
+    for (int f = 0; f < 6; f++) {
+      const double h = (f & 1) ? 0.5 : -0.5;
+      if (cons) {
+        double u2[5];
+#pragma unroll
+        for (int p = 0; p < 5; p++) u2[p] = w[p] + h * sig[f >> 1][p];
+        cons_to_prim(M, u2, face[f]);
+      } else {
+#pragma unroll
+        for (int p = 0; p < 5; p++) face[f][p] = q[p] + h * sig[f >> 1][p];
+      }
+    }
+    int bad = -1;
+#pragma unroll
+    for (int f = 0; f < 6; f++)
+      if (bad < 0 && eos_bad5(M, face[f])) bad = f;
+    if (bad < 0) return;
+    if (vt == M2CG_VAR_PRIMITIVE) {
+#pragma unroll
+      for (int f = 0; f < 6; f++)
+        if (f == bad) {
+#pragma unroll
+          for (int p = 0; p < 5; p++) face[f][p] = q[p];
+        }
+      return;
+    }
+    vt = M2CG_VAR_PRIMITIVE;
+  }
+}
+
+template <int VT>
+__global__ void __launch_bounds__(128) k_reconstruct_var(Params P, StateSet S, const int32_t* __restrict__ id,
+                                                         double* const* fs, unsigned long long* cnt) {
+  int i, j, k;
+  if (!real_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
+  const int64_t c = P.g.at(i, j, k);
+  double q[5];
+#pragma unroll
+  for (int p = 0; p < 5; p++) q[p] = S.q[p][c];
+  const int myid = id[c];
+  double face[6][5];
+  reconstruct_var_cell<VT>(P, S, id, c, q, myid, face);
+  store_faces(P.mats.m[myid], q, face, fs, c, cnt);
+}
 
 // K1b: face states of the face-ghost cells by boundary condition
 // (Reconstructor.cpp:807-889), then the boundary branch of
@@ -796,7 +985,14 @@ static inline int nblk(int64_t n, int b) { return (int)((n + b - 1) / b); }
 void launch_reconstruct(cudaStream_t s, const Params& P, const StateSet& S, const int32_t* id, double* const* fs,
                         unsigned long long* cnt) {
   int64_t n = (int64_t)P.g.nx * P.g.ny * P.g.nz;
-  k_reconstruct<<<nblk(n, 128), 128, 0, s>>>(P, S, id, fs, cnt);
+  if (P.rec_type == M2CG_REC_CONSTANT || P.rec_var == M2CG_VAR_PRIMITIVE)
+    k_reconstruct<<<nblk(n, 128), 128, 0, s>>>(P, S, id, fs, cnt);
+  else if (P.rec_var == M2CG_VAR_CONSERVATIVE)
+    k_reconstruct_var<M2CG_VAR_CONSERVATIVE><<<nblk(n, 128), 128, 0, s>>>(P, S, id, fs, cnt);
+  else if (P.rec_var == M2CG_VAR_PRIMITIVE_CHARACTERISTIC)
+    k_reconstruct_var<M2CG_VAR_PRIMITIVE_CHARACTERISTIC><<<nblk(n, 128), 128, 0, s>>>(P, S, id, fs, cnt);
+  else
+    k_reconstruct_var<M2CG_VAR_CONSERVATIVE_CHARACTERISTIC><<<nblk(n, 128), 128, 0, s>>>(P, S, id, fs, cnt);
   int64_t ng = 2 * ((int64_t)P.g.ny * P.g.nz + (int64_t)P.g.nx * P.g.nz + (int64_t)P.g.nx * P.g.ny);
   k_reconstruct_ghosts<<<nblk(ng, 128), 128, 0, s>>>(P, S, id, fs, cnt);
 }

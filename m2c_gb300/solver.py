@@ -66,6 +66,29 @@ class Solver:
                   "m2cg_download_state")
         return FluidState(V, ID, Phi)
 
+    def get_state_ghosted(self):
+        """(V planes 5 x N, ID, phi) with the ghost layer after the boundary
+        conditions, N = (nx+2)(ny+2)(nz+2), i fastest (the probes' input)."""
+        n = (self.cfg.nx + 2) * (self.cfg.ny + 2) * (self.cfg.nz + 2)
+        V = np.zeros(5 * n)
+        ID = np.zeros(n, np.int32)
+        Phi = np.zeros(n)
+        abi.check(self.lib, self.lib.m2cg_download_ghosted(self.ctx, abi.dptr(V), abi.iptr(ID), abi.dptr(Phi)),
+                  "m2cg_download_ghosted")
+        return V.reshape(5, n), ID, Phi
+
+    def run_to_end(self, max_time, max_its, chunk=64):
+        """The Main.cpp:653-771 loop to MaxTime or MaxIts, whichever comes
+        first, in chunks of graph-replayed steps; returns the counters."""
+        c = self.counters()
+        while c["steps"] < max_its and c["time"] < max_time * (1.0 - 1e-12):
+            n = int(min(chunk, max_its - c["steps"]))
+            before = c["steps"]
+            c = self.run(n)
+            if c["steps"] == before:   # MaxTime reached inside the chunk
+                break
+        return c
+
     def ComputeTimeStepSize(self):
         dt, cfl = C.c_double(), C.c_double()
         abi.check(self.lib, self.lib.m2cg_compute_dt(self.ctx, C.byref(dt), C.byref(cfl)), "m2cg_compute_dt")

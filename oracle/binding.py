@@ -27,6 +27,7 @@ def _load_oracle():
         "orc_levelset_residual": (None, [_P, _D]),
         "orc_compute_dt": (None, [_P, _D, _D]),
         "orc_reinitialize": (C.c_int, [_P, _D]),
+        "orc_download_ghosted": (None, [_P, _D, _I, _D]),
         "orc_advance": (None, [_P, C.c_double]),
         "orc_run": (C.c_int, [_P, C.c_int]),
         "orc_counters": (None, [_P, C.POINTER(Counters)]),
@@ -100,6 +101,15 @@ class OracleSim:
         R = np.zeros(self.n)
         lib().orc_levelset_residual(self.h, dptr(R))
         return R
+
+    def download_ghosted(self):
+        """(V planes 5 x N, ID, phi) with the ghost layer, N = (nx+2)(ny+2)(nz+2), i fastest."""
+        n = (self.cfg.nx + 2) * (self.cfg.ny + 2) * (self.cfg.nz + 2)
+        V = np.zeros(5 * n)
+        ID = np.zeros(n, np.int32)
+        phi = np.zeros(n)
+        lib().orc_download_ghosted(self.h, dptr(V), iptr(ID), dptr(phi))
+        return V.reshape(5, n), ID, phi
 
     def reinitialize(self):
         """One full-domain reinitialization; returns (found_interface, stats dict)."""

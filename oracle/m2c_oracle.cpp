@@ -256,7 +256,110 @@ inline double VanAlbada(double A, double B, int k, double dq0, double dq1) {  //
   return B * (dq1 * a + dq0 * b) / (a + A * b);
 }
 
-// Reconstructor.cpp:335-918, primitive variables.  fs[0..5] = vl, vr, vb, vt, vk, vf (ghosted, AoS).
+// Characteristic variables about a reference primitive state V0, direction
+// dir (FluxFcnBase.h:308-517): the EOS quantities at V0, the left (R0^-1) and
+// right (R0) eigenvector matrices of the Euler flux Jacobian in conservative
+// form, and the primitive <-> conservative differential Q0.  Every entry and
+// product follows the reference's expression order.
+struct CharBasis {
+  double e0, c0, dpdrho0, Gamma0, kin0;
+};
+static CharBasis char_basis(const Eos& e, const double* V0) {
+  CharBasis b;
+  b.e0 = e.GetInternalEnergyPerUnitMass(V0[0], V0[4]);
+  b.c0 = std::sqrt(e.ComputeSoundSpeedSquare(V0[0], b.e0));   // the reference stops if c0^2 < 0
+  b.dpdrho0 = e.GetDpdrho(V0[0], b.e0);
+  b.Gamma0 = e.GetBigGamma(V0[0], b.e0);
+  b.kin0 = 0.5 * (V0[1] * V0[1] + V0[2] * V0[2] + V0[3] * V0[3]);
+  return b;
+}
+static void char_left(const CharBasis& b, const double* V0, int dir, double L[5][5]) {
+  double n[3] = {0, 0, 0};
+  n[dir] = 1.0;
+  const double un0 = V0[dir + 1];
+  const double alpha0 = V0[0] * b.Gamma0 / (V0[4] * b.Gamma0 + V0[0] * b.dpdrho0);
+  const double beta0 = (b.e0 - b.kin0 + V0[4] / V0[0]) * alpha0;
+  L[0][0] = 0.5 * (1.0 - beta0 + un0 / b.c0);
+  L[4][0] = 0.5 * (1.0 - beta0 - un0 / b.c0);
+  L[0][4] = L[4][4] = alpha0 / 2.0;
+  for (int i = 0; i < 3; i++) {
+    L[0][1 + i] = -0.5 * (alpha0 * V0[1 + i] + n[i] / b.c0);
+    L[4][1 + i] = -0.5 * (alpha0 * V0[1 + i] - n[i] / b.c0);
+    L[1 + i][0] = -V0[1 + i] + (beta0 + un0) * n[i];
+    L[1 + i][4] = -alpha0 * n[i];
+    for (int j = 0; j < 3; j++) L[1 + i][1 + j] = (i == j) + alpha0 * n[i] * V0[1 + j] - n[i] * n[j];
+  }
+}
+static void char_right(const CharBasis& b, const double* V0, int dir, double R[5][5]) {
+  double n[3] = {0, 0, 0};
+  n[dir] = 1.0;
+  const double un0 = V0[dir + 1];
+  const double H0 = b.e0 + b.kin0 + V0[4] / V0[0];
+  const double param = b.e0 + b.kin0 - b.dpdrho0 / b.Gamma0 - un0;
+  R[0][0] = 1.0;
+  R[0][4] = 1.0;
+  R[4][0] = H0 - un0 * b.c0;
+  R[4][4] = H0 + un0 * b.c0;
+  for (int i = 0; i < 3; i++) {
+    R[0][1 + i] = n[i];
+    R[1 + i][0] = V0[1 + i] - b.c0 * n[i];
+    R[1 + i][4] = V0[1 + i] + b.c0 * n[i];
+    R[4][1 + i] = V0[1 + i] + param * n[i];
+    for (int j = 0; j < 3; j++) R[1 + i][1 + j] = (i == j) + V0[1 + i] * n[j] - n[i] * n[j];
+  }
+}
+static void matvec5(const double M[5][5], const double* x, double* y) {
+  for (int i = 0; i < 5; i++) {
+    y[i] = 0.0;
+    for (int j = 0; j < 5; j++) y[i] += M[i][j] * x[j];
+  }
+}
+// FluxFcnBase.h:308-359
+static void PrimToPrimChar(const Eos& e, int dir, const double* V0, const double* dV, double* dW) {
+  CharBasis b = char_basis(e, V0);
+  const double Q0_51 = b.e0 + b.kin0 - b.dpdrho0 / b.Gamma0;
+  double t[5];
+  t[0] = dV[0];
+  t[1] = V0[1] * dV[0] + V0[0] * dV[1];
+  t[2] = V0[2] * dV[0] + V0[0] * dV[2];
+  t[3] = V0[3] * dV[0] + V0[0] * dV[3];
+  t[4] = Q0_51 * dV[0] + V0[0] * V0[1] * dV[1] + V0[0] * V0[2] * dV[2] + V0[0] * V0[3] * dV[3] + 1.0 / b.Gamma0 * dV[4];
+  double L[5][5];
+  char_left(b, V0, dir, L);
+  matvec5(L, t, dW);
+}
+// FluxFcnBase.h:364-420
+static void PrimCharToPrim(const Eos& e, int dir, const double* V0, const double* dW, double* dV) {
+  CharBasis b = char_basis(e, V0);
+  double R[5][5], t[5];
+  char_right(b, V0, dir, R);
+  matvec5(R, dW, t);
+  dV[0] = t[0];
+  dV[1] = -V0[1] / V0[0] * t[0] + t[1] / V0[0];
+  dV[2] = -V0[2] / V0[0] * t[0] + t[2] / V0[0];
+  dV[3] = -V0[3] / V0[0] * t[0] + t[3] / V0[0];
+  dV[4] = ((-b.e0 + b.kin0) * b.Gamma0 + b.dpdrho0) * t[0] - b.Gamma0 * (V0[1] * t[1] + V0[2] * t[2] + V0[3] * t[3] - t[4]);
+}
+// FluxFcnBase.h:424-467
+static void ConsToConsChar(const Eos& e, int dir, const double* V0, const double* dU, double* dW) {
+  CharBasis b = char_basis(e, V0);
+  double L[5][5];
+  char_left(b, V0, dir, L);
+  matvec5(L, dU, dW);
+}
+// FluxFcnBase.h:471-517
+static void ConsCharToCons(const Eos& e, int dir, const double* V0, const double* dW, double* dU) {
+  CharBasis b = char_basis(e, V0);
+  double R[5][5];
+  char_right(b, V0, dir, R);
+  matvec5(R, dW, dU);
+}
+
+// Reconstructor.cpp:335-918.  fs[0..5] = vl, vr, vb, vt, vk, vf (ghosted, AoS).
+// Slopes of primitive, conservative, primitive-characteristic or
+// conservative-characteristic differences; a nonphysical face state restarts
+// the cell with primitive variables, and in primitive variables the first
+// nonphysical face reverts to the cell value (Reconstructor.cpp:722-778).
 bool Oracle::Reconstruct(const std::vector<double>& v, const std::vector<int>& id, std::vector<double> fs[6]) {
   for (int f = 0; f < 6; f++) fs[f].assign(N() * 5, 0.0);
   const double A = 1.0, B = 1.0;   // uniform mesh: Reconstructor.cpp:78-84 give exactly 1
@@ -269,6 +372,20 @@ bool Oracle::Reconstruct(const std::vector<double>& v, const std::vector<int>& i
   }
   double alpha = cfg.minmod_coeff;
   int64_t sx = 5, sy = (int64_t)PX * 5, sz = (int64_t)PX * PY * 5;
+  const int var0 = cfg.rec_var;
+  // conservative state of the real and face-ghost cells, with each cell's own
+  // material (Reconstructor.cpp:400-408; edge and corner ghosts are not read)
+  std::vector<double> u;
+  if (cfg.rec_type != M2CG_REC_CONSTANT && (var0 == M2CG_VAR_CONSERVATIVE || var0 == M2CG_VAR_CONSERVATIVE_CHARACTERISTIC)) {
+    u.assign(N() * 5, 0.0);
+    for (int k = -1; k <= NZ; k++)
+      for (int j = -1; j <= NY; j++)
+        for (int i = -1; i <= NX; i++) {
+          if (nface_ghost(i, j, k) > 1) continue;
+          size_t c = idx(i, j, k);
+          vf[id[c]].PrimitiveToConservative(&v[c * 5], &u[c * 5]);
+        }
+  }
 #pragma omp parallel for schedule(static)
   for (int k = 0; k < NZ; k++)
     for (int j = 0; j < NY; j++)
@@ -279,39 +396,76 @@ bool Oracle::Reconstruct(const std::vector<double>& v, const std::vector<int>& i
           for (int f = 0; f < 6; f++) for (int p = 0; p < 5; p++) fs[f][c * 5 + p] = q[p];
           continue;
         }
-        double sig[3][5];
-        int64_t st[3] = {sx, sy, sz};
-        for (int d = 0; d < 3; d++)
-          for (int p = 0; p < 5; p++) {
-            double dq0 = q[p] - q[p - st[d]];
-            double dq1 = q[p + st[d]] - q[p];
-            double s;
-            if (cfg.limiter == M2CG_LIM_GENERALIZED_MINMOD) s = GenMinMod(A, B, alpha, dq0, dq1);
-            else if (cfg.limiter == M2CG_LIM_VANALBADA) s = VanAlbada(A, B, kay, dq0, dq1);
-            else s = 0.5 * (dq0 + dq1);
-            sig[d][p] = s;
-          }
-        if (cfg.slope_near_interface == M2CG_SLOPE_ZERO) {   // Reconstructor.cpp:649-658
-          size_t cs[3] = {1, (size_t)PX, (size_t)PX * PY};
-          for (int d = 0; d < 3; d++)
-            if (id[c] != id[c - cs[d]] || id[c] != id[c + cs[d]])
-              for (int p = 0; p < 5; p++) sig[d][p] = 0.0;
-        }
-        for (int p = 0; p < 5; p++) {   // Reconstructor.cpp:676-688
-          fs[0][c * 5 + p] = q[p] - 0.5 * sig[0][p];
-          fs[1][c * 5 + p] = q[p] + 0.5 * sig[0][p];
-          fs[2][c * 5 + p] = q[p] - 0.5 * sig[1][p];
-          fs[3][c * 5 + p] = q[p] + 0.5 * sig[1][p];
-          fs[4][c * 5 + p] = q[p] - 0.5 * sig[2][p];
-          fs[5][c * 5 + p] = q[p] + 0.5 * sig[2][p];
-        }
-        // Reconstructor.cpp:722-778: the first nonphysical face reverts to the cell value
         const Eos& e = vf[id[c]];
-        for (int f = 0; f < 6; f++) {
-          if (e.CheckState(&fs[f][c * 5])) {
-            for (int p = 0; p < 5; p++) fs[f][c * 5 + p] = q[p];
+        int vt = var0;
+        while (true) {
+          const bool cons = (vt == M2CG_VAR_CONSERVATIVE || vt == M2CG_VAR_CONSERVATIVE_CHARACTERISTIC);
+          const double* w = cons ? &u[c * 5] : q;   // the variables whose differences are limited
+          double sig[3][5];
+          int64_t st[3] = {sx, sy, sz};
+          for (int d = 0; d < 3; d++) {
+            double dq0[5], dq1[5];
+            for (int p = 0; p < 5; p++) {
+              dq0[p] = w[p] - w[p - st[d]];
+              dq1[p] = w[p + st[d]] - w[p];
+            }
+            if (vt == M2CG_VAR_PRIMITIVE_CHARACTERISTIC) {
+              double t[5];
+              PrimToPrimChar(e, d, q, dq0, t); for (int p = 0; p < 5; p++) dq0[p] = t[p];
+              PrimToPrimChar(e, d, q, dq1, t); for (int p = 0; p < 5; p++) dq1[p] = t[p];
+            } else if (vt == M2CG_VAR_CONSERVATIVE_CHARACTERISTIC) {
+              double t[5];
+              ConsToConsChar(e, d, q, dq0, t); for (int p = 0; p < 5; p++) dq0[p] = t[p];
+              ConsToConsChar(e, d, q, dq1, t); for (int p = 0; p < 5; p++) dq1[p] = t[p];
+            }
+            for (int p = 0; p < 5; p++) {
+              double s;
+              if (cfg.limiter == M2CG_LIM_GENERALIZED_MINMOD) s = GenMinMod(A, B, alpha, dq0[p], dq1[p]);
+              else if (cfg.limiter == M2CG_LIM_VANALBADA) s = VanAlbada(A, B, kay, dq0[p], dq1[p]);
+              else s = 0.5 * (dq0[p] + dq1[p]);
+              sig[d][p] = s;
+            }
+          }
+          // Reconstructor.cpp:620-644: back to primitive / conservative differences
+          for (int d = 0; d < 3; d++) {
+            double t[5];
+            if (vt == M2CG_VAR_PRIMITIVE_CHARACTERISTIC) PrimCharToPrim(e, d, q, sig[d], t);
+            else if (vt == M2CG_VAR_CONSERVATIVE_CHARACTERISTIC) ConsCharToCons(e, d, q, sig[d], t);
+            else continue;
+            for (int p = 0; p < 5; p++) sig[d][p] = t[p];
+          }
+          if (cfg.slope_near_interface == M2CG_SLOPE_ZERO) {   // Reconstructor.cpp:649-658
+            size_t cs[3] = {1, (size_t)PX, (size_t)PX * PY};
+            for (int d = 0; d < 3; d++)
+              if (id[c] != id[c - cs[d]] || id[c] != id[c + cs[d]])
+                for (int p = 0; p < 5; p++) sig[d][p] = 0.0;
+          }
+          if (!cons) {
+            for (int p = 0; p < 5; p++) {   // Reconstructor.cpp:676-688
+              fs[0][c * 5 + p] = q[p] - 0.5 * sig[0][p];
+              fs[1][c * 5 + p] = q[p] + 0.5 * sig[0][p];
+              fs[2][c * 5 + p] = q[p] - 0.5 * sig[1][p];
+              fs[3][c * 5 + p] = q[p] + 0.5 * sig[1][p];
+              fs[4][c * 5 + p] = q[p] - 0.5 * sig[2][p];
+              fs[5][c * 5 + p] = q[p] + 0.5 * sig[2][p];
+            }
+          } else {                          // Reconstructor.cpp:689-716
+            for (int f = 0; f < 6; f++) {
+              double u2[5];
+              for (int p = 0; p < 5; p++) u2[p] = (f % 2 == 0) ? w[p] - 0.5 * sig[f / 2][p] : w[p] + 0.5 * sig[f / 2][p];
+              e.ConservativeToPrimitive(u2, &fs[f][c * 5]);
+            }
+          }
+          // Reconstructor.cpp:722-778
+          int bad = -1;
+          for (int f = 0; f < 6 && bad < 0; f++)
+            if (e.CheckState(&fs[f][c * 5])) bad = f;
+          if (bad < 0) break;
+          if (vt == M2CG_VAR_PRIMITIVE) {
+            for (int p = 0; p < 5; p++) fs[bad][c * 5 + p] = q[p];
             break;
           }
+          vt = M2CG_VAR_PRIMITIVE;
         }
       }
   // Ghost faces by boundary condition, Reconstructor.cpp:807-889
@@ -951,6 +1105,17 @@ void orc_download(void* h, double* V, int32_t* id, double* phi) {
         if (id) id[n] = o->ID[c];
         if (phi) phi[n] = o->Phi[c];
       }
+}
+
+// The ghosted arrays (ghost width 1, i fastest): V as 5 planes, id, phi.
+void orc_download_ghosted(void* h, double* V, int32_t* id, double* phi) {
+  Oracle* o = (Oracle*)h;
+  const size_t n = o->N();
+  for (size_t c = 0; c < n; c++) {
+    if (V) for (int p = 0; p < 5; p++) V[(size_t)p * n + c] = o->V[c * 5 + p];
+    if (id) id[c] = o->ID[c];
+    if (phi) phi[c] = o->Phi[c];
+  }
 }
 
 void orc_residual(void* h, double* Rout) {
