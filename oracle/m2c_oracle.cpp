@@ -11,7 +11,9 @@
 //   SpaceOperator::ApplyBoundaryConditions  SpaceOperator.cpp:738-821
 //   SpaceOperator::ClipDensityAndPressure   SpaceOperator.cpp:647-693
 //   SpaceOperator::ComputeTimeStepSize      SpaceOperator.cpp:1223-1330
-//   Reconstructor::Reconstruct (primitive)  Reconstructor.cpp:335-918, limiters Reconstructor.h:96-111
+//   Reconstructor::Reconstruct              Reconstructor.cpp:335-918 (all four variable types), limiters
+//                                           Reconstructor.h:96-111, characteristic transforms FluxFcnBase.h:308-517
+//   LevelSetReinitializer (full, FIXED)     LevelSetReinitializer.cpp:76-176, 304-437, 601-623, 960-1041, 1966-1991
 //   LevelSetOperator FD residual + BCs      LevelSetOperator.cpp:796-870, 408-508
 //   GradientCalculatorFD3 coefficients      GradientCalculatorFD3.cpp:300-470
 //   TimeIntegratorFE/RK2/RK3                TimeIntegrator.cpp:167-250, 319-455, 527-715
