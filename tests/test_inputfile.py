@@ -264,3 +264,18 @@ def test_gpu_reconstruction_variants_one_step_match_oracle(var, flux):
     e = rel_linf(g.V, Vo)
     assert e[0] < 1e-10 and e[4] < 1e-10, e
     assert rel_linf(g.Phi, po) < 1e-10
+
+
+def test_vtr_snapshot_round_trip(tmp_path):
+    from m2c_gb300 import output
+    cs = inf.Case.from_text(CASE)
+    ser = output.SolutionSeries(str(tmp_path) + "/", "solution")
+    ser.write(cs.cfg, cs.V, cs.ID, cs.phi, 0.0)
+    ser.write(cs.cfg, cs.V * 2, cs.ID, cs.phi, 1.5e-4)
+    back = output.read_vtr(str(tmp_path / "solution_0001.vtr"))
+    np.testing.assert_array_equal(back["density"], 2 * cs.V[:, 0])
+    np.testing.assert_array_equal(back["velocity"], 2 * cs.V[:, 1:4])
+    np.testing.assert_array_equal(back["materialid"], cs.ID)
+    np.testing.assert_array_equal(back["levelset0"], cs.phi)
+    pvd = (tmp_path / "solution.pvd").read_text()
+    assert 'timestep="1.500000e-04" file="solution_0001.vtr"' in pvd
