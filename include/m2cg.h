@@ -56,6 +56,9 @@ enum { M2CG_SLOPE_ZERO = 0, M2CG_SLOPE_NONZERO = 1 };
 /* Reconstruction.VariableType (IoData.cpp:1300-1304). */
 enum { M2CG_VAR_PRIMITIVE = 0, M2CG_VAR_CONSERVATIVE = 1, M2CG_VAR_PRIMITIVE_CHARACTERISTIC = 2,
        M2CG_VAR_CONSERVATIVE_CHARACTERISTIC = 3 };
+/* Level-set solver and finite-volume flux (LevelSetSchemeData, IoData.cpp:1544-1556). */
+enum { M2CG_LS_FINITE_VOLUME = 0, M2CG_LS_FINITE_DIFFERENCE = 1 };
+enum { M2CG_LSFLUX_ROE = 0, M2CG_LSFLUX_LLF = 1, M2CG_LSFLUX_UPWIND = 2 };
 /* Multiphase (MultiPhaseData, IoData.h:893-903). */
 enum { M2CG_MPFLUX_EXACT = 0, M2CG_MPFLUX_NUMERICAL = 1, M2CG_MPFLUX_LLF = 2 };
 enum { M2CG_MPREC_CONSTANT = 0, M2CG_MPREC_LINEAR = 1 };
@@ -129,6 +132,13 @@ typedef struct {
   int32_t pad4_;
   double reinit_cfl;           /* CFL (0.8) */
   double reinit_tol;           /* ConvergenceTolerance (2e-4) */
+  /* LevelSet[0] solver and its own reconstruction (LevelSetSchemeData, IoData.cpp:1513-1590) */
+  int32_t ls_solver;           /* Solver: M2CG_LS_FINITE_VOLUME / M2CG_LS_FINITE_DIFFERENCE (default) */
+  int32_t ls_flux;             /* Flux (finite volume): M2CG_LSFLUX_* (default Roe) */
+  double ls_delta;             /* EntropyFixCoefficient of the Roe flux (0.2) */
+  int32_t ls_rec_type;         /* Reconstruction.Type (default Linear) */
+  int32_t ls_limiter;          /* Reconstruction.Limiter (default GeneralizedMinMod) */
+  double ls_minmod_coeff;      /* Reconstruction.GeneralizedMinModCoefficient (1.2) */
 } m2cg_config;
 
 /* Per-step counters (the reference prints these as warnings; SpaceOperator.cpp:681-683,

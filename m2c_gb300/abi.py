@@ -28,6 +28,8 @@ MPREC_CONSTANT, MPREC_LINEAR = 0, 1
 PHASECHANGE_RIEMANN, PHASECHANGE_EXTRAPOLATION = 0, 1
 PCDIR_ALL, PCDIR_UPWIND = 0, 1
 TS_FORWARD_EULER, TS_RK2, TS_RK3 = 0, 1, 2
+LS_FINITE_VOLUME, LS_FINITE_DIFFERENCE = 0, 1
+LSFLUX_ROE, LSFLUX_LLF, LSFLUX_UPWIND = 0, 1, 2
 
 STATUS = {0: "OK", 1: "INVALID_ARG", 2: "CUDA", 3: "NONPHYSICAL", 4: "UNRESOLVED",
           5: "NO_DEVICE", 6: "CAPACITY"}
@@ -64,7 +66,9 @@ class Config(C.Structure):
                 ("ts_type", C.c_int32), ("max_its", C.c_int32),
                 ("cfl", C.c_double), ("timestep", C.c_double), ("max_time", C.c_double),
                 ("warm_start", C.c_int32), ("reinit_frequency", C.c_int32), ("reinit_max_its", C.c_int32),
-                ("pad4_", C.c_int32), ("reinit_cfl", C.c_double), ("reinit_tol", C.c_double)]
+                ("pad4_", C.c_int32), ("reinit_cfl", C.c_double), ("reinit_tol", C.c_double),
+                ("ls_solver", C.c_int32), ("ls_flux", C.c_int32), ("ls_delta", C.c_double),
+                ("ls_rec_type", C.c_int32), ("ls_limiter", C.c_int32), ("ls_minmod_coeff", C.c_double)]
 
 
 class Counters(C.Structure):
@@ -123,6 +127,8 @@ def default_config():
     c.max_time = 1e10
     c.warm_start = 0
     c.reinit_frequency, c.reinit_max_its, c.reinit_cfl, c.reinit_tol = -1, 30, 0.8, 2.0e-4
+    c.ls_solver, c.ls_flux, c.ls_delta = LS_FINITE_DIFFERENCE, LSFLUX_ROE, 0.2
+    c.ls_rec_type, c.ls_limiter, c.ls_minmod_coeff = REC_LINEAR, LIM_GENERALIZED_MINMOD, 1.2
     return c
 
 

@@ -194,6 +194,14 @@ m2cg_status m2cg_fill_params(const m2cg_config& c, m2cg::Params& P) {
   }
   P.flux = c.flux; P.rec_type = c.rec_type; P.limiter = c.limiter; P.slope_zero = (c.slope_near_interface == M2CG_SLOPE_ZERO);
   P.rec_var = c.rec_var;
+  P.ls_fv = (c.n_levelsets > 0 && c.ls_solver == M2CG_LS_FINITE_VOLUME);
+  P.ls_flux = c.ls_flux; P.ls_rec_linear = (c.ls_rec_type == M2CG_REC_LINEAR); P.ls_limiter = c.ls_limiter;
+  P.ls_delta = c.ls_delta; P.ls_minmod = c.ls_minmod_coeff;
+  if (c.ls_solver != M2CG_LS_FINITE_VOLUME && c.ls_solver != M2CG_LS_FINITE_DIFFERENCE) { set_err("bad level-set solver"); return M2CG_ERR_INVALID_ARG; }
+  if (P.ls_fv && c.ts_type == M2CG_TS_FORWARD_EULER) {
+    set_err("the finite-volume level set is supported with the RK2 and RK3 integrators");
+    return M2CG_ERR_INVALID_ARG;
+  }
   P.mp_flux = c.mp_flux; P.mp_recon = c.mp_recon; P.mp_phasechange = c.mp_phasechange; P.mp_pcdir = c.mp_phasechange_dir;
   P.minmod_coeff = c.minmod_coeff; P.roe_delta = c.roe_delta;
   for (int s = 0; s < 6; s++) { P.bc[s] = c.bc[s]; P.ls_bc[s] = c.ls_bc[s]; }
@@ -377,6 +385,10 @@ static int64_t enqueue_stage(m2cg_ctx* x, int stage, bool last, const StateSet& 
   PHASE(PH_FLUX, launch_face_flux(s, P, x->id, x->d_fs, x->d_F, x->cnt)); n++;
   cudaStreamWaitEvent(s, x->ev_join, 0);
   StageArgs A = stage_args(x, stage, last, in, out);
+  if (P.ls_fv) {   // the finite-volume level-set residual of the stage input
+    PHASE(PH_UPDATE, launch_ls_residual(s, P, in, x->rphi)); n++;
+    A.rls_pre = x->rphi;
+  }
   PHASE(PH_UPDATE, launch_update(s, P, A, x->id, x->id_new, x->d_F, x->L, x->sc, x->swept, x->swept_count,
                                   x->swept_cap, x->cnt)); n++;
   if (!last) { PHASE(PH_BC, launch_bc(s, P, out, 1, 1, nullptr, x->sc)); n++; }
@@ -458,6 +470,12 @@ m2cg_status m2cg_config_default(m2cg_config* c) {
   c->reinit_max_its = 30;
   c->reinit_cfl = 0.8;
   c->reinit_tol = 2.0e-4;
+  c->ls_solver = M2CG_LS_FINITE_DIFFERENCE;   // IoData.cpp:1513-1535, 1265-1274
+  c->ls_flux = M2CG_LSFLUX_ROE;
+  c->ls_delta = 0.2;
+  c->ls_rec_type = M2CG_REC_LINEAR;
+  c->ls_limiter = M2CG_LIM_GENERALIZED_MINMOD;
+  c->ls_minmod_coeff = 1.2;
   return M2CG_OK;
 }
 
@@ -1258,6 +1276,10 @@ m2cg_status m2cg_ensemble_create(const m2cg_config* cfgs, int32_t n, m2cg_ensemb
   for (int d = 0; d < n; d++) {
     if (cfgs[d].rec_var != M2CG_VAR_PRIMITIVE) {
       set_err("member %d: the batched step reconstructs primitive variables only", d);
+      return M2CG_ERR_INVALID_ARG;
+    }
+    if (cfgs[d].n_levelsets > 0 && cfgs[d].ls_solver == M2CG_LS_FINITE_VOLUME) {
+      set_err("member %d: the batched step advects the level set by finite differences only", d);
       return M2CG_ERR_INVALID_ARG;
     }
     if (cfgs[d].n_levelsets > 0 && cfgs[d].reinit_frequency > 0) {

@@ -75,6 +75,9 @@ struct Params {
   double inlet[5], inlet2[5];
   int n_ls, ls_matid;
   int ls_bc[6];
+  int ls_fv;            // finite-volume level set (else finite difference)
+  int ls_flux, ls_rec_linear, ls_limiter;
+  double ls_delta, ls_minmod;
   RiemannPrm rp;
   double area[3];
   double inv_negvol;
@@ -154,6 +157,7 @@ struct StageArgs {
   double la, lb, lc;          // phi = la*phi_own_other + lb*phi_n + lc*dt*R (see kernel)
   int ls_use_updated_v;       // forward Euler: level set advected with the updated velocity
   double* R[5];               // residual output (residual-only mode)
+  const double* rls_pre;      // level-set residual computed beforehand (finite volume), else NULL
   int residual_only;
 };
 

@@ -525,7 +525,7 @@ __device__ __forceinline__ void k_update_body(const Params& P, const StageArgs& 
     double vel[3];
     if (A.ls_use_updated_v) { vel[0] = V[1]; vel[1] = V[2]; vel[2] = V[3]; }
     else { vel[0] = A.in.q[1][c]; vel[1] = A.in.q[2][c]; vel[2] = A.in.q[3][c]; }
-    double rls = ls_residual(P, A.phi_lsin, c, i, j, k, vel);
+    double rls = A.rls_pre ? A.rls_pre[c] : ls_residual(P, A.phi_lsin, c, i, j, k, vel);
     double ph;
     double phin = A.phi_tmp[c];
     if (A.stage == 0) ph = A.phi_own[c] + dt * rls;
@@ -561,10 +561,91 @@ __global__ void k_update_ens(const k_update_args* __restrict__ ea, const int64_t
 
 
 // Level-set residual only (LevelSetOperator::ComputeResidual).
+// ---------------------------------------------------------------------------
+// Finite-volume level set at one real cell (LevelSetOperator.cpp:966-1136,
+// 1265-1324): face values from the level set's own reconstruction -- each
+// velocity component along its direction (Reconstructor.cpp:922-1176) and phi
+// (Reconstructor.cpp:335-918 with one DOF) -- for the cell and its neighbours,
+// the neighbours beyond the boundary taking the ghost cells' inward values by
+// boundary type; R = (F_lo,x + G_lo,y + H_lo,z - F_hi,x - G_hi,y - H_hi,z) +
+// phi div(u), the reference's accumulation order.
+__device__ __forceinline__ double ls_limit(const Params& P, double dq0, double dq1) {
+  if (!P.ls_rec_linear) return 0.0;
+  if (P.ls_limiter == M2CG_LIM_GENERALIZED_MINMOD) return gen_minmod(P.ls_minmod, dq0, dq1);
+  if (P.ls_limiter == M2CG_LIM_VANALBADA) return van_albada_fast(dq0, dq1);
+  return 0.5 * (dq0 + dq1);
+}
+__device__ __forceinline__ double ls_slope(const Params& P, const double* __restrict__ q, int64_t c, int64_t s) {
+  return ls_limit(P, q[c] - q[c - s], q[c + s] - q[c]);
+}
+__device__ __forceinline__ double ls_fv_flux(const Params& P, double phim, double phip, double um, double up) {
+  if (P.ls_flux == M2CG_LSFLUX_UPWIND) {
+    const double vmid = 0.5 * (um + up);
+    if (vmid > 0) return phim * um;
+    if (vmid < 0) return phip * up;
+    return 0.5 * (phim * um + phip * up);
+  }
+  if (P.ls_flux == M2CG_LSFLUX_LLF) return 0.5 * (phim * um + phip * up) - 0.5 * fmax(fabs(um), fabs(up)) * (phip - phim);
+  double lam = fabs(0.5 * (um + up));
+  const double tol = fmax(fabs(um), fabs(up)) * P.ls_delta;
+  if (lam < tol) lam = (lam * lam + tol * tol) / (2 * tol);
+  return 0.5 * (phim * um + phip * up) - 0.5 * lam * (phip - phim);
+}
+__device__ __forceinline__ double ls_fv_residual(const Params& P, const StateSet& S, int64_t c, int i, int j, int k) {
+  const Grid& g = P.g;
+  const int64_t st[3] = {1, g.sy, g.sz};
+  const int pos[3] = {i, j, k};
+  const int n[3] = {g.nx, g.ny, g.nz};
+  const double h[3] = {g.dx, g.dy, g.dz};
+  const double* __restrict__ phi = S.q[5];
+  double flo[3], fhi[3], div = 0.0;
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    const double* __restrict__ u = S.q[1 + d];
+    const int64_t s = st[d];
+    const double su = ls_slope(P, u, c, s), sp = ls_slope(P, phi, c, s);
+    div += su / h[d];
+    const double u_m = u[c] - 0.5 * su, u_p = u[c] + 0.5 * su;
+    const double p_m = phi[c] - 0.5 * sp, p_p = phi[c] + 0.5 * sp;
+    double nu, np;
+    if (pos[d] > 0) {
+      nu = u[c - s] + 0.5 * ls_slope(P, u, c - s, s);
+      np = phi[c - s] + 0.5 * ls_slope(P, phi, c - s, s);
+    } else {   // the low ghost's inward values; its image is this cell
+      const int bc = P.bc[2 * d];
+      const bool inlet = (bc == M2CG_BC_INLET || bc == M2CG_BC_INLET2);
+      nu = inlet ? u[c - s] : (bc == M2CG_BC_OUTLET ? u_m : -u_m);
+      np = (inlet || !P.ls_rec_linear) ? phi[c - s] : p_m;
+    }
+    flo[d] = ls_fv_flux(P, np, p_m, nu, u_m) / h[d];
+    if (pos[d] < n[d] - 1) {
+      nu = u[c + s] - 0.5 * ls_slope(P, u, c + s, s);
+      np = phi[c + s] - 0.5 * ls_slope(P, phi, c + s, s);
+    } else {   // the high ghost's inward values
+      const int bc = P.bc[2 * d + 1];
+      const bool inlet = (bc == M2CG_BC_INLET || bc == M2CG_BC_INLET2);
+      nu = inlet ? u[c + s] : (bc == M2CG_BC_OUTLET ? u_p : -u_p);
+      np = (inlet || !P.ls_rec_linear) ? phi[c + s] : p_p;
+    }
+    fhi[d] = ls_fv_flux(P, p_p, np, u_p, nu) / h[d];
+  }
+  double r = flo[0];
+  r += flo[1];
+  r += flo[2];
+  r -= fhi[0];
+  r -= fhi[1];
+  r -= fhi[2];
+  return r + phi[c] * div;
+}
+
 __global__ void k_ls_residual(Params P, StateSet S, double* __restrict__ out) {
   int i, j, k;
   if (!real_cell(P.g, (int64_t)blockIdx.x * blockDim.x + threadIdx.x, i, j, k)) return;
   int64_t c = P.g.at(i, j, k);
+  if (P.ls_fv) {
+    out[c] = ls_fv_residual(P, S, c, i, j, k);
+    return;
+  }
   double vel[3] = {S.q[1][c], S.q[2][c], S.q[3][c]};
   out[c] = ls_residual(P, S.q[5], c, i, j, k, vel);
 }

@@ -20,8 +20,8 @@ plots that go with them.
   the mean of the populated corners, output in the reference's format.
 
 Anything the path does not implement (other EOS, non-uniform meshes, other
-geometric entities, the finite-volume level-set solver, narrow bands, other
-reinitialization treatments) raises NotImplementedError naming the key.
+geometric entities, narrow bands, other reinitialization treatments) raises
+NotImplementedError naming the key.
 """
 import math
 import re
@@ -230,6 +230,8 @@ _PC = {"RiemannSolution": abi.PHASECHANGE_RIEMANN, "Extrapolation": abi.PHASECHA
 _PCDIR = {"All": abi.PCDIR_ALL, "Upwind": abi.PCDIR_UPWIND}
 _TS = {"ForwardEuler": abi.TS_FORWARD_EULER, "RungeKutta2": abi.TS_RK2, "RungeKutta3": abi.TS_RK3}
 _EOS = {"StiffenedGas": abi.EOS_SG, "NobleAbelStiffenedGas": abi.EOS_NASG, "MieGruneisen": abi.EOS_MG}
+_LSSOLVER = {"FiniteVolume": abi.LS_FINITE_VOLUME, "FiniteDifference": abi.LS_FINITE_DIFFERENCE}   # IoData.cpp:1544-1547
+_LSFLUX = {"Roe": abi.LSFLUX_ROE, "LocalLaxFriedrichs": abi.LSFLUX_LLF, "Upwind": abi.LSFLUX_UPWIND}
 
 
 def _int_keys(t):
@@ -351,8 +353,15 @@ class Case:
             d = ls[min(ls)]
             c.n_levelsets = 1
             c.ls_matid = int(d.get("MaterialID", 1))
-            if d.get("Solver", "FiniteDifference") != "FiniteDifference":
-                raise NotImplementedError(f"LevelSet.Solver = {d['Solver']}")
+            c.ls_solver = _tok(_LSSOLVER, d.get("Solver", "FiniteDifference"), "LevelSet.Solver")
+            c.ls_flux = _tok(_LSFLUX, d.get("Flux", "Roe"), "LevelSet.Flux")
+            if "EntropyFixCoefficient" in d:
+                c.ls_delta = float(d["EntropyFixCoefficient"])
+            lrec = d.get("Reconstruction", {})
+            c.ls_rec_type = _tok(_REC, lrec.get("Type", "Linear"), "LevelSet.Reconstruction.Type")
+            c.ls_limiter = _tok(_LIM, lrec.get("Limiter", "GeneralizedMinMod"), "LevelSet.Reconstruction.Limiter")
+            if "GeneralizedMinModCoefficient" in lrec:
+                c.ls_minmod_coeff = float(lrec["GeneralizedMinModCoefficient"])
             if int(d.get("Bandwidth", 2 ** 31 - 1)) < 2 ** 31 - 1:
                 raise NotImplementedError("narrow-band level set (LevelSet.Bandwidth)")
             if d.get("Initialization", "DistanceCalculation") != "DistanceCalculation":

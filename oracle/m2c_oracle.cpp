@@ -81,6 +81,7 @@ struct Oracle {
   void CheckReconstructed(const std::vector<double>& v, const std::vector<int>& id, std::vector<double> fs[6]);
   void ComputeResidual(const std::vector<double>& v, const std::vector<int>& id, std::vector<double>& R, bool store);
   void LevelSetResidual(const std::vector<double>& v, const std::vector<double>& phi, std::vector<double>& R);
+  void LevelSetResidualFV(const std::vector<double>& v, const std::vector<double>& phi, std::vector<double>& R);
   void ComputeDt(const std::vector<double>& v, const std::vector<int>& id, double& dt, double& cfl);
   void Advance(double dt);
   void P2C(const std::vector<double>& v, const std::vector<int>& id, std::vector<double>& u);
@@ -638,8 +639,119 @@ void Oracle::ComputeResidual(const std::vector<double>& v, const std::vector<int
       }
 }
 
+// LevelSetOperator::ComputeLocalAdvectionFlux (LevelSetOperator.cpp:1265-1296)
+static double LsFlux(int type, double delta, double phim, double phip, double um, double up) {
+  if (type == M2CG_LSFLUX_UPWIND) {
+    double vmid = 0.5 * (um + up);
+    if (vmid > 0) return phim * um;
+    if (vmid < 0) return phip * up;
+    return 0.5 * (phim * um + phip * up);
+  }
+  if (type == M2CG_LSFLUX_LLF)
+    return 0.5 * (phim * um + phip * up) - 0.5 * std::max(std::fabs(um), std::fabs(up)) * (phip - phim);
+  double lam = std::fabs(0.5 * (um + up));
+  double tol = std::max(std::fabs(um), std::fabs(up)) * delta;
+  if (lam < tol) lam = (lam * lam + tol * tol) / (2 * tol);
+  return 0.5 * (phim * um + phip * up) - 0.5 * lam * (phip - phim);
+}
+
+// Finite-volume level set (LevelSetOperator.cpp:966-1136, 1265-1324): the
+// level set's own reconstructor gives face values of each velocity component
+// along its direction (Reconstructor::ReconstructIn1D, Reconstructor.cpp:922-1176)
+// and of phi in all directions (Reconstructor::Reconstruct with one DOF and no
+// material IDs, Reconstructor.cpp:335-918); boundary faces take the ghost
+// cells' inward values by boundary type; R = sum of the face fluxes (in the
+// reference's loop order) + phi div(u).
+void Oracle::LevelSetResidualFV(const std::vector<double>& v, const std::vector<double>& phi, std::vector<double>& R) {
+  const size_t n = N();
+  const double h[3] = {dx, dy, dz};
+  const size_t cs[3] = {1, (size_t)PX, (size_t)PX * PY};
+  const bool linear = (cfg.ls_rec_type == M2CG_REC_LINEAR);
+  auto limit = [&](double dq0, double dq1) {
+    if (cfg.ls_limiter == M2CG_LIM_GENERALIZED_MINMOD) return GenMinMod(1.0, 1.0, cfg.ls_minmod_coeff, dq0, dq1);
+    if (cfg.ls_limiter == M2CG_LIM_VANALBADA) return VanAlbada(1.0, 1.0, 2, dq0, dq1);
+    return 0.5 * (dq0 + dq1);
+  };
+  std::vector<double> um[3], up[3], slope[3], pf[6];
+  for (int d = 0; d < 3; d++) { um[d].assign(n, 0.0); up[d].assign(n, 0.0); slope[d].assign(n, 0.0); }
+  for (int f = 0; f < 6; f++) pf[f].assign(n, 0.0);
+  // real cells
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < NX; i++) {
+        size_t c = idx(i, j, k);
+        for (int d = 0; d < 3; d++) {
+          const double* u = &v[1 + d];   // velocity component d, stride 5
+          double sig = 0.0;
+          if (linear) sig = limit(u[c * 5] - u[(c - cs[d]) * 5], u[(c + cs[d]) * 5] - u[c * 5]);
+          um[d][c] = u[c * 5] - 0.5 * sig;
+          up[d][c] = u[c * 5] + 0.5 * sig;
+          slope[d][c] = sig / h[d];
+          double sp = 0.0;
+          if (linear) sp = limit(phi[c] - phi[c - cs[d]], phi[c + cs[d]] - phi[c]);
+          pf[2 * d][c] = phi[c] - 0.5 * sp;
+          pf[2 * d + 1][c] = phi[c] + 0.5 * sp;
+        }
+      }
+  // face-ghost cells: the inward face values
+  for (int k = -1; k <= NZ; k++)
+    for (int j = -1; j <= NY; j++)
+      for (int i = -1; i <= NX; i++) {
+        if (nface_ghost(i, j, k) != 1) continue;
+        int side = (i < 0) ? 0 : (i >= NX) ? 1 : (j < 0) ? 2 : (j >= NY) ? 3 : (k < 0) ? 4 : 5;
+        int ii = i < 0 ? 0 : i >= NX ? NX - 1 : i;
+        int jj = j < 0 ? 0 : j >= NY ? NY - 1 : j;
+        int kk = k < 0 ? 0 : k >= NZ ? NZ - 1 : k;
+        size_t g = idx(i, j, k), im = idx(ii, jj, kk);
+        int d = side / 2;
+        bool low = (side % 2 == 0);
+        int bc = cfg.bc[side];
+        const double ug = v[g * 5 + 1 + d];
+        // velocity along d (Reconstructor.cpp:1056-1152)
+        double& uin = low ? up[d][g] : um[d][g];
+        const double uimg = low ? um[d][im] : up[d][im];
+        if (bc == M2CG_BC_INLET || bc == M2CG_BC_INLET2) uin = ug;
+        else if (bc == M2CG_BC_OUTLET) uin = uimg;
+        else uin = -uimg;
+        // phi (Reconstructor.cpp:807-889; with one DOF the walls' sign flip touches nothing)
+        double& pin = pf[low ? 2 * d + 1 : 2 * d][g];
+        if (!linear || bc == M2CG_BC_INLET || bc == M2CG_BC_INLET2) pin = phi[g];
+        else pin = pf[low ? 2 * d : 2 * d + 1][im];
+      }
+  // fluxes over the interior and the upper ghost layers (LevelSetOperator.cpp:1091-1122)
+  std::vector<double> res(n, 0.0);
+  for (int k = 0; k <= NZ; k++)
+    for (int j = 0; j <= NY; j++)
+      for (int i = 0; i <= NX; i++) {
+        size_t c = idx(i, j, k);
+        if (k != NZ && j != NY) {
+          double f = LsFlux(cfg.ls_flux, cfg.ls_delta, pf[1][c - cs[0]], pf[0][c], up[0][c - cs[0]], um[0][c]) / h[0];
+          res[c - cs[0]] -= f;
+          res[c] += f;
+        }
+        if (k != NZ && i != NX) {
+          double f = LsFlux(cfg.ls_flux, cfg.ls_delta, pf[3][c - cs[1]], pf[2][c], up[1][c - cs[1]], um[1][c]) / h[1];
+          res[c - cs[1]] -= f;
+          res[c] += f;
+        }
+        if (j != NY && i != NX) {
+          double f = LsFlux(cfg.ls_flux, cfg.ls_delta, pf[5][c - cs[2]], pf[4][c], up[2][c - cs[2]], um[2][c]) / h[2];
+          res[c - cs[2]] -= f;
+          res[c] += f;
+        }
+      }
+  R.assign(n, 0.0);
+  for (int k = 0; k < NZ; k++)
+    for (int j = 0; j < NY; j++)
+      for (int i = 0; i < NX; i++) {
+        size_t c = idx(i, j, k);
+        R[c] = res[c] + phi[c] * (slope[0][c] + slope[1][c] + slope[2][c]);   // LevelSetOperator.cpp:1300-1324
+      }
+}
+
 // LevelSetOperator.cpp:796-870 (full domain, finite difference)
 void Oracle::LevelSetResidual(const std::vector<double>& v, const std::vector<double>& phi, std::vector<double>& R) {
+  if (cfg.ls_solver == M2CG_LS_FINITE_VOLUME) { LevelSetResidualFV(v, phi, R); return; }
   R.assign(N(), 0.0);
   double h[3] = {dx, dy, dz};
   size_t cs[3] = {1, (size_t)PX, (size_t)PX * PY};

@@ -5,14 +5,15 @@ tests/golden/make_riemann_lines.py).
 
 The line plots pin the whole step -- reconstruction in all four variable
 types, HLLC / generalized Roe / LLF fluxes, SG and Mie-Grueneisen materials,
-RK2 and RK3, the exact interface Riemann solver, the level set (with
-reinitialization in Test3) and the end-of-step material update -- against
+RK2 and RK3, the exact interface Riemann solver, the finite-difference and
+finite-volume level set (with reinitialization in Test3) and the end-of-step
+material update by Riemann solutions or extrapolation -- against
 the reference's outputs: the same number of steps and the same values to
 within 1e-6 of each field's maximum.  Test11 and Test12 drive air to
 near-vacuum with pressure clipping; a 1e-14 relative change of the initial
 density moves their final state by 2-3e-2 (and Test11's step count by 2), so
-they are held to that band.  Test4 uses the finite-volume level-set solver,
-which this path does not implement."""
+they are held to that band.  Test4 advects the level set by the
+finite-volume solver."""
 import json
 import os
 
@@ -22,7 +23,7 @@ import pytest
 from m2c_gb300 import abi, inputfile as inf
 
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden", "riemann_lines.json")
-PINNED = ["Test1", "Test2", "Test3", "Test5", "Test6", "Test8", "Test9", "Test10"]
+PINNED = ["Test1", "Test2", "Test3", "Test4", "Test5", "Test6", "Test8", "Test9", "Test10"]
 CHAOTIC = ["Test11", "Test12"]
 
 
@@ -112,7 +113,7 @@ def test_case_configuration_and_initial_state():
 
 
 def test_unsupported_keys_are_refused():
-    for bad in ("under Space { under LevelSet[0] { Solver = FiniteVolume; } }",
+    for bad in ("under Space { under LevelSet[0] { Bandwidth = 6; } }",
                 "under Equations { under Material[0] { EquationOfState = JonesWilkinsLee; } }",
                 "under InitialCondition { under GeometricEntities { under Parallelepiped[0] { X0 = 1; } } }"):
         with pytest.raises(NotImplementedError):
@@ -180,11 +181,6 @@ def test_oracle_chaotic_line_plots_within_their_sensitivity(name):
     assert abs(cnt["time"] - case["time"]) <= 1e-12 * case["time"]
     err = line_errors(rows, case)
     assert max(err[k] for k in ("rho", "vx", "p", "phi")) < 0.1, err
-
-
-def test_finite_volume_level_set_case_is_refused():
-    with pytest.raises(NotImplementedError):
-        inf.Case.from_tree(golden()["Test4"]["tree"])
 
 
 def test_write_line_round_trip(tmp_path):
@@ -279,3 +275,28 @@ def test_vtr_snapshot_round_trip(tmp_path):
     np.testing.assert_array_equal(back["levelset0"], cs.phi)
     pvd = (tmp_path / "solution.pvd").read_text()
     assert 'timestep="1.500000e-04" file="solution_0001.vtr"' in pvd
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("flux", [abi.LSFLUX_ROE, abi.LSFLUX_LLF, abi.LSFLUX_UPWIND])
+@pytest.mark.parametrize("lim", [abi.LIM_NONE, abi.LIM_VANALBADA])
+def test_gpu_finite_volume_level_set_matches_oracle(flux, lim):
+    from helpers import rel_linf
+    from m2c_gb300 import problems
+    from m2c_gb300.solver import FluidState, Solver
+    from oracle import binding as ob
+    c, V, ID, phi = problems.shock_bubble(n=20)
+    c.ls_solver, c.ls_flux, c.ls_limiter = abi.LS_FINITE_VOLUME, flux, lim
+    c.bc[2] = abi.BC_OUTLET          # every boundary rule of the level-set faces
+    s = Solver(c, FluidState(V, ID, phi))
+    o = ob.OracleSim(c)
+    o.upload(V, ID, phi)
+    assert rel_linf(s.LevelSetResidual(), o.levelset_residual()) < 1e-12
+    for _ in range(3):
+        dt, _ = o.compute_dt()
+        o.advance(dt)
+        s.AdvanceOneTimeStep(dt)
+    g = s.get_state()
+    Vo, IDo, po = o.download()
+    np.testing.assert_array_equal(g.ID, IDo)
+    assert rel_linf(g.Phi, po) < 1e-10
