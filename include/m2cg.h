@@ -262,7 +262,9 @@ m2cg_status m2cg_riemann_batch(m2cg_ctx* ctx, int64_t n,
  * ExactRiemannSolverBase.cpp:34-50).  Host arrays:
  *   W      n x 6  {rho_l, u_l, p_l, rho_r, u_r, p_r}
  *   eos    n x 10 {type (M2CG_EOS_SG / M2CG_EOS_NASG), gamma, pc, b, q} left, then right
- *   warm_p n starting pressures (> 0: learned warm start, see m2cg_mlp_*) or NULL
+ *   warm_p n starting pressures (> 0: learned warm start, see m2cg_mlp_*) or NULL; used on every
+ *          problem that has one (the in-step warm start of m2cg_set_warm_start uses its predictions
+ *          only where the acoustic pressure jump exceeds 5 % of the mean pressure)
  *   out    n x 4  {p*, u*, rho*_l, rho*_r}
  *   iters  wave-pair evaluations (bracketing + main loop), err as m2cg_riemann_batch (optional)
  *   kernel_ms  device time of the solve kernel alone (optional). */

@@ -1360,6 +1360,7 @@ void orc_riemann_batch(const m2cg_config* cfg, int64_t n, const double* Vm, cons
 void orc_riemann_batch_eos(const m2cg_config* cfg, int64_t n, const double* W, const double* E, const double* warm_p,
                            double* out, int32_t* iters, int32_t* err) {
   RiemannParams rp;
+  rp.warm_gate = 0.0;   // given starting pressures are used on every problem
   rp.maxIts_main = cfg->maxits_main; rp.maxIts_bracket = cfg->maxits_bracket; rp.maxIts_shock = cfg->maxits_shock;
   rp.numSteps_rarefaction = cfg->numsteps_rarefaction; rp.tol_main = cfg->tol_main; rp.tol_shock = cfg->tol_shock;
   rp.tol_rarefaction = cfg->tol_rarefaction; rp.min_pressure = cfg->min_pressure;
