@@ -81,7 +81,8 @@ _SCHEMA = {
                           "ReferenceSpecificEnthalpy", "ReferenceTemperature"},
     "Material": {"EquationOfState", "DensityCutOff", "PressureCutOff", "DensityUpperLimit", "PressureUpperLimit",
                  "DensityPrescribedAtFailure"},
-    "InitialState": _STATE_KEYS, "Inlet": _STATE_KEYS, "Inlet2": _STATE_KEYS, "DefaultInitialState": _STATE_KEYS,
+    "InitialState": _STATE_KEYS, "Inlet": _STATE_KEYS, "Inlet2": _STATE_KEYS, "Farfield": _STATE_KEYS,
+    "Farfield2": _STATE_KEYS, "DefaultInitialState": _STATE_KEYS,
 }
 
 
@@ -212,7 +213,8 @@ def parse(text):
 # ---------------------------------------------------------------------------
 # IoData keyword tables (values as in the reference's enums)
 
-_BC = {"Inlet": abi.BC_INLET, "Inlet2": abi.BC_INLET2, "Wall": abi.BC_SLIPWALL, "SlipWall": abi.BC_SLIPWALL,
+_BC = {"Inlet": abi.BC_INLET, "Inlet2": abi.BC_INLET2, "Farfield": abi.BC_INLET, "Farfield2": abi.BC_INLET2,
+       "Wall": abi.BC_SLIPWALL, "SlipWall": abi.BC_SLIPWALL,
        "StickWall": abi.BC_STICKWALL, "NoSlipWall": abi.BC_STICKWALL, "Symmetry": abi.BC_SYMMETRY,
        "Outlet": abi.BC_OUTLET}                                                   # IoData.cpp:527-535
 _LSBC = {"ZeroNeumann": abi.LSBC_ZERO_NEUMANN, "LinearExtrapolation": abi.LSBC_LINEAR_EXTRAPOLATION,
@@ -325,8 +327,9 @@ class Case:
                 c.mat[m].pmin = float(d["PressureCutOff"])
 
         bcs = t.get("BoundaryConditions", {})
-        inlet = _state(bcs.get("Inlet"))
-        inlet2 = _state(bcs.get("Inlet2"))
+        # Farfield / Farfield2 name the same states as Inlet / Inlet2 (IoData.cpp:1976-1979)
+        inlet = _state({**bcs.get("Inlet", {}), **bcs.get("Farfield", {})})
+        inlet2 = _state({**bcs.get("Inlet2", {}), **bcs.get("Farfield2", {})})
         for p, v in enumerate(_vec(inlet)):
             c.inlet[p] = v
         for p, v in enumerate(_vec(inlet2)):

@@ -1,14 +1,15 @@
-"""Golden end-of-run line plots of the reference's own Riemann-problem tests.
+"""Golden end-of-run line plots of the reference's own tests.
 
 For every Tests/RiemannProblems/Test*/ directory of the reference (Test7, JWL,
-skipped): the input file parsed by m2c_gb300.inputfile.parse (the nested
+skipped) and the two-dimensional Tests/ExplosionShyue98 case: the input file
+parsed by m2c_gb300.inputfile.parse (the nested
 key/value tree, which the tests turn into a configuration and initial state
 with Case.from_tree), and the final line plot results/line_0001.txt written
 by the reference (ProbeOutput.cpp:483-597): time, time step and the columns
-density, velocity x, pressure, material ID and level set at the 200 points.
-Writes riemann_lines.json beside this script.
+density, velocity x, pressure, material ID and level set at the line's points.
+Writes reference_lines.json beside this script.
 
-Usage: python tests/golden/make_riemann_lines.py [reference_dir]
+Usage: python tests/golden/make_reference_lines.py [reference_dir]
 """
 import json
 import os
@@ -24,11 +25,11 @@ REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
 
 def main():
     base = os.path.join(REF, "Tests", "RiemannProblems")
+    dirs = [(name, os.path.join(base, name)) for name in sorted(os.listdir(base), key=lambda s: (len(s), s))
+            if name.startswith("Test") and name != "Test7"]
+    dirs.append(("ExplosionShyue98", os.path.join(REF, "Tests", "ExplosionShyue98")))
     out = {}
-    for name in sorted(os.listdir(base), key=lambda s: (len(s), s)):
-        d = os.path.join(base, name)
-        if not name.startswith("Test") or name == "Test7":
-            continue
+    for name, d in dirs:
         tree = parse(open(os.path.join(d, "input.st")).read())
         lines = open(os.path.join(d, "results", "line_0001.txt")).read().splitlines()
         m = re.match(r"## Time: (\S+), Time step: (\d+)\.", lines[2])
@@ -37,7 +38,7 @@ def main():
         out[name] = {"tree": tree, "time": float(m.group(1)), "step": int(m.group(2)),
                      "rho": cols[1], "vx": cols[2], "p": cols[5], "id": cols[7],
                      "phi": cols[8] if len(cols) > 8 else None}
-    with open(os.path.join(HERE, "riemann_lines.json"), "w") as f:
+    with open(os.path.join(HERE, "reference_lines.json"), "w") as f:
         json.dump(out, f, separators=(",", ":"))
     print(f"wrote {len(out)} cases")
 
