@@ -207,6 +207,11 @@ def ensemble_bench(n_domains, steps):
         for i, (c, V, ID, phi) in enumerate(doms):
             ens.member(i).set_state(FluidState(V, ID, phi))
 
+    # the batched step's interface-solve budget, tuned on real steps first
+    reset()
+    budget, tuned_ms = ens.autotune(steps=2)
+    out["autotune"] = {"first_pass_eval_budget": budget, "ms_per_step": tuned_ms,
+                       "candidates": [4, 8, 16, 32, 64, 1 << 20]}
     for mode in ("batched", "sequential"):
         run = ens.run if mode == "batched" else ens.run_sequential
         reset()

@@ -361,6 +361,13 @@ m2cg_ctx* m2cg_ensemble_member(m2cg_ensemble* ens, int32_t i);
 m2cg_status m2cg_ensemble_run(m2cg_ensemble* ens, int32_t n_steps, float* ms);
 m2cg_status m2cg_ensemble_run_sequential(m2cg_ensemble* ens, int32_t n_steps, float* ms);
 int64_t m2cg_ensemble_kernel_launches(const m2cg_ensemble* ens);
+/* No reference counterpart: tunes the batched step's interface-solve schedule.
+ * Each candidate first-pass evaluation budget cand[0..n_cand) runs `steps`
+ * real steps of the run (the members' states advance; the budget changes the
+ * schedule, not the results); the fastest is kept for later m2cg_ensemble_run
+ * calls.  best / ms_per_step (optional) receive the choice and its time. */
+m2cg_status m2cg_ensemble_autotune(m2cg_ensemble* ens, int32_t steps, int32_t n_cand, const int32_t* cand,
+                                   int32_t* best, float* ms_per_step);
 
 /* ---- timing on the context stream -------------------------------------- */
 m2cg_status m2cg_sync(m2cg_ctx* ctx);

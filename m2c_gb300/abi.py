@@ -227,6 +227,7 @@ def load(path=None):
         "m2cg_ensemble_run": (C.c_int, [_P, C.c_int32, _F]),
         "m2cg_ensemble_run_sequential": (C.c_int, [_P, C.c_int32, _F]),
         "m2cg_ensemble_kernel_launches": (C.c_int64, [_P]),
+        "m2cg_ensemble_autotune": (C.c_int, [_P, C.c_int32, C.c_int32, _I, _I, _F]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -1374,6 +1374,43 @@ m2cg_status m2cg_ensemble_run(m2cg_ensemble* e, int32_t n_steps, float* ms) {
   return M2CG_OK;
 }
 
+// Tuning of the batched step's launch configuration: the interface solves'
+// first-pass evaluation budget (how much of each solve runs in the pool of
+// one-thread-per-face blocks before the remaining solves move to the
+// one-warp-per-face straggler pass) decides how much of the stage waits on the
+// longest solves.  It changes the schedule, not the results.  Every candidate
+// runs `steps` real steps of the run (the state advances); the fastest is kept.
+m2cg_status m2cg_ensemble_autotune(m2cg_ensemble* e, int32_t steps, int32_t n_cand, const int32_t* cand,
+                                   int32_t* best, float* ms_per_step) {
+  if (!e || steps < 1 || n_cand < 1 || !cand) { set_err("bad autotune arguments"); return M2CG_ERR_INVALID_ARG; }
+  for (int c = 0; c < n_cand; c++)
+    if (cand[c] < 1) { set_err("evaluation budgets must be positive"); return M2CG_ERR_INVALID_ARG; }
+  auto rebuild = [&](int limit) -> m2cg_status {
+    CK(cudaStreamSynchronize(e->stream));
+    if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
+    for (void* p : e->dev) cudaFree(p);
+    e->dev.clear();
+    e->tab_i = 0;
+    e->eval_limit = limit;
+    return M2CG_OK;
+  };
+  float best_ms = 0.0f;
+  int best_limit = e->eval_limit;
+  for (int c = 0; c < n_cand; c++) {
+    m2cg_status st = rebuild(cand[c]);
+    if (st != M2CG_OK) return st;
+    float ms = 0.0f;
+    st = m2cg_ensemble_run(e, steps, &ms);
+    if (st != M2CG_OK) return st;
+    if (c == 0 || ms < best_ms) { best_ms = ms; best_limit = cand[c]; }
+  }
+  m2cg_status st = rebuild(best_limit);
+  if (st != M2CG_OK) return st;
+  if (best) *best = best_limit;
+  if (ms_per_step) *ms_per_step = best_ms / steps;
+  return M2CG_OK;
+}
+
 m2cg_status m2cg_ensemble_run_sequential(m2cg_ensemble* e, int32_t n_steps, float* ms) {
   if (!e || n_steps < 0) { set_err("bad ensemble arguments"); return M2CG_ERR_INVALID_ARG; }
   CK(cudaStreamSynchronize(e->stream));

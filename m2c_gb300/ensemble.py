@@ -40,6 +40,17 @@ class Ensemble:
                   "m2cg_ensemble_run_sequential")
         return ms.value
 
+    def autotune(self, steps=2, budgets=(4, 8, 16, 32, 64, 1 << 20)):
+        """Pick the interface solves' first-pass evaluation budget by timing
+        `steps` real steps per candidate (the states advance); returns
+        (budget, ms per step)."""
+        import numpy as np
+        cand = np.ascontiguousarray(budgets, np.int32)
+        best, ms = C.c_int32(), C.c_float()
+        abi.check(self.lib, self.lib.m2cg_ensemble_autotune(self.h, int(steps), len(cand), abi.iptr(cand),
+                                                            C.byref(best), C.byref(ms)), "m2cg_ensemble_autotune")
+        return best.value, ms.value
+
     def kernel_launches(self):
         return self.lib.m2cg_ensemble_kernel_launches(self.h)
 

@@ -54,3 +54,27 @@ def test_ensemble_matches_members_run_alone():
     assert ens.kernel_launches() > 0
     ens.close()
     seq.close()
+
+
+@pytest.mark.gpu
+def test_autotuned_ensemble_matches_members_run_alone():
+    """The autotuner's candidate budgets change the interface solves' schedule,
+    not their results: after tuning (whose trial steps are real steps) every
+    member ends bit for bit where it ends advanced alone."""
+    doms = [problems.bubble_collapse(*d) for d in SMALL]
+    ens = Ensemble([d[0] for d in doms])
+    for i, (c, V, ID, phi) in enumerate(doms):
+        ens.member(i).set_state(FluidState(V, ID, phi))
+    budgets = (2, 8, 1 << 20)
+    best, ms = ens.autotune(steps=1, budgets=budgets)
+    assert best in budgets and ms > 0
+    ens.run(2)   # 3 tuning steps + 2
+    for i, (c, V, ID, phi) in enumerate(doms):
+        solo = Solver(c, FluidState(V, ID, phi))
+        solo.run(5)
+        a, b = ens.member(i).get_state(), solo.get_state()
+        assert np.array_equal(a.ID, b.ID), i
+        assert np.array_equal(a.V, b.V), i
+        assert np.array_equal(a.Phi, b.Phi), i
+        solo.close()
+    ens.close()
