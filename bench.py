@@ -290,6 +290,25 @@ def large_bench(n, steps, warmup=2, ws_train=1 << 20):
     return out
 
 
+def max_over_ranks(pg, x):
+    """The largest x over all ranks (the job's time is its slowest rank's);
+    x itself without a process group.  NCCL reduces device tensors, gloo host
+    tensors."""
+    if pg is None:
+        return x
+    import torch
+    dev = "cuda" if pg.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([float(x)], dtype=torch.float64, device=dev)
+    pg.all_reduce(t, op=pg.ReduceOp.MAX)
+    return float(t.item())
+
+
+def job_rate(world, cells, stages, steps, seconds):
+    """Whole-job cell-stage updates per second: every rank advances its own
+    replica of `cells` cells, timed by the slowest rank."""
+    return world * cells * stages * steps / seconds
+
+
 def run_gb300(args):
     rank, world, local = dist_info()
     pg = None
@@ -331,13 +350,8 @@ def run_gb300(args):
     launches = lib.m2cg_kernel_launches(ctx) - l0
     c1 = s.counters()
     clk = clocks.stop()
-    t_ms = ms.value
-    if pg:
-        import torch
-        t = torch.tensor([t_ms], dtype=torch.float64, device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        t_ms = float(t.item())
-    value = world * cells * stages * args.steps / (t_ms * 1e-3)
+    t_ms = max_over_ranks(pg, ms.value)
+    value = job_rate(world, cells, stages, args.steps, t_ms * 1e-3)
     solves = c1["riemann_solves"] - c0["riemann_solves"]
     iters = c1["riemann_iterations"] - c0["riemann_iterations"]
 
@@ -409,12 +423,8 @@ def run_gb300(args):
         e2e_step()
     te = time.perf_counter() - t0
     barrier()
-    if pg:
-        import torch
-        t = torch.tensor([te], dtype=torch.float64, device="cuda")
-        pg.all_reduce(t, op=pg.ReduceOp.MAX)
-        te = float(t.item())
-    e2e_value = world * cells * stages * e2e_steps / te
+    te = max_over_ranks(pg, te)
+    e2e_value = job_rate(world, cells, stages, e2e_steps, te)
     for p in (hv, hi, hp):
         lib.m2cg_host_free(p)
 
