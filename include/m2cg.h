@@ -126,8 +126,7 @@ typedef struct {
   /* Learned warm start for the interface Riemann solve (no reference counterpart) */
   int32_t warm_start;          /* 0 = cold start (reference), 1 = MLP warm start */
   /* LevelSet[0].Reinitialization (IoData.cpp:1421-1429): full domain, first layer FIXED */
-  int32_t reinit_frequency;    /* Frequency: every that many steps (<= 0: never, the default;
-                                  FrequencyDt, the time-interval trigger, is not offered) */
+  int32_t reinit_frequency;    /* Frequency: every that many steps (<= 0: never, the default) */
   int32_t reinit_max_its;      /* MaxIts (30) */
   int32_t pad4_;
   double reinit_cfl;           /* CFL (0.8) */
@@ -139,6 +138,8 @@ typedef struct {
   int32_t ls_rec_type;         /* Reconstruction.Type (default Linear) */
   int32_t ls_limiter;          /* Reconstruction.Limiter (default GeneralizedMinMod) */
   double ls_minmod_coeff;      /* Reconstruction.GeneralizedMinModCoefficient (1.2) */
+  double reinit_frequency_dt;  /* Reinitialization.FrequencyDt: after every step that crosses a multiple of
+                                  this time (> 0 takes precedence over Frequency, Utils.cpp:344-349) */
 } m2cg_config;
 
 /* Per-step counters (the reference prints these as warnings; SpaceOperator.cpp:681-683,

@@ -68,7 +68,8 @@ class Config(C.Structure):
                 ("warm_start", C.c_int32), ("reinit_frequency", C.c_int32), ("reinit_max_its", C.c_int32),
                 ("pad4_", C.c_int32), ("reinit_cfl", C.c_double), ("reinit_tol", C.c_double),
                 ("ls_solver", C.c_int32), ("ls_flux", C.c_int32), ("ls_delta", C.c_double),
-                ("ls_rec_type", C.c_int32), ("ls_limiter", C.c_int32), ("ls_minmod_coeff", C.c_double)]
+                ("ls_rec_type", C.c_int32), ("ls_limiter", C.c_int32), ("ls_minmod_coeff", C.c_double),
+                ("reinit_frequency_dt", C.c_double)]
 
 
 class Counters(C.Structure):
@@ -129,6 +130,7 @@ def default_config():
     c.reinit_frequency, c.reinit_max_its, c.reinit_cfl, c.reinit_tol = -1, 30, 0.8, 2.0e-4
     c.ls_solver, c.ls_flux, c.ls_delta = LS_FINITE_DIFFERENCE, LSFLUX_ROE, 0.2
     c.ls_rec_type, c.ls_limiter, c.ls_minmod_coeff = REC_LINEAR, LIM_GENERALIZED_MINMOD, 1.2
+    c.reinit_frequency_dt = -1.0
     return c
 
 

@@ -476,6 +476,7 @@ m2cg_status m2cg_config_default(m2cg_config* c) {
   c->ls_rec_type = M2CG_REC_LINEAR;
   c->ls_limiter = M2CG_LIM_GENERALIZED_MINMOD;
   c->ls_minmod_coeff = 1.2;
+  c->reinit_frequency_dt = -1.0;
   return M2CG_OK;
 }
 
@@ -497,6 +498,7 @@ static m2cg_status reinit_prepare(m2cg_ctx* x) {
   a.tol = x->cfg.reinit_tol;
   a.max_its = x->cfg.reinit_max_its;
   a.freq = x->cfg.reinit_frequency;
+  a.freq_dt = x->cfg.reinit_frequency_dt;
   a.phi = x->S[0].q[5];
   CK(x->alloc(&a.phi1, (size_t)g.ntot));
   CK(x->alloc(&a.phi2, (size_t)g.ntot));
@@ -555,7 +557,8 @@ static m2cg_status create_ctx(const m2cg_config* cfg, double* ext_scratch, m2cg_
     return M2CG_ERR_CUDA;
   }
   st = ctx_alloc(x);
-  if (st == M2CG_OK && x->P.n_ls > 0 && cfg->reinit_frequency > 0) st = reinit_prepare(x);
+  if (st == M2CG_OK && x->P.n_ls > 0 && (cfg->reinit_frequency > 0 || cfg->reinit_frequency_dt > 0))
+    st = reinit_prepare(x);
   if (st != M2CG_OK) { m2cg_destroy(x); return st; }
   *out = x;
   return M2CG_OK;
@@ -818,7 +821,8 @@ m2cg_status m2cg_run(m2cg_ctx* x, int32_t n_steps, m2cg_counters* counters) {
   // it on the device (a step past MaxTime is not taken and not counted)
   long long step0 = 0;
   const int freq = x->ri_gated ? x->cfg.reinit_frequency : 0;
-  if (freq > 0) {
+  const bool by_time = x->ri_gated && x->cfg.reinit_frequency_dt > 0;   // the gate decides on the device
+  if (freq > 0 && !by_time) {
     CK(cudaMemcpyAsync(&step0, &x->sc->steps, sizeof(step0), cudaMemcpyDeviceToHost, s));
     CK(cudaStreamSynchronize(s));
   }
@@ -826,7 +830,7 @@ m2cg_status m2cg_run(m2cg_ctx* x, int32_t n_steps, m2cg_counters* counters) {
   for (int i = 0; i < n_steps; i++) {
     CK(cudaGraphLaunch(x->graph_exec, s));
     x->launches += x->launches_per_step;
-    if (freq > 0 && (step0 + i + 1) % freq == 0) {
+    if (by_time || (freq > 0 && (step0 + i + 1) % freq == 0)) {
       CK(cudaGraphLaunch(x->ri_gated, s));
       ri++;
     }
@@ -1287,7 +1291,7 @@ m2cg_status m2cg_ensemble_create(const m2cg_config* cfgs, int32_t n, m2cg_ensemb
       set_err("member %d: the batched step advects the level set by finite differences only", d);
       return M2CG_ERR_INVALID_ARG;
     }
-    if (cfgs[d].n_levelsets > 0 && cfgs[d].reinit_frequency > 0) {
+    if (cfgs[d].n_levelsets > 0 && (cfgs[d].reinit_frequency > 0 || cfgs[d].reinit_frequency_dt > 0)) {
       set_err("member %d: the batched step does not reinitialize level sets (reinit_frequency must be <= 0)", d);
       return M2CG_ERR_INVALID_ARG;
     }

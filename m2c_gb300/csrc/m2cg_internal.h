@@ -130,7 +130,8 @@ struct ReinitArgs {
   double hmin;         // min(dx, dy, dz)
   double tol;
   int max_its;
-  int freq;            // gate: every freq-th completed step (<= 0: no gate)
+  int freq;            // gate: every freq-th completed step (<= 0: never) ...
+  double freq_dt;      // ... or, when > 0, after every step crossing a multiple of freq_dt
   double* phi;         // the level set (ghosted), updated in place
   double* phi1;        // sub-stage states
   double* phi2;

@@ -98,13 +98,19 @@ M2CG_DEV void block_max_atomic(unsigned long long v, unsigned long long* dst) {
   }
 }
 
-// Gate: run this call?  (every freq-th completed step when gated; never with
-// MaxIts <= 0, where the reference's loop does not execute and the failsafe
-// accepts the input).
+// Gate: run this call?  (when gated: after every freq-th completed step, or
+// after every step that crosses a multiple of freq_dt; never with MaxIts <= 0,
+// where the reference's loop does not execute and the failsafe accepts the
+// input).
 __global__ void k_ri_begin(ReinitArgs a, cudaGraphConditionalHandle h, int gated) {
   ReinitState* st = a.st;
   bool go = a.max_its > 0;
-  if (gated) go = go && a.sc && a.sc->active && a.freq > 0 && (a.sc->steps % a.freq) == 0;
+  if (gated) {   // Utils.cpp:337-357: the time interval when given, else the step count
+    bool due;
+    if (a.freq_dt > 0) due = floor(a.sc->time / a.freq_dt) != floor((a.sc->time - a.sc->dt) / a.freq_dt);
+    else due = a.freq > 0 && (a.sc->steps % a.freq) == 0;
+    go = go && a.sc && a.sc->active && due;
+  }
   st->run = go ? 1 : 0;
   st->detected = 0;
   st->restore = 0;

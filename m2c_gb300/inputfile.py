@@ -377,8 +377,7 @@ class Case:
             if re_:
                 if re_.get("FirstLayerTreatment", "Fixed") != "Fixed":
                     raise NotImplementedError(f"Reinitialization.FirstLayerTreatment = {re_['FirstLayerTreatment']}")
-                if float(re_.get("FrequencyDt", -1.0)) > 0:
-                    raise NotImplementedError("Reinitialization.FrequencyDt")
+                c.reinit_frequency_dt = float(re_.get("FrequencyDt", -1.0))
                 c.reinit_frequency = int(re_.get("Frequency", -1))
                 c.reinit_max_its = int(re_.get("MaxIts", 30))
                 c.reinit_cfl = float(re_.get("CFL", 0.8))

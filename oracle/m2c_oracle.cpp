@@ -1074,7 +1074,10 @@ void Oracle::EndOfStep(std::vector<double>& phi0) {
   UpdateIDGhosts(ID);
   // level-set reinitialization at the user frequency (TimeIntegrator.cpp:756-768,
   // LevelSetOperator.cpp:1338-1361, Utils.cpp:337-357 with frequency_dt unset)
-  if (cfg.reinit_frequency > 0 && time_step % cfg.reinit_frequency == 0) Reinitialize();
+  bool due = (cfg.reinit_frequency_dt > 0)
+                 ? std::floor(time / cfg.reinit_frequency_dt) != std::floor((time - last_dt) / cfg.reinit_frequency_dt)
+                 : (cfg.reinit_frequency > 0 && time_step % cfg.reinit_frequency == 0);
+  if (due) Reinitialize();
   // UpdateStateVariablesAfterInterfaceMotion
   std::vector<std::array<int, 3>> unresolved;
   std::vector<double> Vold = V;

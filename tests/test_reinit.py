@@ -191,3 +191,40 @@ def test_gpu_steps_with_reinit_match_oracle(ts):
     assert rel_linf(g.Phi, phio) < 1e-8
     assert np.all(rel_linf(g.V, Vo)[[0, 4]] < 1e-8)
     np.testing.assert_array_equal(g.ID, IDo)
+
+
+def test_oracle_time_interval_trigger():
+    """FrequencyDt takes precedence over Frequency (Utils.cpp:344-349): a
+    reinitialization follows every step whose interval (t - dt, t] crosses a
+    multiple of FrequencyDt."""
+    c, V, ID, phi = problems.shock_bubble(n=16)
+    o = ob.OracleSim(c)
+    o.upload(V, ID, phi)
+    times = []
+    for _ in range(6):
+        o.run(1)
+        times.append(o.counters()["time"])
+    dt_mean = times[-1] / 6
+    c.reinit_frequency, c.reinit_frequency_dt = 1, 2.5 * dt_mean
+    o = ob.OracleSim(c)
+    o.upload(V, ID, phi)
+    o.run(6)
+    t = np.array([0.0] + times)
+    expect = int(np.sum(np.floor(t[1:] / c.reinit_frequency_dt) != np.floor(t[:-1] / c.reinit_frequency_dt)))
+    assert 1 <= expect < 6
+    assert o.reinitialize()[1]["calls"] - 1 == expect
+
+
+@pytest.mark.gpu
+def test_gpu_time_interval_trigger_matches_oracle():
+    from m2c_gb300.solver import FluidState, Solver
+    c, V, ID, phi = problems.shock_bubble(n=24)
+    c.reinit_frequency_dt = 1.2e-5   # dt is about 5.5e-6 here: steps 3 and 5 cross a multiple
+    s = Solver(c, FluidState(V, ID, phi))
+    o = ob.OracleSim(c)
+    o.upload(V, ID, phi)
+    s.run(6)
+    o.run(6)
+    calls = o.reinitialize()[1]["calls"] - 1
+    assert calls == 2 and s.reinit_stats()["calls"] == calls
+    assert rel_linf(s.get_state().Phi, o.download()[2]) < 1e-8
