@@ -269,6 +269,9 @@ def large_bench(n, steps, warmup=2, ws_train=1 << 20):
                      "riemann_first_pass_ms_per_step": float(ph[4]),
                      "riemann_stragglers_ms_per_step": float(ph[8]),
                      "interface_faces_per_stage": (c1["interface_faces"] - c0["interface_faces"]) / (3 * steps),
+                     "swept_cells": c1["swept_cells"] - c0["swept_cells"],
+                     "unresolved_cells": c1["unresolved_cells"] - c0["unresolved_cells"],
+                     "clipped_cells": c1["clipped_cells"] - c0["clipped_cells"],
                      "reinit_calls": r1["calls"] - r0["calls"],
                      "reinit_iterations": r1["iterations"] - r0["iterations"],
                      "reinit_retries": r1["retries"] - r0["retries"]}
