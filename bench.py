@@ -59,7 +59,7 @@ def parse():
     ap.add_argument("--cpu-size", type=int, default=96)
     ap.add_argument("--cpu-steps", type=int, default=2)
     ap.add_argument("--no-cpu", action="store_true")
-    # level-set reinitialization every F steps in the main workload (0: off, the BASELINE shape)
+    # level-set reinitialization every F steps in the main workload (0: off, as the 256^3 workload runs)
     ap.add_argument("--reinit", type=int, default=0)
     # learned warm start: training / test problems of the study (0 disables it)
     ap.add_argument("--ws-train", type=int, default=1 << 20)

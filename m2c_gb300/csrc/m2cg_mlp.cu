@@ -3,7 +3,7 @@
 // two states and their EOS parameters.  The exact solver starts from a pair
 // bracketing the prediction (in place of the acoustic pair,
 // ExactRiemannSolverBase.cpp:1107-1158) and still converges to the same
-// tolerance, so it remains both the fallback and the judge.
+// tolerance, so its answer, not the prediction, is the result.
 //
 // The three 64-wide layers run on the tensor cores: tcgen05.mma with BF16
 // operands staged in shared memory and FP32 accumulators in tensor memory, one
