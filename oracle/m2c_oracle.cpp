@@ -43,6 +43,7 @@ namespace {
 struct Counters {
   int64_t interface_faces = 0, riemann_errors = 0, riemann_iterations = 0, riemann_solves = 0;
   int64_t clipped_cells = 0, clipped_faces = 0, nonphysical = 0, swept_cells = 0, unresolved_cells = 0, steps = 0;
+  int64_t unresolved_fixed = 0;
   int64_t fallbacks = 0;
 };
 
@@ -87,6 +88,8 @@ struct Oracle {
   void P2C(const std::vector<double>& v, const std::vector<int>& id, std::vector<double>& u);
   void C2P(const std::vector<double>& u, const std::vector<int>& id, std::vector<double>& v);
   void EndOfStep(std::vector<double>& phi0);
+  void UpdateIDByLevelSet(const std::vector<double>& phi_old);
+  void FixUnresolvedNodes(const std::vector<std::array<int, 3>>& unresolved);
   // level-set reinitialization (full domain, first layer FIXED)
   double reinit_cfl = 0.8;
   int reinit_retries = 0, reinit_failures = 0, reinit_calls = 0, reinit_iters = 0;
@@ -1021,18 +1024,17 @@ bool Oracle::Reinitialize() {
   }
 }
 
-// TimeIntegrator.cpp:720-843 with MultiPhaseOperator.cpp:153-357, 947-1274.
-void Oracle::EndOfStep(std::vector<double>& phi0) {
-  std::vector<int> IDn = ID;
+// MultiPhaseOperator::UpdateMaterialIDByLevelSet (MultiPhaseOperator.cpp:153-357,
+// one level set) from phi_old to Phi, then the ID ghosts.
+void Oracle::UpdateIDByLevelSet(const std::vector<double>& phi_old) {
   int lsmat = cfg.ls_matid;
-  // UpdateMaterialIDByLevelSet (one level set)
   std::vector<char> tag(N(), 0);
   std::vector<std::array<int, 3>> remaining;
   for (int k = 0; k < NZ; k++)
     for (int j = 0; j < NY; j++)
       for (int i = 0; i < NX; i++) {
         size_t c = idx(i, j, k);
-        if (Phi[c] * phi0[c] > 0.0) continue;
+        if (Phi[c] * phi_old[c] > 0.0) continue;
         if (Phi[c] < 0) ID[c] = lsmat;
         else { tag[c] = 1; remaining.push_back({i, j, k}); }
       }
@@ -1072,6 +1074,100 @@ void Oracle::EndOfStep(std::vector<double>& phi0) {
     }
   }
   UpdateIDGhosts(ID);
+}
+
+// MultiPhaseOperator::FixUnresolvedNodes (MultiPhaseOperator.cpp:1279-1480; no
+// embedded surfaces, failsafe density applied): each unresolved cell takes the
+// upwind-weighted mean of its resolved same-material neighbours (weight =
+// max(0, unit neighbour velocity . unit direction from the neighbour to the
+// cell)), else their inverse-distance mean, else keeps pressure and velocity
+// and takes an inverse-distance density from up to 10 layers, else the
+// material's failsafe density.  As in the reference, the flag marking the
+// first accumulated neighbour is set once for the whole list (line 1296), so
+// later cells add their upwind neighbours onto their own advected state.
+void Oracle::FixUnresolvedNodes(const std::vector<std::array<int, 3>>& unresolved) {
+  const double lo[3] = {cfg.x0, cfg.y0, cfg.z0}, h[3] = {dx, dy, dz};
+  auto coord = [&](int i, int j, int k, double* x) {
+    const int q[3] = {i, j, k};
+    for (int d = 0; d < 3; d++) x[d] = lo[d] + 0.5 * h[d] + q[d] * h[d];
+  };
+  auto listed = [&](int i, int j, int k) {
+    for (auto& p : unresolved) if (p[0] == i && p[1] == j && p[2] == k) return true;
+    return false;
+  };
+  bool reset = false;
+  for (auto& p : unresolved) {
+    const int i = p[0], j = p[1], k = p[2];
+    const size_t c = idx(i, j, k);
+    double x0[3];
+    coord(i, j, k, x0);
+    double sum_weight = 0.0, sum_weight2 = 0.0, vtmp[5] = {0, 0, 0, 0, 0};
+    for (int nk = k - 1; nk <= k + 1; nk++)
+      for (int nj = j - 1; nj <= j + 1; nj++)
+        for (int ni = i - 1; ni <= i + 1; ni++) {
+          if (outside(ni, nj, nk)) continue;
+          const size_t nc = idx(ni, nj, nk);
+          if (ID[nc] != ID[c]) continue;
+          if (ni == i && nj == j && nk == k) continue;
+          if (listed(ni, nj, nk)) continue;
+          double x1[3], v1[3], d[3];
+          coord(ni, nj, nk, x1);
+          for (int q = 0; q < 3; q++) v1[q] = V[nc * 5 + 1 + q];
+          double v1norm = std::sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+          if (v1norm != 0) { double r = 1.0 / v1norm; for (int q = 0; q < 3; q++) v1[q] *= r; }
+          for (int q = 0; q < 3; q++) d[q] = x0[q] - x1[q];
+          double dn = std::sqrt(d[0] * d[0] + d[1] * d[1] + d[2] * d[2]);
+          { double r = 1.0 / dn; for (int q = 0; q < 3; q++) d[q] *= r; }
+          double weight = std::max(0.0, d[0] * v1[0] + d[1] * v1[1] + d[2] * v1[2]);
+          if (weight > 0) {
+            sum_weight += weight;
+            for (int q = 0; q < 5; q++) {
+              if (reset) V[c * 5 + q] += weight * V[nc * 5 + q];
+              else V[c * 5 + q] = weight * V[nc * 5 + q];
+            }
+            reset = true;
+          }
+          for (int q = 0; q < 5; q++) vtmp[q] += 1.0 / dn * V[nc * 5 + q];
+          sum_weight2 += 1.0 / dn;
+        }
+    if (cfg.mp_phasechange_dir == M2CG_PCDIR_UPWIND && sum_weight > 0) {
+      double r = 1.0 / sum_weight;
+      for (int q = 0; q < 5; q++) V[c * 5 + q] *= r;
+      continue;
+    }
+    if (sum_weight2 > 0) {
+      for (int q = 0; q < 5; q++) V[c * 5 + q] = vtmp[q] / sum_weight2;
+      continue;
+    }
+    double density = 0.0;
+    for (int layer = 1; layer <= 10; layer++) {
+      for (int nk = k - layer; nk <= k + layer; nk++)
+        for (int nj = j - layer; nj <= j + layer; nj++)
+          for (int ni = i - layer; ni <= i + layer; ni++) {
+            if (outside(ni, nj, nk)) continue;
+            if (ni < -1 || ni > NX || nj < -1 || nj > NY || nk < -1 || nk > NZ) continue;
+            const size_t nc = idx(ni, nj, nk);
+            if (ID[nc] != ID[c]) continue;
+            if (ni == i && nj == j && nk == k) continue;
+            if (listed(ni, nj, nk)) continue;
+            double x1[3];
+            coord(ni, nj, nk, x1);
+            double dist = std::sqrt((x1[0] - x0[0]) * (x1[0] - x0[0]) + (x1[1] - x0[1]) * (x1[1] - x0[1]) +
+                                    (x1[2] - x0[2]) * (x1[2] - x0[2]));
+            sum_weight += 1.0 / dist;
+            density += (1.0 / dist) * V[nc * 5];
+          }
+      if (sum_weight > 0) { V[c * 5] = density / sum_weight; break; }
+    }
+    if (sum_weight == 0) V[c * 5] = cfg.mat[ID[c]].failsafe_density;
+  }
+}
+
+// TimeIntegrator.cpp:720-843 with MultiPhaseOperator.cpp:153-357, 947-1274.
+void Oracle::EndOfStep(std::vector<double>& phi0) {
+  std::vector<int> IDn = ID;
+  int lsmat = cfg.ls_matid;
+  UpdateIDByLevelSet(phi0);
   // level-set reinitialization at the user frequency (TimeIntegrator.cpp:756-768,
   // LevelSetOperator.cpp:1338-1361, Utils.cpp:337-357 with frequency_dt unset)
   bool due = (cfg.reinit_frequency_dt > 0)
@@ -1159,9 +1255,23 @@ void Oracle::EndOfStep(std::vector<double>& phi0) {
         }
       }
   cnt.unresolved_cells += (int64_t)unresolved.size();
-  // Unresolved cells: the reference reinitializes phi here, which needs a
-  // configured reinitializer (TimeIntegrator.cpp:776-797); without one it
-  // stops.  The oracle counts them and leaves their state as advected.
+  // Unresolved cells (TimeIntegrator.cpp:776-797): background cells among them
+  // return to the level set's material (phi -> -phi), the level set is
+  // reinitialized, the IDs follow the sign changes, and the states are
+  // extrapolated from resolved neighbours.  The reinitialization is
+  // mandatory there; without a configured reinitializer the reference stops,
+  // and the oracle counts the cells and leaves their state as advected.
+  if (!unresolved.empty() && (cfg.reinit_frequency > 0 || cfg.reinit_frequency_dt > 0)) {
+    std::vector<double> phi_tmp = Phi;
+    for (auto& p : unresolved) {   // UpdateLevelSetsInUnresolvedCells, MultiPhaseOperator.cpp:1364-1420
+      size_t c = idx(p[0], p[1], p[2]);
+      if (!(Phi[c] < 0)) Phi[c] = -Phi[c];
+    }
+    Reinitialize();
+    UpdateIDByLevelSet(phi_tmp);
+    FixUnresolvedNodes(unresolved);
+    cnt.unresolved_fixed += (int64_t)unresolved.size();
+  }
   ClipAll(V, ID);
   ApplyBC(V);
 }
