@@ -160,6 +160,8 @@ typedef struct {
   double cfl;                  /* last CFL number */
   int64_t riemann_fallbacks;   /* solves retried with the non-adaptive solver (ExactRiemannSolverBase.cpp:178-193, 323-337) */
   int64_t path_capped;         /* solves whose integration-path cache reached its capacity */
+  int64_t unresolved_fixed;    /* unresolved cells repaired after a forced reinitialization
+                                  (TimeIntegrator.cpp:776-797; needs reinitialization configured) */
 } m2cg_counters;
 
 typedef struct m2cg_ctx m2cg_ctx;
@@ -198,6 +200,12 @@ m2cg_status m2cg_compute_dt(m2cg_ctx* ctx, double* dt, double* cfl);
  * level set).  Any pointer may be NULL.  Used by probes and line plots
  * (ProbeOutput.cpp:360-597, 848-886), which interpolate across the boundary. */
 m2cg_status m2cg_download_ghosted(m2cg_ctx* ctx, double* V, int32_t* id, double* phi);
+/* Solution at n probe points xyz[3n] (ProbeOutput::SetupInterpolation and
+ * InterpolateSolutionAtProbe, ProbeOutput.cpp:360-480, 849-886): trilinear over the
+ * ghosted cell-centre grid; out[n * 6] (n * 7 with a level set) per point: rho, vx, vy,
+ * vz, p, material ID (interpolated), phi.  A point outside the ghosted grid, or one whose
+ * eight corners are all edge / corner ghosts, is M2CG_ERR_INVALID_ARG. */
+m2cg_status m2cg_sample_points(m2cg_ctx* ctx, int32_t n, const double* xyz, double* out);
 
 /* SpaceOperator::ComputeResidual on the current state with the stored
  * Riemann solutions refreshed (SpaceOperator.cpp:2573-2641, first RK stage).

@@ -78,7 +78,8 @@ class Counters(C.Structure):
                 ("clipped_cells", C.c_int64), ("clipped_faces", C.c_int64), ("nonphysical", C.c_int64),
                 ("swept_cells", C.c_int64), ("unresolved_cells", C.c_int64), ("steps", C.c_int64),
                 ("time", C.c_double), ("dt", C.c_double), ("cfl", C.c_double),
-                ("riemann_fallbacks", C.c_int64), ("path_capped", C.c_int64)]
+                ("riemann_fallbacks", C.c_int64), ("path_capped", C.c_int64),
+                ("unresolved_fixed", C.c_int64)]
 
     def as_dict(self):
         return {name: getattr(self, name) for name, _ in self._fields_}
@@ -196,6 +197,7 @@ def load(path=None):
         "m2cg_reinitialize": (C.c_int, [_P, C.POINTER(ReinitStats)]),
         "m2cg_fp64_peak": (C.c_int, [C.c_int32, _D, C.POINTER(C.c_float)]),
         "m2cg_download_ghosted": (C.c_int, [_P, _D, _I, _D]),
+        "m2cg_sample_points": (C.c_int, [_P, C.c_int32, _D, _D]),
         "m2cg_get_reinit_stats": (C.c_int, [_P, C.POINTER(ReinitStats)]),
         "m2cg_conserved_totals": (C.c_int, [_P, _D]),
         "m2cg_riemann_batch": (C.c_int, [_P, C.c_int64, _D, _I, _D, _I, _D, _D, _I, _D, _D, _I, _I]),

@@ -21,6 +21,9 @@ void launch_update(cudaStream_t, const Params&, const StageArgs&, const int32_t*
 void launch_ls_residual(cudaStream_t, const Params&, const StateSet&, double*);
 void launch_bc(cudaStream_t, const Params&, const StateSet&, int, int, int32_t*, const DevScalars*);
 cudaError_t reinit_build_graph(cudaStream_t, const ReinitArgs&, int, int, cudaGraphExec_t*);
+cudaError_t unres_build_graph(cudaStream_t, const UnresArgs&, int, cudaGraphExec_t*);
+void launch_sample_points(cudaStream_t, const Params&, const StateSet&, const int32_t*, const ProbePoint*, int,
+                          double*);
 void launch_dt(cudaStream_t, const Params&, const StateSet&, const int32_t*, DevScalars*, int, double);
 void launch_compact(cudaStream_t, const Params&, const int32_t*, const IfaceList&, unsigned long long*,
                     const DevScalars*);
@@ -148,6 +151,11 @@ struct m2cg_ctx {
   ReinitArgs ri = {};
   cudaGraphExec_t ri_gated = nullptr, ri_now = nullptr;
   long long ri_bodies_seen = 0;
+  // repair of unresolved swept cells when reinitialization is configured:
+  // the reinitialization gated on the step's list, then the repair graph
+  cudaGraphExec_t ri_unres = nullptr, ur_exec = nullptr;
+  UnresArgs ur = {};
+  unsigned long long ur_repairs_seen = 0;
   // batch buffers
   std::vector<void*> batch;
   int64_t batch_n = 0;
@@ -402,6 +410,7 @@ static int64_t enqueue_step(m2cg_ctx* x, int mode, double fixed_dt) {
   PHASE(PH_DT, launch_dt(s, x->P, x->S[0], x->id, x->sc, mode, fixed_dt)); n += 2;
   cudaMemsetAsync(x->L.count, 0, sizeof(unsigned long long), s);
   cudaMemsetAsync(x->swept_count, 0, sizeof(unsigned long long), s);
+  if (x->P.unres_count) cudaMemsetAsync(x->P.unres_count, 0, sizeof(unsigned long long), s);
   PHASE(PH_COMPACT, launch_compact(s, x->P, x->id, x->L, x->cnt, x->sc)); n++;
   const int ts = x->cfg.ts_type;
   if (ts == M2CG_TS_FORWARD_EULER) {
@@ -517,6 +526,50 @@ static m2cg_status reinit_prepare(m2cg_ctx* x) {
   CK(cudaStreamSynchronize(x->stream));
   CK(reinit_build_graph(x->stream, a, x->nsm, 1, &x->ri_gated));
   CK(reinit_build_graph(x->stream, a, x->nsm, 0, &x->ri_now));
+  if (x->cfg.reinit_frequency > 0 || x->cfg.reinit_frequency_dt > 0) {
+    // unresolved swept cells are repaired after the step (TimeIntegrator.cpp:776-797)
+    const int cap = 4096;
+    CK(x->alloc(&a.unres, cap));
+    CK(x->alloc(&a.unres_count, 1));
+    CK(x->alloc(&a.unres_phi_old, cap));
+    CK(cudaMemsetAsync(a.unres_count, 0, sizeof(unsigned long long), x->stream));
+    a.unres_cap = cap;
+    a.cnt = x->cnt;
+    x->P.unres = a.unres;
+    x->P.unres_count = a.unres_count;
+    x->P.unres_cap = cap;
+    CK(reinit_build_graph(x->stream, a, x->nsm, 2, &x->ri_unres));
+    UnresArgs& u = x->ur;
+    u.P = x->P;
+    u.lo[0] = x->cfg.x0; u.lo[1] = x->cfg.y0; u.lo[2] = x->cfg.z0;
+    for (int m = 0; m < x->cfg.n_materials && m < M2CG_MAX_MATERIALS; m++) u.failsafe[m] = x->cfg.mat[m].failsafe_density;
+    u.S = x->S[0];
+    u.bk = a.bk;
+    u.id = x->id;
+    u.id_new = x->id_new;
+    u.cand = x->cand;
+    u.swept = x->swept;
+    u.swept_count = x->swept_count;
+    u.swept_cap = x->swept_cap;
+    u.list = a.unres;
+    u.count = a.unres_count;
+    u.phi_old = a.unres_phi_old;
+    u.cnt = x->cnt;
+    u.sc = x->sc;
+    CK(unres_build_graph(x->stream, u, x->nsm, &x->ur_exec));
+    CK(cudaStreamSynchronize(x->stream));
+  }
+  return M2CG_OK;
+}
+
+// After a step: the reinitialization and repair for unresolved swept cells
+// (both gated on the device by the step's list).
+static m2cg_status enqueue_repair(m2cg_ctx* x, int64_t* ri) {
+  if (!x->ur_exec) return M2CG_OK;
+  CK(cudaGraphLaunch(x->ri_unres, x->stream));
+  CK(cudaGraphLaunch(x->ur_exec, x->stream));
+  *ri += 1;
+  x->launches += 1;   // the repair gate; the passes are counted per repair
   return M2CG_OK;
 }
 
@@ -529,6 +582,13 @@ static m2cg_status reinit_account(m2cg_ctx* x, int64_t graph_launches) {
   CK(cudaStreamSynchronize(x->stream));
   x->launches += 2 * graph_launches + 7 * (h.bodies - x->ri_bodies_seen);
   x->ri_bodies_seen = h.bodies;
+  if (x->ur_exec) {   // 13 launches in the body of the repair graph
+    unsigned long long r = 0;
+    CK(cudaMemcpyAsync(&r, &x->cnt[CNT_UNRES_REPAIRS], sizeof(r), cudaMemcpyDeviceToHost, x->stream));
+    CK(cudaStreamSynchronize(x->stream));
+    x->launches += 13 * (int64_t)(r - x->ur_repairs_seen);
+    x->ur_repairs_seen = r;
+  }
   return M2CG_OK;
 }
 
@@ -572,6 +632,8 @@ void m2cg_destroy(m2cg_ctx* x) {
   if (x->graph_exec) cudaGraphExecDestroy(x->graph_exec);
   if (x->ri_gated) cudaGraphExecDestroy(x->ri_gated);
   if (x->ri_now) cudaGraphExecDestroy(x->ri_now);
+  if (x->ri_unres) cudaGraphExecDestroy(x->ri_unres);
+  if (x->ur_exec) cudaGraphExecDestroy(x->ur_exec);
   for (void* p : x->allocs) cudaFree(p);
   for (void* p : x->batch) cudaFree(p);
   if (x->batch_scratch) cudaFree(x->batch_scratch);
@@ -719,9 +781,69 @@ m2cg_status m2cg_advance(m2cg_ctx* x, double dt) {
     CK(cudaGraphLaunch(x->ri_gated, x->stream));
     ri = 1;
   }
+  { m2cg_status st = enqueue_repair(x, &ri); if (st != M2CG_OK) return st; }
   CK(cudaStreamSynchronize(x->stream));
   CK(cudaGetLastError());
   return reinit_account(x, ri);
+}
+
+// Probe points: ProbeOutput::SetupInterpolation (ProbeOutput.cpp:360-480) on
+// the host, then the interpolation on the device.
+m2cg_status m2cg_sample_points(m2cg_ctx* x, int32_t n, const double* xyz, double* out) {
+  if (!x || n < 0 || (n > 0 && (!xyz || !out))) { set_err("bad argument"); return M2CG_ERR_INVALID_ARG; }
+  if (n == 0) return M2CG_OK;
+  if (n > (1 << 20)) { set_err("at most 2^20 probe points per call"); return M2CG_ERR_INVALID_ARG; }
+  const Grid& g = x->P.g;
+  const int nn[3] = {g.nx, g.ny, g.nz};
+  const double lo[3] = {x->cfg.x0, x->cfg.y0, x->cfg.z0};
+  const double h[3] = {g.dx, g.dy, g.dz};
+  auto coord = [&](int d, int gi) { return lo[d] + 0.5 * h[d] + (double)(gi - 1) * h[d]; };   // ghosted index gi
+  std::vector<ProbePoint> pts((size_t)n);
+  for (int q = 0; q < n; q++) {
+    ProbePoint& p = pts[q];
+    int ijk[3];
+    for (int d = 0; d < 3; d++) {
+      const double v = xyz[3 * q + d];
+      const int np = nn[d] + 2;
+      if (!(v >= coord(d, 0)) || !(v < coord(d, np - 1))) {
+        set_err("cannot locate probe node %d in the domain", q);
+        return M2CG_ERR_INVALID_ARG;
+      }
+      int i = 0;
+      while (i < np - 1 && !(v < coord(d, i + 1))) i++;   // first ghosted i with v < c[i+1]
+      ijk[d] = i;
+      p.w[d] = (v - coord(d, i)) / (coord(d, i + 1) - coord(d, i));
+    }
+    p.i = ijk[0]; p.j = ijk[1]; p.k = ijk[2];
+    p.valid = 0;
+    p.nvalid = 0;
+    p.pad = 0;
+    for (int m = 0; m < 8; m++) {
+      const int c[3] = {ijk[0] + (m & 1), ijk[1] + ((m >> 1) & 1), ijk[2] + ((m >> 2) & 1)};
+      int ghost_dirs = 0;
+      for (int d = 0; d < 3; d++) ghost_dirs += (c[d] == 0 || c[d] == nn[d] + 1) ? 1 : 0;
+      if (ghost_dirs <= 1) { p.valid |= 1u << m; p.nvalid++; }
+    }
+    if (p.nvalid == 0) {
+      set_err("probe node %d is too close to the edges of the domain boundary", q);
+      return M2CG_ERR_INVALID_ARG;
+    }
+  }
+  const int nf = 6 + (x->P.n_ls > 0 ? 1 : 0);
+  cudaStream_t s = x->stream;
+  ProbePoint* dp = nullptr;
+  double* dout = nullptr;
+  CK(cudaMallocAsync(&dp, (size_t)n * sizeof(ProbePoint), s));
+  CK(cudaMallocAsync(&dout, (size_t)n * nf * sizeof(double), s));
+  CK(cudaMemcpyAsync(dp, pts.data(), (size_t)n * sizeof(ProbePoint), cudaMemcpyHostToDevice, s));
+  launch_sample_points(s, x->P, x->S[0], x->id, dp, n, dout);
+  x->launches += 1;
+  CK(cudaMemcpyAsync(out, dout, (size_t)n * nf * sizeof(double), cudaMemcpyDeviceToHost, s));
+  CK(cudaFreeAsync(dp, s));
+  CK(cudaFreeAsync(dout, s));
+  CK(cudaStreamSynchronize(s));
+  CK(cudaGetLastError());
+  return M2CG_OK;
 }
 
 m2cg_status m2cg_get_reinit_stats(m2cg_ctx* x, m2cg_reinit_stats* out) {
@@ -778,8 +900,9 @@ m2cg_status m2cg_get_counters(m2cg_ctx* x, m2cg_counters* c) {
   c->cfl = s.cfl;
   c->riemann_fallbacks = (int64_t)h[CNT_FALLBACK];
   c->path_capped = (int64_t)h[CNT_PATH_CAPPED];
-  if (h[CNT_IF_OVERFLOW] || h[CNT_SWEPT_OVERFLOW]) {
-    set_err("interface or swept-cell list overflow");
+  c->unresolved_fixed = (int64_t)h[CNT_UNRES_FIXED];
+  if (h[CNT_IF_OVERFLOW] || h[CNT_SWEPT_OVERFLOW] || h[CNT_UNRES_OVERFLOW]) {
+    set_err("interface, swept-cell or unresolved-cell list overflow");
     return M2CG_ERR_CAPACITY;
   }
   return M2CG_OK;
@@ -834,6 +957,8 @@ m2cg_status m2cg_run(m2cg_ctx* x, int32_t n_steps, m2cg_counters* counters) {
       CK(cudaGraphLaunch(x->ri_gated, s));
       ri++;
     }
+    m2cg_status st = enqueue_repair(x, &ri);
+    if (st != M2CG_OK) return st;
   }
   CK(cudaStreamSynchronize(s));
   CK(cudaGetLastError());

@@ -51,7 +51,8 @@ M2CG_DEV bool ghost_face_cell(const Grid& g, int64_t t, int& side, int& i, int& 
 // Device counter slots (int64).
 enum {
   CNT_IFACE = 0, CNT_RERR, CNT_RITER, CNT_RSOLVE, CNT_CLIPCELL, CNT_CLIPFACE, CNT_BAD, CNT_SWEPT, CNT_UNRES,
-  CNT_IF_OVERFLOW, CNT_PATH_CAPPED, CNT_SWEPT_OVERFLOW, CNT_BADID, CNT_FALLBACK, CNT_N
+  CNT_IF_OVERFLOW, CNT_PATH_CAPPED, CNT_SWEPT_OVERFLOW, CNT_BADID, CNT_FALLBACK, CNT_UNRES_FIXED,
+  CNT_UNRES_OVERFLOW, CNT_UNRES_REPAIRS, CNT_N
 };
 
 // Scalars that live on the device for the whole run (no host round trip per step).
@@ -75,6 +76,11 @@ struct Params {
   double inlet[5], inlet2[5];
   int n_ls, ls_matid;
   int ls_bc[6];
+  // unresolved swept cells of the current step, listed for the repair that
+  // follows a step when reinitialization is configured (else NULL)
+  int64_t* unres;
+  unsigned long long* unres_count;
+  int unres_cap;
   int ls_fv;            // finite-volume level set (else finite difference)
   int ls_flux, ls_rec_linear, ls_limiter;
   double ls_delta, ls_minmod;
@@ -116,10 +122,33 @@ struct ReinitState {
   int restore;                   // the next first sub-stage restarts from the backup
   int iter;                      // iteration of the current attempt
   int body_runs;                 // loop-body executions of the current call (bounded)
-  int pad;
+  int keep;                      // write the backup even when the loop does not run
   double cfl;                    // pseudo-time CFL; reduced by 1.5 per retry and kept
   long long calls, iterations, retries, failures, bodies;
   double last_res, last_dphi;
+};
+
+// The repair of the step's unresolved swept cells (TimeIntegrator.cpp:776-797)
+// after the reinitialization that it forces: the IDs follow the sign changes
+// of phi (MultiPhaseOperator.cpp:153-357 against the phi before the repair),
+// then FixUnresolvedNodes (MultiPhaseOperator.cpp:1279-1480) and clipping.
+struct UnresArgs {
+  Params P;
+  double lo[3];                          // domain origin: cell centres at lo + 0.5 h + i h
+  double failsafe[M2CG_MAX_MATERIALS];   // Material.FailSafeDensity
+  StateSet S;                            // the solution (V and phi)
+  double* bk;                            // phi before the repair (the reinitialization's backup)
+  int32_t* id;
+  int32_t* id_new;
+  int32_t* cand;
+  int64_t* swept;                        // cells whose sign changed in the repair
+  unsigned long long* swept_count;
+  int64_t swept_cap;
+  const int64_t* list;                   // the unresolved cells, sorted by index
+  const unsigned long long* count;
+  const double* phi_old;                 // their phi before the sign flip
+  unsigned long long* cnt;
+  const DevScalars* sc;
 };
 
 struct ReinitArgs {
@@ -140,6 +169,24 @@ struct ReinitArgs {
   uint8_t* tag;        // first-layer nodes (held fixed)
   ReinitState* st;
   const DevScalars* sc;
+  // the step's unresolved swept cells (the repair's reinitialization runs when
+  // there are any: the list is sorted, their phi saved and made negative)
+  int64_t* unres;
+  unsigned long long* unres_count;
+  int unres_cap;
+  double* unres_phi_old;
+  unsigned long long* cnt;
+};
+
+// A probe point located on the ghosted cell-centre grid: lower corner
+// (ghosted indices), populated corners (bit m: corner m in the order c000,
+// c100, c010, c110, c001, c101, c011, c111) and trilinear coordinates.
+struct ProbePoint {
+  int i, j, k;
+  unsigned valid;
+  int nvalid;
+  int pad;
+  double w[3];
 };
 
 struct StageArgs {

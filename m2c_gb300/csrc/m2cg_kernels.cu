@@ -921,7 +921,14 @@ __device__ __forceinline__ void k_swept_update_body(const Params& P, const State
           }
       if (sum_w > 0) { counter = 1; for (int p = 0; p < 5; p++) out[p] = vs[p] / sum_w; }
     }
-    if (counter == 0) { atomic_inc(&cnt[CNT_UNRES]); continue; }
+    if (counter == 0) {
+      atomic_inc(&cnt[CNT_UNRES]);
+      if (P.unres) {
+        const unsigned long long u = atomicAdd(P.unres_count, 1ull);
+        if (u < (unsigned long long)P.unres_cap) P.unres[u] = c;
+      }
+      continue;
+    }
     const DevMat& M = P.mats.m[myid];
     eos_clip(M, out);
     if (eos_bad5(M, out)) atomic_inc(&cnt[CNT_BAD]);
@@ -1108,17 +1115,27 @@ void launch_compact(cudaStream_t s, const Params& P, const int32_t* id, const If
   int64_t n = (int64_t)(P.g.nx + 1) * (P.g.ny + 1) * (P.g.nz + 1);
   k_compact_interfaces<<<nblk(n, 256), 256, 0, s>>>(P, id, L, cnt, sc);
 }
+// The "remaining" cells of a swept list take their IDs from their neighbours
+// (three passes; six launches).
+void launch_resolve_remaining(cudaStream_t s, const Params& P, int32_t* id_new, const int64_t* swept,
+                              const unsigned long long* swept_count, int64_t swept_cap, int32_t* cand,
+                              const DevScalars* sc, int nsm) {
+  const int passes = 3;
+  for (int p = 0; p < passes; p++) {
+    k_resolve_remaining<<<nsm * 2, 256, 0, s>>>(P, id_new, swept, swept_count, swept_cap, cand, p == passes - 1, sc);
+    k_commit_remaining<<<nsm * 2, 256, 0, s>>>(id_new, swept, swept_count, swept_cap, cand, sc);
+  }
+}
+void launch_commit_ids(cudaStream_t s, int32_t* id, const int32_t* id_new, const int64_t* swept,
+                       const unsigned long long* swept_count, int64_t swept_cap, const DevScalars* sc, int nsm) {
+  k_commit_ids<<<nsm * 2, 256, 0, s>>>(id, id_new, swept, swept_count, swept_cap, sc);
+}
 void launch_end_of_step(cudaStream_t s, const Params& P, const StateSet& S, int32_t* id, int32_t* id_new,
                         const IfaceList& L, const int64_t* swept, const unsigned long long* swept_count,
                         int64_t swept_cap, int32_t* cand, unsigned long long* cnt, const DevScalars* sc, int nsm) {
-  int blocks = nsm * 2;
-  const int passes = 3;
-  for (int p = 0; p < passes; p++) {
-    k_resolve_remaining<<<blocks, 256, 0, s>>>(P, id_new, swept, swept_count, swept_cap, cand, p == passes - 1, sc);
-    k_commit_remaining<<<blocks, 256, 0, s>>>(id_new, swept, swept_count, swept_cap, cand, sc);
-  }
-  k_swept_update<<<blocks, 128, 0, s>>>(P, S, id, id_new, L, swept, swept_count, swept_cap, cnt, sc);
-  k_commit_ids<<<blocks, 256, 0, s>>>(id, id_new, swept, swept_count, swept_cap, sc);
+  launch_resolve_remaining(s, P, id_new, swept, swept_count, swept_cap, cand, sc, nsm);
+  k_swept_update<<<nsm * 2, 128, 0, s>>>(P, S, id, id_new, L, swept, swept_count, swept_cap, cnt, sc);
+  launch_commit_ids(s, id, id_new, swept, swept_count, swept_cap, sc, nsm);
   launch_bc(s, P, S, 1, 1, id, sc);
 }
 void launch_conserved(cudaStream_t s, const Params& P, const StateSet& S, const int32_t* id, double* partial,

@@ -26,6 +26,12 @@
 
 namespace m2cg {
 
+void launch_bc(cudaStream_t, const Params&, const StateSet&, int, int, int32_t*, const DevScalars*);
+void launch_resolve_remaining(cudaStream_t, const Params&, int32_t*, const int64_t*, const unsigned long long*,
+                              int64_t, int32_t*, const DevScalars*, int);
+void launch_commit_ids(cudaStream_t, int32_t*, const int32_t*, const int64_t*, const unsigned long long*, int64_t,
+                       const DevScalars*, int);
+
 namespace {
 
 constexpr int RI_THREADS = 128;
@@ -98,18 +104,43 @@ M2CG_DEV void block_max_atomic(unsigned long long v, unsigned long long* dst) {
   }
 }
 
-// Gate: run this call?  (when gated: after every freq-th completed step, or
-// after every step that crosses a multiple of freq_dt; never with MaxIts <= 0,
-// where the reference's loop does not execute and the failsafe accepts the
-// input).
+// Gate: run this call?  gated = 1: after every freq-th completed step, or after
+// every step that crosses a multiple of freq_dt; gated = 2: when the step left
+// unresolved swept cells (TimeIntegrator.cpp:776-797), whose list is then
+// sorted into the reference's (k, j, i) order, their phi saved, and made
+// negative where it is not (MultiPhaseOperator.cpp:1364-1420); never with
+// MaxIts <= 0, where the reference's loop does not execute and the failsafe
+// accepts the input.
 __global__ void k_ri_begin(ReinitArgs a, cudaGraphConditionalHandle h, int gated) {
   ReinitState* st = a.st;
   bool go = a.max_its > 0;
-  if (gated) {   // Utils.cpp:337-357: the time interval when given, else the step count
+  st->keep = 0;
+  if (gated == 1) {   // Utils.cpp:337-357: the time interval when given, else the step count
     bool due;
     if (a.freq_dt > 0) due = floor(a.sc->time / a.freq_dt) != floor((a.sc->time - a.sc->dt) / a.freq_dt);
     else due = a.freq > 0 && (a.sc->steps % a.freq) == 0;
     go = go && a.sc && a.sc->active && due;
+  } else if (gated == 2) {
+    unsigned long long n = *a.unres_count;
+    if (n > (unsigned long long)a.unres_cap) {
+      a.cnt[CNT_UNRES_OVERFLOW] += 1;
+      n = (unsigned long long)a.unres_cap;
+      *a.unres_count = n;
+    }
+    int64_t* L = a.unres;
+    for (unsigned long long s = 1; s < n; s++) {   // insertion sort: the list is short
+      const int64_t v = L[s];
+      unsigned long long t = s;
+      for (; t > 0 && L[t - 1] > v; t--) L[t] = L[t - 1];
+      L[t] = v;
+    }
+    for (unsigned long long s = 0; s < n; s++) {
+      const double p = a.phi[L[s]];
+      a.unres_phi_old[s] = p;
+      if (!(p < 0)) a.phi[L[s]] = -p;
+    }
+    st->keep = n > 0 ? 1 : 0;
+    go = go && n > 0;
   }
   st->run = go ? 1 : 0;
   st->detected = 0;
@@ -125,7 +156,7 @@ __global__ void k_ri_begin(ReinitArgs a, cudaGraphConditionalHandle h, int gated
 // and the smoothed sign phi / sqrt(phi^2 + h_min^2) on the interior.
 __global__ void __launch_bounds__(RI_THREADS) k_ri_prep(ReinitArgs a) {
   ReinitState* st = a.st;
-  if (!st->run) return;
+  if (!st->run && !st->keep) return;
   const Grid& g = a.g;
   for (int64_t t = (int64_t)blockIdx.x * RI_THREADS + threadIdx.x; t < g.ntot; t += (int64_t)gridDim.x * RI_THREADS)
     a.bk[t] = a.phi[t];
@@ -296,6 +327,170 @@ __global__ void k_ri_ctl(ReinitArgs a, cudaGraphConditionalHandle h) {
   cudaGraphSetConditional(h, more ? 1u : 0u);
 }
 
+// ---------------------------------------------------------------------------
+// Repair of the step's unresolved swept cells, after the reinitialization that
+// the gate of mode 2 ran.  One graph: a one-thread gate, then an IF node whose
+// body restores the saved phi of the listed cells into the backup (which then
+// holds phi as it was before the repair), moves the IDs of the cells whose
+// sign changed, repairs the listed cells' states and clips them.
+
+M2CG_DEV void cell_ijk(const Grid& g, int64_t c, int& i, int& j, int& k) {
+  int64_t r = c;
+  i = (int)(r % g.px) - 1; r /= g.px;
+  j = (int)(r % g.py) - 1;
+  k = (int)(r / g.py) - 1;
+}
+
+// whether c is in the sorted list
+M2CG_DEV bool listed(const int64_t* L, int64_t n, int64_t c) {
+  int64_t lo = 0, hi = n;
+  while (lo < hi) {
+    const int64_t m = (lo + hi) >> 1;
+    if (L[m] < c) lo = m + 1;
+    else hi = m;
+  }
+  return lo < n && L[lo] == c;
+}
+
+__global__ void k_ur_begin(UnresArgs a, cudaGraphConditionalHandle h) {
+  const bool go = *a.count > 0;
+  if (go) {
+    *a.swept_count = 0;
+    a.cnt[CNT_UNRES_REPAIRS] += 1;
+  }
+  cudaGraphSetConditional(h, go ? 1u : 0u);
+}
+
+__global__ void k_ur_restore(UnresArgs a) {
+  const int64_t n = (int64_t)*a.count;
+  for (int64_t s = threadIdx.x; s < n; s += blockDim.x) a.bk[a.list[s]] = a.phi_old[s];
+}
+
+// MultiPhaseOperator::UpdateMaterialIDByLevelSet against the phi before the
+// repair (MultiPhaseOperator.cpp:190-222): a sign change makes the cell the
+// level set's material when phi < 0, else a "remaining" cell resolved from its
+// neighbours by the passes that follow.
+__global__ void __launch_bounds__(256) k_ur_mark(UnresArgs a) {
+  const Grid& g = a.P.g;
+  const double* phi = a.S.q[5];
+  const int64_t rows = (int64_t)g.ny * g.nz;
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int k = (int)(r / g.ny), j = (int)(r - (int64_t)k * g.ny);
+    const int64_t base = g.at(0, j, k);
+    for (int i = threadIdx.x; i < g.nx; i += blockDim.x) {
+      const int64_t c = base + i;
+      const double ph = phi[c];
+      if (ph * a.bk[c] > 0.0) continue;
+      const int nid = ph < 0 ? a.P.ls_matid : -1 - a.id[c];
+      const unsigned long long s = atomicAdd(a.swept_count, 1ull);
+      if ((int64_t)s < a.swept_cap) a.swept[s] = c;
+      else atomicAdd(&a.cnt[CNT_SWEPT_OVERFLOW], 1ull);
+      a.id_new[c] = nid;
+    }
+  }
+}
+
+// MultiPhaseOperator::FixUnresolvedNodes (MultiPhaseOperator.cpp:1279-1480, no
+// embedded surfaces), one thread in list order: each cell takes the upwind-
+// weighted mean of its resolved same-material neighbours (weight = max(0,
+// unit neighbour velocity . unit direction from the neighbour to the cell)),
+// else their inverse-distance mean, else keeps velocity and pressure and
+// takes an inverse-distance density over up to 10 layers, else the material's
+// failsafe density.  The flag that marks the first accumulated neighbour is
+// set once for the whole list, as in the reference (line 1296): later cells
+// accumulate onto their own advected state.
+__global__ void k_ur_fix(UnresArgs a) {
+  const int64_t n = (int64_t)*a.count;
+  const Grid& g = a.P.g;
+  const double h[3] = {g.dx, g.dy, g.dz};
+  double* const* q = a.S.q;
+  const int32_t* id = a.id;
+  bool reset = false;
+  for (int64_t s = 0; s < n; s++) {
+    const int64_t c = a.list[s];
+    int i, j, k;
+    cell_ijk(g, c, i, j, k);
+    const int myid = id[c];
+    const int pos[3] = {i, j, k};
+    double x0[3];
+    for (int d = 0; d < 3; d++) x0[d] = a.lo[d] + 0.5 * h[d] + pos[d] * h[d];
+    double sw = 0.0, sw2 = 0.0, vt[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int nk = k - 1; nk <= k + 1; nk++)
+      for (int nj = j - 1; nj <= j + 1; nj++)
+        for (int ni = i - 1; ni <= i + 1; ni++) {
+          if (ni < 0 || ni >= g.nx || nj < 0 || nj >= g.ny || nk < 0 || nk >= g.nz) continue;
+          const int64_t nc = g.at(ni, nj, nk);
+          if (id[nc] != myid || nc == c || listed(a.list, n, nc)) continue;
+          const int npos[3] = {ni, nj, nk};
+          double x1[3], v1[3], dv[3];
+          for (int d = 0; d < 3; d++) x1[d] = a.lo[d] + 0.5 * h[d] + npos[d] * h[d];
+          for (int d = 0; d < 3; d++) v1[d] = q[1 + d][nc];
+          const double v1norm = sqrt(v1[0] * v1[0] + v1[1] * v1[1] + v1[2] * v1[2]);
+          if (v1norm != 0) { const double r = 1.0 / v1norm; for (int d = 0; d < 3; d++) v1[d] *= r; }
+          for (int d = 0; d < 3; d++) dv[d] = x0[d] - x1[d];
+          const double dn = sqrt(dv[0] * dv[0] + dv[1] * dv[1] + dv[2] * dv[2]);
+          { const double r = 1.0 / dn; for (int d = 0; d < 3; d++) dv[d] *= r; }
+          const double dot = dv[0] * v1[0] + dv[1] * v1[1] + dv[2] * v1[2];
+          const double w = 0.0 < dot ? dot : 0.0;
+          if (w > 0) {
+            sw += w;
+            for (int p = 0; p < 5; p++) {
+              if (reset) q[p][c] += w * q[p][nc];
+              else q[p][c] = w * q[p][nc];
+            }
+            reset = true;
+          }
+          for (int p = 0; p < 5; p++) vt[p] += 1.0 / dn * q[p][nc];
+          sw2 += 1.0 / dn;
+        }
+    if (a.P.mp_pcdir == M2CG_PCDIR_UPWIND && sw > 0) {
+      const double r = 1.0 / sw;
+      for (int p = 0; p < 5; p++) q[p][c] *= r;
+      continue;
+    }
+    if (sw2 > 0) {
+      for (int p = 0; p < 5; p++) q[p][c] = vt[p] / sw2;
+      continue;
+    }
+    double density = 0.0;
+    for (int layer = 1; layer <= 10; layer++) {
+      for (int nk = k - layer; nk <= k + layer; nk++)
+        for (int nj = j - layer; nj <= j + layer; nj++)
+          for (int ni = i - layer; ni <= i + layer; ni++) {
+            if (ni < 0 || ni >= g.nx || nj < 0 || nj >= g.ny || nk < 0 || nk >= g.nz) continue;
+            const int64_t nc = g.at(ni, nj, nk);
+            if (id[nc] != myid || nc == c || listed(a.list, n, nc)) continue;
+            const int npos[3] = {ni, nj, nk};
+            double x1[3];
+            for (int d = 0; d < 3; d++) x1[d] = a.lo[d] + 0.5 * h[d] + npos[d] * h[d];
+            const double dist = sqrt((x1[0] - x0[0]) * (x1[0] - x0[0]) + (x1[1] - x0[1]) * (x1[1] - x0[1]) +
+                                     (x1[2] - x0[2]) * (x1[2] - x0[2]));
+            sw += 1.0 / dist;
+            density += (1.0 / dist) * q[0][nc];
+          }
+      if (sw > 0) { q[0][c] = density / sw; break; }
+    }
+    if (sw == 0) q[0][c] = a.failsafe[myid];
+  }
+  a.cnt[CNT_UNRES_FIXED] += (unsigned long long)n;
+}
+
+// ClipDensityAndPressure (TimeIntegrator.cpp:800) of the repaired cells and of
+// the cells whose ID the repair changed.
+__global__ void k_ur_clip(UnresArgs a) {
+  const int64_t n = (int64_t)*a.count;
+  const int64_t m = (int64_t)min((unsigned long long)a.swept_cap, *a.swept_count);
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n + m; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t c = t < n ? a.list[t] : a.swept[t - n];
+    const DevMat& M = a.P.mats.m[a.id[c]];
+    double V[5];
+    for (int p = 0; p < 5; p++) V[p] = a.S.q[p][c];
+    eos_clip(M, V);
+    if (t < n && eos_bad5(M, V)) atomicAdd(&a.cnt[CNT_BAD], 1ull);
+    for (int p = 0; p < 5; p++) a.S.q[p][c] = V[p];
+  }
+}
+
 }  // namespace
 
 // The reinitialization graph: gate, preparation, then the WHILE loop.
@@ -353,6 +548,63 @@ cudaError_t reinit_build_graph(cudaStream_t s, const ReinitArgs& a, int nsm, int
   return cudaSuccess;
 fail:
 #undef RI_CK
+  cudaGraphDestroy(g);
+  return e;
+}
+
+// The repair graph: gate, then the IF node with the repair passes.
+cudaError_t unres_build_graph(cudaStream_t s, const UnresArgs& a, int nsm, cudaGraphExec_t* out) {
+  *out = nullptr;
+  cudaGraph_t g = nullptr;
+  cudaError_t e = cudaGraphCreate(&g, 0);
+  if (e != cudaSuccess) return e;
+  cudaGraphConditionalHandle h;
+  const int64_t rows = (int64_t)a.P.g.ny * a.P.g.nz;
+  const int mblocks = (int)std::min<int64_t>(rows, (int64_t)nsm * 8);
+  cudaGraphNodeParams np = {};
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  cudaStreamCaptureStatus cs;
+  cudaGraph_t cap = nullptr, body = nullptr;
+  cudaGraphNode_t cn;
+#define UR_CK(x) do { e = (x); if (e != cudaSuccess) goto fail; } while (0)
+  UR_CK(cudaGraphConditionalHandleCreate(&h, g, 0, cudaGraphCondAssignDefault));
+  UR_CK(cudaStreamBeginCaptureToGraph(s, g, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  k_ur_begin<<<1, 1, 0, s>>>(a, h);
+  e = cudaStreamGetCaptureInfo(s, &cs, nullptr, nullptr, &deps, nullptr, &nd);
+  if (e == cudaSuccess) {
+    np.type = cudaGraphNodeTypeConditional;
+    np.conditional.handle = h;
+    np.conditional.type = cudaGraphCondTypeIf;
+    np.conditional.size = 1;
+    e = cudaGraphAddNode(&cn, g, deps, nullptr, nd, &np);
+  }
+  if (e == cudaSuccess) e = cudaStreamUpdateCaptureDependencies(s, &cn, nullptr, 1, cudaStreamSetCaptureDependencies);
+  {
+    cudaError_t e2 = cudaStreamEndCapture(s, &cap);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (e != cudaSuccess) goto fail;
+  body = np.conditional.phGraph_out[0];
+  UR_CK(cudaStreamBeginCaptureToGraph(s, body, nullptr, nullptr, 0, cudaStreamCaptureModeThreadLocal));
+  k_ur_restore<<<1, 256, 0, s>>>(a);
+  k_ur_mark<<<mblocks, 256, 0, s>>>(a);
+  launch_resolve_remaining(s, a.P, a.id_new, a.swept, a.swept_count, a.swept_cap, a.cand, a.sc, nsm);
+  launch_commit_ids(s, a.id, a.id_new, a.swept, a.swept_count, a.swept_cap, a.sc, nsm);
+  launch_bc(s, a.P, a.S, 0, 0, a.id, a.sc);   // ID ghosts (MultiPhaseOperator.cpp:919-942)
+  k_ur_fix<<<1, 1, 0, s>>>(a);
+  k_ur_clip<<<nsm, 256, 0, s>>>(a);
+  launch_bc(s, a.P, a.S, 1, 0, nullptr, a.sc);   // V ghosts
+  {
+    cudaError_t e2 = cudaStreamEndCapture(s, &cap);
+    if (e == cudaSuccess) e = e2;
+  }
+  if (e != cudaSuccess) goto fail;
+  UR_CK(cudaGraphInstantiate(out, g, 0));
+  cudaGraphDestroy(g);
+  return cudaSuccess;
+fail:
+#undef UR_CK
   cudaGraphDestroy(g);
   return e;
 }

@@ -1425,6 +1425,7 @@ void orc_counters(void* h, m2cg_counters* c) {
   c->dt = o->last_dt;
   c->cfl = o->last_cfl;
   c->riemann_fallbacks = o->cnt.fallbacks;
+  c->unresolved_fixed = o->cnt.unresolved_fixed;
 }
 
 void orc_conserved_totals(void* h, double* tot) {
