@@ -26,6 +26,7 @@ UNITS = {
     "m2cg_mlp.cu": [],
     "m2cg_reinit.cu": ["-fmad=false"],
     "m2cg_peak.cu": [],
+    "m2cg_probe.cu": ["-fmad=false"],
 }
 
 

@@ -18,6 +18,9 @@ plots that go with them.
   points evenly spaced on the segment, trilinear interpolation over the
   ghosted cell-centre grid with unpopulated edge / corner ghosts replaced by
   the mean of the populated corners, output in the reference's format.
+* `ProbeOutput`: time histories at the probe nodes of `Output.Probes`
+  (ProbeOutput.cpp:14-350, 599-848; IoData.cpp:3152-3230), written when
+  Utils.cpp:337-357 says so, one file per requested field.
 
 Anything the path does not implement (other EOS, non-uniform meshes, other
 geometric entities, narrow bands, other reinitialization treatments) raises
@@ -269,6 +272,8 @@ class Case:
         self.cfg = None
         self.V = self.ID = self.phi = None
         self.line_plots = []
+        self.probes = None
+        self.prefix = ""
         self.max_time = 1e10
         self.max_its = 2 ** 31 - 1
         self.variable_type = "Primitive"
@@ -428,6 +433,9 @@ class Case:
                                     "x0": [float(d.get("X0", 0.0)), float(d.get("Y0", 0.0)), float(d.get("Z0", 0.0))],
                                     "x1": [float(d.get("Xmax", 0.0)), float(d.get("Ymax", 0.0)),
                                            float(d.get("Zmax", 0.0))]})
+        self.prefix = str(out.get("Prefix", ""))
+        if "Probes" in out:
+            self.probes = _probes(out["Probes"])
         return self
 
     # -- initial state -------------------------------------------------------
@@ -504,9 +512,96 @@ class Case:
 # Line plots
 
 
+# probe files of the path (Probes::setup, IoData.cpp:3198-3230) and the column
+# of each in the sampled values
+_PROBE_FIELDS = {"Density": 0, "VelocityX": 1, "VelocityY": 2, "VelocityZ": 3, "Pressure": 4, "MaterialID": 5,
+                 "LevelSet0": 6, "LevelSet1": 7, "LevelSet2": 8, "LevelSet3": 9, "LevelSet4": 10}
+_PROBE_UNSUPPORTED = ("Temperature", "DeltaTemperature", "LaserRadiance", "LaserIrradiance", "IonizationResult",
+                      "ReferenceMap", "PrincipalElasticStresses")
+
+
+def _probes(pr):
+    """Output.Probes: frequency (default -100: only forced writes), time
+    interval, file per field, and the node locations (ProbeOutput.cpp:14-45)."""
+    for k in _PROBE_UNSUPPORTED:
+        if pr.get(k):
+            raise NotImplementedError(f"Output.Probes.{k}")
+    nodes = pr.get("Node", {})
+    locs = [None] * len(nodes)
+    for i, d in nodes.items():
+        if not 0 <= int(i) < len(nodes):
+            raise ValueError(f"Probe node index ({i}) out of range. Should be between 0 and {len(nodes) - 1}.")
+        locs[int(i)] = (float(d.get("X", -1.0e20)), float(d.get("Y", -1.0e20)), float(d.get("Z", -1.0e20)))
+    files = {k: str(pr[k]) for k in _PROBE_FIELDS if pr.get(k)}
+    return {"frequency": int(pr.get("Frequency", -100)), "frequency_dt": float(pr.get("TimeInterval", -1.0)),
+            "files": files, "nodes": locs}
+
+
 def _ghost_coords(n, lo, hi):
     h = (hi - lo) / n
     return lo + 0.5 * h + np.arange(-1, n + 1) * h     # ghosted cell centres
+
+
+def locate_points(cfg, points):
+    """ProbeOutput::SetupInterpolation (ProbeOutput.cpp:360-480) for points on
+    the ghosted cell-centre grid: per point the ghosted indices (i, j, k) of
+    the lower corner, the trilinear coordinates and which of the eight corners
+    are populated (edge and corner ghosts are not)."""
+    nx, ny, nz = cfg.nx, cfg.ny, cfg.nz
+    px, py, pz = nx + 2, ny + 2, nz + 2
+    cx = _ghost_coords(nx, cfg.x0, cfg.xmax)
+    cy = _ghost_coords(ny, cfg.y0, cfg.ymax)
+    cz = _ghost_coords(nz, cfg.z0, cfg.zmax)
+
+    def locate(c, v):
+        # first ghosted index i with v < c[i+1] (ProbeOutput.cpp:392-413)
+        for i in range(len(c) - 1):
+            if v < c[i + 1]:
+                return i, (v - c[i]) / (c[i + 1] - c[i])
+        raise ValueError("probe point outside the mesh")
+
+    def populated(i, j, k):
+        out = (i == 0 or i == px - 1) + (j == 0 or j == py - 1) + (k == 0 or k == pz - 1)
+        return out <= 1
+
+    setup = []
+    for q, p in enumerate(points):
+        if (p[0] < cx[0] or p[0] >= cx[-1] or p[1] < cy[0] or p[1] >= cy[-1] or p[2] < cz[0] or p[2] >= cz[-1]):
+            raise ValueError(f"cannot locate probe node {q} in the domain")
+        (i, xi), (j, eta), (k, zeta) = locate(cx, p[0]), locate(cy, p[1]), locate(cz, p[2])
+        corners = [(i, j, k), (i + 1, j, k), (i, j + 1, k), (i + 1, j + 1, k),
+                   (i, j, k + 1), (i + 1, j, k + 1), (i, j + 1, k + 1), (i + 1, j + 1, k + 1)]
+        valid = [populated(*cc) for cc in corners]
+        if not any(valid):
+            raise ValueError(f"probe node {q} is too close to the edges of the domain boundary")
+        setup.append(((i, j, k), (xi, eta, zeta), valid))
+    return setup
+
+
+def interpolate_points(cfg, setup, fields):
+    """ProbeOutput::InterpolateSolutionAtProbe (ProbeOutput.cpp:849-886): each
+    field (a ghosted array, i fastest) at each located point; unpopulated
+    corners take the mean of the populated ones.  Returns (points, fields)."""
+    px, py = cfg.nx + 2, cfg.ny + 2
+    out = np.zeros((len(setup), len(fields)))
+    for q, ((i, j, k), (xi, eta, zeta), valid) in enumerate(setup):
+        corners = [(i, j, k), (i + 1, j, k), (i, j + 1, k), (i + 1, j + 1, k),
+                   (i, j, k + 1), (i + 1, j, k + 1), (i, j + 1, k + 1), (i + 1, j + 1, k + 1)]
+        lin = [(kk * py + jj) * px + ii for ii, jj, kk in corners]
+        for fi, f in enumerate(fields):
+            cvals = [f[l] if v else 0.0 for l, v in zip(lin, valid)]
+            if sum(valid) < 8:
+                avg = sum(cvals) / sum(valid)
+                cvals = [cv if v else avg for cv, v in zip(cvals, valid)]
+            c000, c100, c010, c110, c001, c101, c011, c111 = cvals
+            c00 = c000 * (1.0 - xi) + c100 * xi        # MathTools/trilinear_interpolation.h:50-62
+            c01 = c001 * (1.0 - xi) + c101 * xi
+            c10 = c010 * (1.0 - xi) + c110 * xi
+            c11 = c011 * (1.0 - xi) + c111 * xi
+            c0 = c00 * (1.0 - eta) + c10 * eta
+            c1 = c01 * (1.0 - eta) + c11 * eta
+            out[q, fi] = c0 * (1.0 - zeta) + c1 * zeta
+    return out
 
 
 def sample_line(cfg, plot, Vg, IDg, phig=None):
@@ -520,57 +615,72 @@ def sample_line(cfg, plot, Vg, IDg, phig=None):
     x0, x1 = np.asarray(plot["x0"], float), np.asarray(plot["x1"], float)
     dxyz = (x1 - x0) / (npts - 1)
     h = math.sqrt(float((dxyz ** 2).sum()))
-    nx, ny, nz = cfg.nx, cfg.ny, cfg.nz
-    px, py, pz = nx + 2, ny + 2, nz + 2
-    cx = _ghost_coords(nx, cfg.x0, cfg.xmax)
-    cy = _ghost_coords(ny, cfg.y0, cfg.ymax)
-    cz = _ghost_coords(nz, cfg.z0, cfg.zmax)
     fields = [Vg[p] for p in range(5)] + [IDg.astype(np.float64)]
     if phig is not None and cfg.n_levelsets:
         fields.append(phig)
-    rows = []
+    vals = interpolate_points(cfg, locate_points(cfg, [x0 + q * dxyz for q in range(npts)]), fields)
+    dist = np.array([q * h for q in range(npts)])[:, None]
+    return np.hstack([dist, vals[:, :5], np.zeros((npts, 1)), vals[:, 5:]])   # temperature column: 0
 
-    def locate(c, v):
-        # first ghosted index i with v < c[i+1] (ProbeOutput.cpp:392-413)
-        for i in range(len(c) - 1):
-            if v < c[i + 1]:
-                return i, (v - c[i]) / (c[i + 1] - c[i])
-        raise ValueError("probe point outside the mesh")
 
-    def populated(i, j, k):   # ghosted indices; edge and corner ghosts are not
-        out = (i == 0 or i == px - 1) + (j == 0 or j == py - 1) + (k == 0 or k == pz - 1)
-        return out <= 1
+def is_time_to_write(time, dt, step, frequency_dt, frequency, last, force):
+    """Utils.cpp:337-357: forced writes unless one was made at this time; else
+    the time interval when given, else the step count."""
+    if force:
+        return time > last + 0.1 * dt
+    if frequency_dt > 0:
+        return math.floor(time / frequency_dt) != math.floor((time - dt) / frequency_dt)
+    return frequency > 0 and step % frequency == 0
 
-    for q in range(npts):
-        p = x0 + q * dxyz
-        if (p[0] < cx[0] or p[0] >= cx[-1] or p[1] < cy[0] or p[1] >= cy[-1] or p[2] < cz[0] or p[2] >= cz[-1]):
-            raise ValueError(f"cannot locate probe node {q} in the domain")
-        (i, xi), (j, eta), (k, zeta) = locate(cx, p[0]), locate(cy, p[1]), locate(cz, p[2])
-        corners = [(i, j, k), (i + 1, j, k), (i, j + 1, k), (i + 1, j + 1, k),
-                   (i, j, k + 1), (i + 1, j, k + 1), (i, j + 1, k + 1), (i + 1, j + 1, k + 1)]
-        valid = [populated(*cc) for cc in corners]
-        if not any(valid):
-            raise ValueError(f"probe node {q} is too close to the edges of the domain boundary")
-        lin = [(kk * py + jj) * px + ii for ii, jj, kk in corners]
-        row = [q * h]
-        for fi, f in enumerate(fields):
-            cvals = [f[l] if v else 0.0 for l, v in zip(lin, valid)]
-            if sum(valid) < 8:
-                avg = sum(cvals) / sum(valid)
-                cvals = [cv if v else avg for cv, v in zip(cvals, valid)]
-            c000, c100, c010, c110, c001, c101, c011, c111 = cvals
-            c00 = c000 * (1.0 - xi) + c100 * xi        # MathTools/trilinear_interpolation.h:50-62
-            c01 = c001 * (1.0 - xi) + c101 * xi
-            c10 = c010 * (1.0 - xi) + c110 * xi
-            c11 = c011 * (1.0 - xi) + c111 * xi
-            c0 = c00 * (1.0 - eta) + c10 * eta
-            c1 = c01 * (1.0 - eta) + c11 * eta
-            val = c0 * (1.0 - zeta) + c1 * zeta
-            row.append(val)
-            if fi == 4:
-                row.append(0.0)   # temperature
-        rows.append(row)
-    return np.array(rows)
+
+class ProbeOutput:
+    """Time histories at the probe nodes (ProbeOutput.cpp:14-350, 599-848): one
+    file per requested field, named prefix + file name, one line per output:
+    the step, the time and the field at every node.  `write` takes the
+    ghosted state (Solver.get_state_ghosted, OracleSim.download_ghosted) or,
+    with `solver=`, samples the nodes on the device (Solver.sample_points)."""
+
+    def __init__(self, case, prefix=None):
+        p = case.probes or {"frequency": -100, "frequency_dt": -1.0, "files": {}, "nodes": []}
+        self.cfg = case.cfg
+        self.frequency, self.frequency_dt = p["frequency"], p["frequency_dt"]
+        self.nodes = [tuple(n) for n in p["nodes"]]
+        self.setup = locate_points(self.cfg, self.nodes) if self.nodes else []
+        self.last = -1.0
+        pre = case.prefix if prefix is None else prefix
+        self.files = {k: open(pre + name, "w") for k, name in p["files"].items()}
+
+    def due(self, time, dt, step, force=False):
+        return bool(self.nodes) and is_time_to_write(time, dt, step, self.frequency_dt, self.frequency,
+                                                     self.last, force)
+
+    def write(self, time, dt, step, Vg=None, IDg=None, phig=None, force=False, solver=None):
+        """Appends a line to every file when the frequency says so; returns
+        whether it wrote."""
+        if not self.due(time, dt, step, force):
+            return False
+        if solver is not None:
+            vals = solver.sample_points(self.nodes)
+        else:
+            fields = [Vg[q] for q in range(5)] + [np.asarray(IDg, np.float64)]
+            if phig is not None and self.cfg.n_levelsets:
+                fields.append(phig)
+            vals = interpolate_points(self.cfg, self.setup, fields)
+        for key, f in self.files.items():
+            col = _PROBE_FIELDS[key]
+            if col >= vals.shape[1]:   # LevelSet<n> beyond the level sets: file stays empty
+                continue
+            f.write(("%10d    %16.8e    " if key == "Density" else "%8d    %16.8e    ") % (step, time))
+            for v in vals[:, col]:
+                f.write("%16.8e    " % v)
+            f.write("\n")
+            f.flush()
+        self.last = time
+        return True
+
+    def close(self):
+        for f in self.files.values():
+            f.close()
 
 
 def write_line(path, plot, rows, time, step):

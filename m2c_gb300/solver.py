@@ -77,6 +77,16 @@ class Solver:
                   "m2cg_download_ghosted")
         return V.reshape(5, n), ID, Phi
 
+    def sample_points(self, points):
+        """The solution at probe points (ProbeOutput.cpp:360-480, 849-886), on
+        the device: rows of rho, vx, vy, vz, p, material ID, phi."""
+        pts = np.ascontiguousarray(np.asarray(points, np.float64).reshape(-1, 3))
+        nf = 6 + (1 if self.cfg.n_levelsets else 0)
+        out = np.zeros((len(pts), nf))
+        abi.check(self.lib, self.lib.m2cg_sample_points(self.ctx, len(pts), abi.dptr(pts), abi.dptr(out)),
+                  "m2cg_sample_points")
+        return out
+
     def run_to_end(self, max_time, max_its, chunk=64):
         """The Main.cpp:653-771 loop to MaxTime or MaxIts, whichever comes
         first, in chunks of graph-replayed steps; returns the counters."""
