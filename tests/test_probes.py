@@ -1,0 +1,158 @@
+"""Probe time histories (ProbeOutput.cpp:14-350, 360-480, 599-886; IoData.cpp:
+3152-3230; Utils.cpp:337-357): parsing of Output.Probes, the write schedule,
+the file layout, the interpolation (exact on fields linear in x, y, z, and
+the same numbers as the line-plot sampler), and the device sampler against
+the host one on the same ghosted state."""
+import numpy as np
+import pytest
+
+from m2c_gb300 import inputfile as inf
+
+CASE = """
+under Mesh { X0 = 0.0; Xmax = 1.0; Y0 = 0.0; Ymax = 0.5; Z0 = 0.0; Zmax = 0.25;
+  NumberOfCellsX = 16; NumberOfCellsY = 8; NumberOfCellsZ = 4;
+  BoundaryConditionX0 = Inlet; BoundaryConditionXmax = Outlet; BoundaryConditionY0 = Symmetry;
+  BoundaryConditionYmax = Symmetry; BoundaryConditionZ0 = Symmetry; BoundaryConditionZmax = Symmetry; }
+under Equations {
+  under Material[0] { EquationOfState = StiffenedGas; under StiffenedGasModel { SpecificHeatRatio = 6.12;
+                                                                               PressureConstant = 3.43e8; } }
+  under Material[1] { EquationOfState = StiffenedGas; under StiffenedGasModel { SpecificHeatRatio = 1.4; } }
+}
+under InitialCondition { under GeometricEntities {
+  under Sphere[0] { Center_x = 0.4; Center_y = 0.25; Center_z = 0.125; Radius = 0.12;
+                    under InitialState { MaterialID = 1; Density = 1.2; Pressure = 1.0e5; } } } }
+under BoundaryConditions { under Inlet { Density = 1050.0; Pressure = 5.0e7; VelocityX = 20.0; } }
+under Space { under NavierStokes { Flux = HLLC; under Reconstruction { Type = Linear; Limiter = VanAlbada; } }
+  under LevelSet[0] { MaterialID = 1; } }
+under ExactRiemannSolution { Tolerance = 1.0e-10; }
+under Time { MaxTime = 1.0; CFL = 0.4; MaxIts = 6; under Explicit { Type = RungeKutta2; } }
+under Output { Prefix = "out_";
+  under Probes { Frequency = 2; Density = "rho.txt"; Pressure = "p.txt"; VelocityX = "vx.txt";
+                 MaterialID = "id.txt"; LevelSet0 = "phi.txt"; LevelSet1 = "phi1.txt";
+                 under Node[0] { X = 0.41; Y = 0.26; Z = 0.13; }
+                 under Node[2] { X = 0.0; Y = 0.0; Z = 0.0; }
+                 under Node[1] { X = 0.97; Y = 0.49; Z = 0.01; } } }
+"""
+
+NODES = [(0.41, 0.26, 0.13), (0.97, 0.49, 0.01), (0.0, 0.0, 0.0)]
+
+
+def test_probes_are_parsed():
+    cs = inf.Case.from_text(CASE)
+    p = cs.probes
+    assert cs.prefix == "out_"
+    assert p["frequency"] == 2 and p["frequency_dt"] == -1.0
+    assert p["nodes"] == NODES
+    assert p["files"] == {"Density": "rho.txt", "Pressure": "p.txt", "VelocityX": "vx.txt", "MaterialID": "id.txt",
+                          "LevelSet0": "phi.txt", "LevelSet1": "phi1.txt"}
+
+
+@pytest.mark.parametrize("bad", ["Temperature = \"t.txt\";", "under Node[5] { X = 0.5; }"])
+def test_probe_inputs_outside_the_path_are_refused(bad):
+    text = CASE.replace("Frequency = 2;", "Frequency = 2; " + bad)
+    with pytest.raises((NotImplementedError, ValueError)):
+        inf.Case.from_text(text)
+
+
+def test_write_schedule():
+    """Utils.cpp:337-357: forced writes skip a time already written; the time
+    interval wins over the step count."""
+    w = inf.is_time_to_write
+    assert w(1.0, 0.1, 4, -1.0, 2, -1.0, False) and not w(1.0, 0.1, 3, -1.0, 2, -1.0, False)
+    assert not w(1.0, 0.1, 3, -1.0, -100, -1.0, False)
+    assert w(1.0, 0.1, 3, -1.0, -100, 0.5, True) and not w(1.0, 0.1, 3, -1.0, -100, 1.0, True)
+    assert w(0.31, 0.02, 1, 0.1, 2, -1.0, False) and not w(0.33, 0.02, 2, 0.1, 2, -1.0, False)
+
+
+def test_interpolation_is_exact_on_linear_fields_and_agrees_with_the_line_sampler():
+    cs = inf.Case.from_text(CASE)
+    c = cs.cfg
+    px, py, pz = c.nx + 2, c.ny + 2, c.nz + 2
+    h = np.array([(c.xmax - c.x0) / c.nx, (c.ymax - c.y0) / c.ny, (c.zmax - c.z0) / c.nz])
+    ii, jj, kk = np.meshgrid(np.arange(px), np.arange(py), np.arange(pz), indexing="ij")
+    xg = (c.x0 + (ii - 0.5) * h[0]).transpose(2, 1, 0).ravel()
+    yg = (c.y0 + (jj - 0.5) * h[1]).transpose(2, 1, 0).ravel()
+    zg = (c.z0 + (kk - 0.5) * h[2]).transpose(2, 1, 0).ravel()
+    f = 1.0 + 2.0 * xg - 3.0 * yg + 0.5 * zg
+    inner = [(0.41, 0.26, 0.13), (0.2, 0.1, 0.2), (0.95, 0.45, 0.2)]
+    vals = inf.interpolate_points(c, inf.locate_points(c, inner), [f])
+    exact = [1.0 + 2.0 * x - 3.0 * y + 0.5 * z for x, y, z in inner]
+    np.testing.assert_allclose(vals[:, 0], exact, rtol=1e-12)
+    # a point in a corner of the domain: its lower corners are edge / corner ghosts
+    setup = inf.locate_points(c, [(0.0, 0.0, 0.0)])
+    assert sum(setup[0][2]) == 4
+    # the same numbers as the line sampler at the same points
+    plot = {"NumberOfPoints": 2, "x0": list(inner[0]), "x1": list(inner[2])}
+    Vg = np.stack([f, 2 * f, f, f, 3 * f])
+    rows = inf.sample_line(c, plot, Vg, np.zeros(f.size, np.int32), f)
+    pv = inf.interpolate_points(c, inf.locate_points(c, [inner[0], inner[2]]), [Vg[0], Vg[1], Vg[4], f])
+    np.testing.assert_array_equal(rows[:, [1, 2, 5, 8]], pv)
+
+
+def _run_oracle_with_probes(tmp_path):
+    from oracle import binding as ob
+    cs = inf.Case.from_text(CASE)
+    o = ob.OracleSim(cs.cfg)
+    o.upload(cs.V, cs.ID, cs.phi)
+    pr = inf.ProbeOutput(cs, prefix=str(tmp_path) + "/")
+    assert pr.write(0.0, 0.0, 0, *o.download_ghosted(), force=True)
+    history = []
+    for _ in range(cs.max_its):
+        o.run(1)
+        cnt = o.counters()
+        history.append(pr.write(cnt["time"], cnt["dt"], cnt["steps"], *o.download_ghosted()))
+    cnt = o.counters()
+    assert not pr.write(cnt["time"], cnt["dt"], cnt["steps"], *o.download_ghosted(), force=True)   # step 6 written
+    pr.close()
+    return cs, o, history
+
+
+def test_probe_files_follow_the_reference_layout(tmp_path):
+    cs, o, history = _run_oracle_with_probes(tmp_path)
+    assert history == [False, True, False, True, False, True]
+    rho = (tmp_path / "rho.txt").read_text().splitlines()
+    p = (tmp_path / "p.txt").read_text().splitlines()
+    assert len(rho) == 4 and len(p) == 4
+    assert (tmp_path / "phi1.txt").read_text() == ""   # one level set: LevelSet1 stays empty
+    # "%10d    %16.8e    " + nodes x "%16.8e    " for density, "%8d" for the others
+    assert rho[1][:10] == "%10d" % 2 and p[1][:8] == "%8d" % 2
+    assert len(rho[1]) == 10 + 4 + (16 + 4) * 4 and len(p[1]) == 8 + 4 + (16 + 4) * 4
+    last = [float(v) for v in rho[-1].split()]
+    assert last[0] == 6 and last[1] == pytest.approx(o.counters()["time"], rel=1e-8)
+    # node 0 sits in the gas bubble, node 1 in water
+    Vg, IDg, pg = o.download_ghosted()
+    vals = inf.interpolate_points(cs.cfg, inf.locate_points(cs.cfg, NODES), [Vg[0], IDg.astype(float), pg])
+    np.testing.assert_allclose(last[2:], vals[:, 0], rtol=1e-8)
+    ids = [float(v) for v in (tmp_path / "id.txt").read_text().splitlines()[-1].split()[2:]]
+    np.testing.assert_allclose(ids, vals[:, 1], rtol=1e-8)
+    assert vals[0, 2] < 0 < vals[1, 2]
+
+
+@pytest.mark.gpu
+def test_gpu_sampler_matches_the_host_sampler(tmp_path):
+    from m2c_gb300.solver import FluidState, Solver
+    cs = inf.Case.from_text(CASE)
+    s = Solver(cs.cfg, FluidState(cs.V, cs.ID, cs.phi))
+    s.run(3)
+    Vg, IDg, pg = s.get_state_ghosted()
+    rng = np.random.default_rng(7)
+    c = cs.cfg
+    lo = np.array([c.x0, c.y0, c.z0]) - 0.5 * np.array([1 / 16, 0.5 / 8, 0.25 / 4])
+    hi = np.array([c.xmax, c.ymax, c.zmax]) + 0.49 * np.array([1 / 16, 0.5 / 8, 0.25 / 4])
+    pts = [tuple(lo + (hi - lo) * rng.random(3)) for _ in range(200)] + NODES
+    host = inf.interpolate_points(c, inf.locate_points(c, pts), [Vg[q] for q in range(5)] +
+                                  [IDg.astype(np.float64), pg])
+    dev = s.sample_points(pts)
+    np.testing.assert_array_equal(dev, host)
+    with pytest.raises(RuntimeError):
+        s.sample_points([(2.0, 0.1, 0.1)])
+    # the probe writer on the device path writes the same lines as on the host path
+    (tmp_path / "d").mkdir()
+    (tmp_path / "h").mkdir()
+    a = inf.ProbeOutput(cs, prefix=str(tmp_path / "d") + "/")
+    b = inf.ProbeOutput(cs, prefix=str(tmp_path / "h") + "/")
+    assert a.write(1.0, 0.1, 2, solver=s) and b.write(1.0, 0.1, 2, Vg, IDg, pg)
+    a.close()
+    b.close()
+    for name in ("rho.txt", "p.txt", "vx.txt", "id.txt", "phi.txt"):
+        assert (tmp_path / "d" / name).read_text() == (tmp_path / "h" / name).read_text()
