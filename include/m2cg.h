@@ -206,6 +206,14 @@ m2cg_status m2cg_download_ghosted(m2cg_ctx* ctx, double* V, int32_t* id, double*
  * vz, p, material ID (interpolated), phi.  A point outside the ghosted grid, or one whose
  * eight corners are all edge / corner ghosts, is M2CG_ERR_INVALID_ARG. */
 m2cg_status m2cg_sample_points(m2cg_ctx* ctx, int32_t n, const double* xyz, double* out);
+/* Per-material integrals over the real cells whose centres lie in box = {xmin, xmax,
+ * ymin, ymax, zmin, zmax} (NULL: everywhere), as EnergyIntegrationOutput computes them
+ * on a Cartesian mesh (EnergyIntegrationOutput.cpp:247-610): out[n_materials *
+ * M2CG_N_INTEGRALS], per material: volume, mass, total energy rho (|u|^2/2 + e), total
+ * enthalpy rho (|u|^2/2 + e) + p, kinetic energy, internal energy rho e (each times the
+ * cell volume, summed). */
+#define M2CG_N_INTEGRALS 6
+m2cg_status m2cg_integrate(m2cg_ctx* ctx, const double* box, double* out);
 
 /* SpaceOperator::ComputeResidual on the current state with the stored
  * Riemann solutions refreshed (SpaceOperator.cpp:2573-2641, first RK stage).

@@ -24,6 +24,8 @@ cudaError_t reinit_build_graph(cudaStream_t, const ReinitArgs&, int, int, cudaGr
 cudaError_t unres_build_graph(cudaStream_t, const UnresArgs&, int, cudaGraphExec_t*);
 void launch_sample_points(cudaStream_t, const Params&, const StateSet&, const int32_t*, const ProbePoint*, int,
                           double*);
+int launch_integrate(cudaStream_t, const Params&, const StateSet&, const int32_t*, const Box3&, const double*, int,
+                     double*);
 void launch_dt(cudaStream_t, const Params&, const StateSet&, const int32_t*, DevScalars*, int, double);
 void launch_compact(cudaStream_t, const Params&, const int32_t*, const IfaceList&, unsigned long long*,
                     const DevScalars*);
@@ -843,6 +845,35 @@ m2cg_status m2cg_sample_points(m2cg_ctx* x, int32_t n, const double* xyz, double
   CK(cudaFreeAsync(dout, s));
   CK(cudaStreamSynchronize(s));
   CK(cudaGetLastError());
+  return M2CG_OK;
+}
+
+// EnergyIntegrationOutput's per-material integrals over a box (Cartesian mesh).
+m2cg_status m2cg_integrate(m2cg_ctx* x, const double* box, double* out) {
+  if (!x || !out) { set_err("null argument"); return M2CG_ERR_INVALID_ARG; }
+  Box3 b;
+  for (int d = 0; d < 3; d++) {
+    b.lo[d] = box ? box[2 * d] : -DBL_MAX;
+    b.hi[d] = box ? box[2 * d + 1] : DBL_MAX;
+  }
+  const double lo[3] = {x->cfg.x0, x->cfg.y0, x->cfg.z0};
+  const int Q = M2CG_MAX_MATERIALS * M2CG_N_INTEGRALS;
+  const int blocks = launch_integrate(x->stream, x->P, x->S[0], x->id, b, lo, x->nsm, nullptr);
+  double* d = nullptr;
+  CK(cudaMallocAsync(&d, (size_t)blocks * Q * sizeof(double), x->stream));
+  launch_integrate(x->stream, x->P, x->S[0], x->id, b, lo, x->nsm, d);
+  x->launches += 1;
+  std::vector<double> h((size_t)blocks * Q);
+  CK(cudaMemcpyAsync(h.data(), d, h.size() * sizeof(double), cudaMemcpyDeviceToHost, x->stream));
+  CK(cudaFreeAsync(d, x->stream));
+  CK(cudaStreamSynchronize(x->stream));
+  CK(cudaGetLastError());
+  for (int m = 0; m < x->P.n_mat; m++)
+    for (int q = 0; q < M2CG_N_INTEGRALS; q++) {
+      double v = 0.0;
+      for (int blk = 0; blk < blocks; blk++) v += h[(size_t)blk * Q + m * M2CG_N_INTEGRALS + q];
+      out[m * M2CG_N_INTEGRALS + q] = v;
+    }
   return M2CG_OK;
 }
 

@@ -189,6 +189,10 @@ struct ProbePoint {
   double w[3];
 };
 
+struct Box3 {
+  double lo[3], hi[3];
+};
+
 struct StageArgs {
   // residual input (neighbors) and own-cell inputs of the stage combination
   StateSet in;          // V and phi of the stage input (residual evaluated here)

@@ -21,6 +21,9 @@ plots that go with them.
 * `ProbeOutput`: time histories at the probe nodes of `Output.Probes`
   (ProbeOutput.cpp:14-350, 599-848; IoData.cpp:3152-3230), written when
   Utils.cpp:337-357 says so, one file per requested field.
+* `EnergyIntegrationOutput`: per-material volume, mass and energies in a box
+  (`Output.EnergyIntegration`; EnergyIntegrationOutput.cpp:13-245,
+  IoData.cpp:3237-3281), from `Solver.integrate` on the device.
 
 Anything the path does not implement (other EOS, non-uniform meshes, other
 geometric entities, narrow bands, other reinitialization treatments) raises
@@ -273,6 +276,7 @@ class Case:
         self.V = self.ID = self.phi = None
         self.line_plots = []
         self.probes = None
+        self.energy_integration = None
         self.prefix = ""
         self.max_time = 1e10
         self.max_its = 2 ** 31 - 1
@@ -436,6 +440,8 @@ class Case:
         self.prefix = str(out.get("Prefix", ""))
         if "Probes" in out:
             self.probes = _probes(out["Probes"])
+        if "EnergyIntegration" in out:
+            self.energy_integration = _energy_integration(out["EnergyIntegration"])
         return self
 
     # -- initial state -------------------------------------------------------
@@ -535,6 +541,23 @@ def _probes(pr):
     files = {k: str(pr[k]) for k in _PROBE_FIELDS if pr.get(k)}
     return {"frequency": int(pr.get("Frequency", -100)), "frequency_dt": float(pr.get("TimeInterval", -1.0)),
             "files": files, "nodes": locs}
+
+
+# EnergyIntegrationData::setup (IoData.cpp:3256-3281): file per quantity and
+# its column in the integrals
+_INTEGRALS = {"Volume": 0, "Mass": 1, "TotalEnergy": 2, "TotalEnthalpy": 3, "KineticEnergy": 4,
+              "InternalEnergy": 5}
+
+
+def _energy_integration(ei):
+    for k in ("PotentialEnergy", "LaserRadiation"):
+        if ei.get(k):
+            raise NotImplementedError(f"Output.EnergyIntegration.{k}")
+    big = 1.7976931348623157e308
+    box = [float(ei.get(k, v)) for k, v in (("Xmin", -big), ("Xmax", big), ("Ymin", -big), ("Ymax", big),
+                                            ("Zmin", -big), ("Zmax", big))]
+    return {"frequency": int(ei.get("Frequency", -100)), "frequency_dt": float(ei.get("TimeInterval", -1.0)),
+            "files": {k: str(ei[k]) for k in _INTEGRALS if ei.get(k)}, "box": box}
 
 
 def _ghost_coords(n, lo, hi):
@@ -675,6 +698,42 @@ class ProbeOutput:
                 f.write("%16.8e    " % v)
             f.write("\n")
             f.flush()
+        self.last = time
+        return True
+
+    def close(self):
+        for f in self.files.values():
+            f.close()
+
+
+class EnergyIntegrationOutput:
+    """Per-material integrals in the box of `Output.EnergyIntegration`
+    (EnergyIntegrationOutput.cpp:126-245): one file per quantity, one line per
+    output: the step, the time, the value of every material and their sum.
+    `write` takes any object with `integrate(box)` (Solver: on the device;
+    OracleSim: the CPU restatement)."""
+
+    def __init__(self, case, prefix=None):
+        e = case.energy_integration or {"frequency": -100, "frequency_dt": -1.0, "files": {}, "box": None}
+        self.frequency, self.frequency_dt, self.box = e["frequency"], e["frequency_dt"], e["box"]
+        self.last = -1.0
+        pre = case.prefix if prefix is None else prefix
+        self.files = {k: open(pre + name, "w") for k, name in e["files"].items()}
+
+    def write(self, time, dt, step, sim, force=False):
+        if not is_time_to_write(time, dt, step, self.frequency_dt, self.frequency, self.last, force):
+            return False
+        if self.files:
+            vals = sim.integrate(self.box)
+            for key, f in self.files.items():
+                col = _INTEGRALS[key]
+                f.write("%10d    %16.8e    " % (step, time))
+                total = 0.0
+                for v in vals[:, col]:
+                    f.write("%16.8e  " % v)
+                    total += v
+                f.write("%16.8e\n" % total)
+                f.flush()
         self.last = time
         return True
 

@@ -87,6 +87,16 @@ class Solver:
                   "m2cg_sample_points")
         return out
 
+    def integrate(self, box=None):
+        """EnergyIntegrationOutput's per-material integrals on the device: rows
+        per material of (volume, mass, total energy, total enthalpy, kinetic,
+        internal) over the cells whose centres lie in box = (xmin, xmax, ymin,
+        ymax, zmin, zmax), or everywhere."""
+        out = np.zeros((self.cfg.n_materials, 6))
+        b = None if box is None else np.ascontiguousarray(box, np.float64)
+        abi.check(self.lib, self.lib.m2cg_integrate(self.ctx, abi.dptr(b), abi.dptr(out)), "m2cg_integrate")
+        return out
+
     def run_to_end(self, max_time, max_its, chunk=64):
         """The Main.cpp:653-771 loop to MaxTime or MaxIts, whichever comes
         first, in chunks of graph-replayed steps; returns the counters."""

@@ -32,6 +32,7 @@ def _load_oracle():
         "orc_run": (C.c_int, [_P, C.c_int]),
         "orc_counters": (None, [_P, C.POINTER(Counters)]),
         "orc_conserved_totals": (None, [_P, _D]),
+        "orc_integrate": (None, [_P, _D, _D]),
         "orc_riemann_batch": (None, [C.POINTER(Config), C.c_int64, _D, _I, _D, _I, _D, _D, _I, _D, _D, _I, _I, _D]),
         "orc_flux_batch": (None, [C.POINTER(Config), C.c_int64, _I, _D, _D, _I, _D]),
     }
@@ -101,6 +102,15 @@ class OracleSim:
         R = np.zeros(self.n)
         lib().orc_levelset_residual(self.h, dptr(R))
         return R
+
+    def integrate(self, box=None):
+        """Per-material (volume, mass, total energy, total enthalpy, kinetic,
+        internal) over the cells whose centres lie in box (xmin, xmax, ymin,
+        ymax, zmin, zmax)."""
+        out = np.zeros((self.cfg.n_materials, 6))
+        b = None if box is None else np.ascontiguousarray(box, np.float64)
+        lib().orc_integrate(self.h, dptr(b), dptr(out))
+        return out
 
     def download_ghosted(self):
         """(V planes 5 x N, ID, phi) with the ghost layer, N = (nx+2)(ny+2)(nz+2), i fastest."""

@@ -1441,6 +1441,40 @@ void orc_conserved_totals(void* h, double* tot) {
       }
 }
 
+// EnergyIntegrationOutput::IntegrateVolume / Mass / TotalEnergy / TotalEnthalpy /
+// KineticEnergy / InternalEnergy (EnergyIntegrationOutput.cpp:247-610, Cartesian
+// mesh): per material, over the cells whose centres lie in the box, in (k, j, i)
+// order.  out[n_materials * 6].
+void orc_integrate(void* h, const double* box, double* out) {
+  Oracle* o = (Oracle*)h;
+  const int nm = o->cfg.n_materials;
+  for (int q = 0; q < nm * 6; q++) out[q] = 0.0;
+  const double lo[3] = {o->cfg.x0, o->cfg.y0, o->cfg.z0}, hh[3] = {o->dx, o->dy, o->dz};
+  for (int k = 0; k < o->NZ; k++)
+    for (int j = 0; j < o->NY; j++)
+      for (int i = 0; i < o->NX; i++) {
+        const int q3[3] = {i, j, k};
+        bool in = true;
+        for (int d = 0; d < 3; d++) {
+          const double x = lo[d] + 0.5 * hh[d] + q3[d] * hh[d];   // MeshGenerator.cpp:166-171
+          if (box && !(x >= box[2 * d] && x <= box[2 * d + 1])) in = false;
+        }
+        if (!in) continue;
+        const size_t c = o->idx(i, j, k);
+        const int m = o->ID[c];
+        const double* v = &o->V[c * 5];
+        const double vsq = v[1] * v[1] + v[2] * v[2] + v[3] * v[3];
+        const double e = o->vf[m].GetInternalEnergyPerUnitMass(v[0], v[4]);
+        double* a = out + m * 6;
+        a[0] += o->vol;
+        a[1] += v[0] * o->vol;
+        a[2] += v[0] * (0.5 * vsq + e) * o->vol;
+        a[3] += (v[0] * (0.5 * vsq + e) + v[4]) * o->vol;
+        a[4] += 0.5 * v[0] * vsq * o->vol;
+        a[5] += v[0] * e * o->vol;
+      }
+}
+
 // Batched exact Riemann solves (ExactRiemannSolverBase.cpp:59-347).
 void orc_riemann_batch(const m2cg_config* cfg, int64_t n, const double* Vm, const int32_t* idm, const double* Vp,
                        const int32_t* idp, const double* dir, double* Vs, int32_t* id, double* Vsm, double* Vsp,

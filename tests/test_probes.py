@@ -156,3 +156,91 @@ def test_gpu_sampler_matches_the_host_sampler(tmp_path):
     b.close()
     for name in ("rho.txt", "p.txt", "vx.txt", "id.txt", "phi.txt"):
         assert (tmp_path / "d" / name).read_text() == (tmp_path / "h" / name).read_text()
+
+
+# ---------------------------------------------------------------------------
+# Per-material integrals (EnergyIntegrationOutput.cpp:126-610)
+
+EI = """under Output { Prefix = "out_";
+  under EnergyIntegration { Frequency = 3; Volume = "vol.txt"; Mass = "mass.txt"; TotalEnergy = "E.txt";
+                            TotalEnthalpy = "H.txt"; KineticEnergy = "K.txt"; InternalEnergy = "IE.txt";
+                            Xmin = 0.1; Xmax = 0.7; Zmax = 0.2; } }
+"""
+
+
+def _ei_case():
+    return inf.Case.from_text(CASE.split("under Output")[0] + EI)
+
+
+def _sg_integrals(cfg, V, ID, box):
+    """The integrals restated in numpy for stiffened gases: e = (p + gamma pc) / ((gamma - 1) rho)."""
+    from m2c_gb300.problems import cell_centers
+    X, Y, Z = cell_centers(cfg)
+    vol = (cfg.xmax - cfg.x0) / cfg.nx * (cfg.ymax - cfg.y0) / cfg.ny * (cfg.zmax - cfg.z0) / cfg.nz
+    inb = (X >= box[0]) & (X <= box[1]) & (Y >= box[2]) & (Y <= box[3]) & (Z >= box[4]) & (Z <= box[5])
+    g = np.array([cfg.mat[m].gamma for m in range(cfg.n_materials)])[ID]
+    pc = np.array([cfg.mat[m].pc for m in range(cfg.n_materials)])[ID]
+    rho, p = V[:, 0], V[:, 4]
+    e = (p + g * pc) / ((g - 1.0) * rho)
+    vsq = (V[:, 1:4] ** 2).sum(1)
+    q = np.stack([np.ones_like(rho), rho, rho * (0.5 * vsq + e), rho * (0.5 * vsq + e) + p, 0.5 * rho * vsq,
+                  rho * e], 1) * vol
+    return np.stack([q[inb & (ID == m)].sum(0) for m in range(cfg.n_materials)])
+
+
+def test_energy_integration_is_parsed_and_refuses_potential_energy():
+    cs = _ei_case()
+    ei = cs.energy_integration
+    assert ei["frequency"] == 3 and ei["box"][:5] == [0.1, 0.7, -1.7976931348623157e308, 1.7976931348623157e308,
+                                                      -1.7976931348623157e308] and ei["box"][5] == 0.2
+    assert set(ei["files"]) == {"Volume", "Mass", "TotalEnergy", "TotalEnthalpy", "KineticEnergy", "InternalEnergy"}
+    with pytest.raises(NotImplementedError):
+        inf.Case.from_text(CASE.split("under Output")[0] + EI.replace("Frequency = 3;",
+                                                                       "Frequency = 3; PotentialEnergy = \"u.txt\";"))
+
+
+def test_oracle_integrals_and_file_layout(tmp_path):
+    from oracle import binding as ob
+    cs = _ei_case()
+    o = ob.OracleSim(cs.cfg)
+    o.upload(cs.V, cs.ID, cs.phi)
+    box = cs.energy_integration["box"]
+    np.testing.assert_allclose(o.integrate(box), _sg_integrals(cs.cfg, cs.V, cs.ID, box), rtol=1e-12)
+    full = o.integrate()
+    assert full[:, 0].sum() == pytest.approx(1.0 * 0.5 * 0.25, rel=1e-12)
+    # cell centres (i + 1/2) / 16 in [0.1, 0.7]: i = 2..10; (k + 1/2) / 16 <= 0.2: k = 0..2
+    assert o.integrate(box)[:, 0].sum() == pytest.approx(0.125 * 9 / 16 * 3 / 4, rel=1e-12)
+    w = inf.EnergyIntegrationOutput(cs, prefix=str(tmp_path) + "/")
+    wrote = []
+    for _ in range(6):
+        o.run(1)
+        c = o.counters()
+        wrote.append(w.write(c["time"], c["dt"], c["steps"], o))
+    w.close()
+    assert wrote == [False, False, True, False, False, True]
+    lines = (tmp_path / "mass.txt").read_text().splitlines()
+    assert len(lines) == 2
+    # "%10d    %16.8e    " + materials x "%16.8e  " + "%16.8e\n" (the sum)
+    assert len(lines[1]) == 10 + 4 + 16 + 4 + (16 + 2) * 2 + 16
+    vals = [float(v) for v in lines[1].split()]
+    assert vals[0] == 6
+    ref = o.integrate(box)
+    np.testing.assert_allclose(vals[2:4], ref[:, 1], rtol=1e-8)
+    assert vals[4] == pytest.approx(ref[:, 1].sum(), rel=1e-8)
+
+
+@pytest.mark.gpu
+def test_gpu_integrals_match_oracle():
+    from m2c_gb300.solver import FluidState, Solver
+    from oracle import binding as ob
+    cs = _ei_case()
+    s = Solver(cs.cfg, FluidState(cs.V, cs.ID, cs.phi))
+    o = ob.OracleSim(cs.cfg)
+    o.upload(cs.V, cs.ID, cs.phi)
+    box = cs.energy_integration["box"]
+    for b in (box, None):
+        np.testing.assert_allclose(s.integrate(b), o.integrate(b), rtol=1e-12)   # same state: summation order only
+    np.testing.assert_array_equal(s.integrate(box), s.integrate(box))   # fixed reduction order
+    s.run(3)
+    o.run(3)
+    np.testing.assert_allclose(s.integrate(box), o.integrate(box), rtol=1e-9)
