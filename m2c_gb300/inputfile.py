@@ -277,6 +277,7 @@ class Case:
         self.line_plots = []
         self.probes = None
         self.energy_integration = None
+        self.solution = {"base": "solution", "frequency": 0, "frequency_dt": -1.0}
         self.prefix = ""
         self.max_time = 1e10
         self.max_its = 2 ** 31 - 1
@@ -434,10 +435,15 @@ class Case:
         for k, d in sorted(out.get("LinePlot", {}).items()):
             self.line_plots.append({"index": k, "FileName": d.get("FileName", ""),
                                     "NumberOfPoints": int(d.get("NumberOfPoints", 0)),
+                                    "frequency": int(d.get("Frequency", -100)),
+                                    "frequency_dt": float(d.get("TimeInterval", -1.0)),
                                     "x0": [float(d.get("X0", 0.0)), float(d.get("Y0", 0.0)), float(d.get("Z0", 0.0))],
                                     "x1": [float(d.get("Xmax", 0.0)), float(d.get("Ymax", 0.0)),
                                            float(d.get("Zmax", 0.0))]})
         self.prefix = str(out.get("Prefix", ""))
+        # solution snapshots (OutputData, IoData.cpp:2970-2974, 3027-3031)
+        self.solution = {"base": str(out.get("Solution", "solution")), "frequency": int(out.get("Frequency", 0)),
+                         "frequency_dt": float(out.get("TimeInterval", -1.0))}
         if "Probes" in out:
             self.probes = _probes(out["Probes"])
         if "EnergyIntegration" in out:

@@ -244,3 +244,80 @@ def test_gpu_integrals_match_oracle():
     s.run(3)
     o.run(3)
     np.testing.assert_allclose(s.integrate(box), o.integrate(box), rtol=1e-9)
+
+
+# ---------------------------------------------------------------------------
+# The main loop with its outputs (Main.cpp:571-782)
+
+RUN = """under Output { Prefix = "PREFIX"; Frequency = 3;
+  under LinePlot[0] { FileName = "line"; NumberOfPoints = 9; Frequency = 2; X0 = 0.03; Xmax = 0.97;
+                      Y0 = 0.25; Ymax = 0.25; Z0 = 0.1; Zmax = 0.1; }
+  under Probes { Frequency = 2; Pressure = "p.txt"; under Node[0] { X = 0.41; Y = 0.26; Z = 0.13; } }
+  under EnergyIntegration { Frequency = 3; Mass = "mass.txt"; } }
+"""
+
+
+class _OracleRun:
+    """The oracle behind the Solver's stepping and output methods."""
+
+    def __init__(self, cs):
+        from oracle import binding as ob
+        self.o = ob.OracleSim(cs.cfg)
+        self.o.upload(cs.V, cs.ID, cs.phi)
+
+    def run(self, n):
+        self.o.run(n)
+        return self.o.counters()
+
+    def counters(self):
+        return self.o.counters()
+
+    def get_state(self):
+        from m2c_gb300.solver import FluidState
+        return FluidState(*self.o.download())
+
+    def get_state_ghosted(self):
+        return self.o.download_ghosted()
+
+    def integrate(self, box=None):
+        return self.o.integrate(box)
+
+
+def _run_case(sim_factory, tmp_path):
+    from m2c_gb300 import driver
+    cs = inf.Case.from_text(CASE.split("under Output")[0] + RUN.replace("PREFIX", str(tmp_path) + "/r_"))
+    sim = sim_factory(cs)
+    return driver.run_case(cs, sim), sim
+
+
+def test_run_case_writes_every_output_on_its_schedule(tmp_path):
+    (c, written), sim = _run_case(_OracleRun, tmp_path)
+    assert c["steps"] == 6
+    # snapshots: 0 (initial), 3, 6; lines and probes: 0, 2, 4, 6; energy: 0, 3, 6
+    assert written == {"snapshots": 3, "lines": 4, "probes": 4, "energy": 3}
+    names = sorted(p.name for p in tmp_path.iterdir())
+    assert names == ["r_line_0000.txt", "r_line_0001.txt", "r_line_0002.txt", "r_line_0003.txt", "r_mass.txt",
+                     "r_p.txt", "r_solution.pvd", "r_solution_0000.vtr", "r_solution_0001.vtr",
+                     "r_solution_0002.vtr"]
+    head = (tmp_path / "r_line_0003.txt").read_text().splitlines()
+    assert head[2].startswith("## Time: ") and head[2].endswith("Time step: 6.")
+    assert [int(l.split()[0]) for l in (tmp_path / "r_p.txt").read_text().splitlines()] == [0, 2, 4, 6]
+    assert [int(l.split()[0]) for l in (tmp_path / "r_mass.txt").read_text().splitlines()] == [0, 3, 6]
+    from m2c_gb300 import output
+    snap = output.read_vtr(str(tmp_path / "r_solution_0002.vtr"))   # the final state
+    np.testing.assert_array_equal(snap["density"], sim.get_state().V[:, 0])
+    assert "<DataSet timestep" in (tmp_path / "r_solution.pvd").read_text()
+
+
+@pytest.mark.gpu
+def test_gpu_run_case_matches_oracle_outputs(tmp_path):
+    from m2c_gb300.solver import FluidState, Solver
+    (tmp_path / "o").mkdir()
+    (tmp_path / "g").mkdir()
+    (co, wo), _ = _run_case(_OracleRun, tmp_path / "o")
+    (cg, wg), _ = _run_case(lambda cs: Solver(cs.cfg, FluidState(cs.V, cs.ID, cs.phi)), tmp_path / "g")
+    assert wo == wg and co["steps"] == cg["steps"] == 6
+    for name in ("r_line_0003.txt", "r_p.txt", "r_mass.txt"):
+        a = np.loadtxt(tmp_path / "o" / name)
+        b = np.loadtxt(tmp_path / "g" / name)
+        np.testing.assert_allclose(b, a, rtol=1e-7, atol=1e-9 * np.abs(a).max())
