@@ -1,0 +1,72 @@
+"""The C++ adapter (include/m2cg.hpp): a reference-shaped driver in C++
+(tests/cpp/adapter_check.cpp) compiled with g++ against libm2cg.so.  On the
+CPU it must compile, link and surface the library's error as m2cg::Error; on
+the GPU its results must equal the Python binding's for the same inputs."""
+import os
+import shutil
+import subprocess
+
+import numpy as np
+import pytest
+
+from m2c_gb300 import abi, problems
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+LIBDIR = os.path.join(ROOT, "m2c_gb300", "lib")
+
+
+def _compile(tmp_path):
+    gxx = shutil.which("g++")
+    if gxx is None or not os.path.exists(os.path.join(LIBDIR, "libm2cg.so")):
+        pytest.skip("g++ or libm2cg.so missing")
+    exe = str(tmp_path / "adapter_check")
+    cmd = [gxx, "-std=c++17", "-O1", "-Wall", "-Wextra", "-Werror", "-I", os.path.join(ROOT, "include"),
+           os.path.join(ROOT, "tests", "cpp", "adapter_check.cpp"), "-L", LIBDIR, "-lm2cg",
+           "-Wl,-rpath," + LIBDIR, "-o", exe]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def _inputs(tmp_path):
+    c, V, ID, phi = problems.shock_bubble(n=16)
+    d = tmp_path / "in_"
+    (tmp_path / "in_cfg.bin").write_bytes(bytes(memoryview(c)))
+    np.ascontiguousarray(V).tofile(str(d) + "V.bin")
+    np.ascontiguousarray(ID, np.int32).tofile(str(d) + "ID.bin")
+    np.ascontiguousarray(phi).tofile(str(d) + "phi.bin")
+    return c, V, ID, phi, str(d)
+
+
+def test_adapter_compiles_links_and_reports_library_errors(tmp_path):
+    exe = _compile(tmp_path)
+    c, V, ID, phi, pre = _inputs(tmp_path)
+    r = subprocess.run([exe, pre, "2", str(tmp_path / "out_")], capture_output=True, text=True, timeout=600)
+    if r.returncode == 3:   # no GPU here: the library's status and message come through m2cg::Error
+        assert r.stdout.startswith("error %d " % 5) and "m2cg_create" in r.stdout, r.stdout
+    else:
+        assert r.returncode == 0, r.stdout + r.stderr
+
+
+@pytest.mark.gpu
+def test_gpu_adapter_matches_python_binding(tmp_path):
+    from m2c_gb300.solver import FluidState, Solver
+    exe = _compile(tmp_path)
+    c, V, ID, phi, pre = _inputs(tmp_path)
+    r = subprocess.run([exe, pre, "3", str(tmp_path / "out_")], capture_output=True, text=True, timeout=600)
+    assert r.returncode == 0, r.stdout + r.stderr
+    o = str(tmp_path / "out_")
+    s = Solver(c, FluidState(V, ID, phi))
+    dt, cfl = s.ComputeTimeStepSize()
+    np.testing.assert_array_equal(np.fromfile(o + "dt.bin"), [dt, cfl])
+    np.testing.assert_array_equal(np.fromfile(o + "R.bin").reshape(-1, 5), s.ComputeResidual())
+    cnt = s.run(3)
+    g = s.get_state()
+    np.testing.assert_array_equal(np.fromfile(o + "V.bin").reshape(-1, 5), g.V)
+    np.testing.assert_array_equal(np.fromfile(o + "ID.bin", np.int32), g.ID)
+    np.testing.assert_array_equal(np.fromfile(o + "phi.bin"), g.Phi)
+    cc = abi.Counters.from_buffer_copy(open(o + "counters.bin", "rb").read())
+    assert cc.steps == cnt["steps"] == 3 and cc.time == cnt["time"]
+    rs = np.fromfile(o + "riemann.bin")
+    assert rs[15] in (10.0, 0.0, 11.0) and np.all(np.isfinite(rs[:15]))   # err 0, id 0 or 1
+    assert np.all(np.isfinite(np.fromfile(o + "flux.bin")))
