@@ -64,6 +64,7 @@ enum { M2CG_MPFLUX_EXACT = 0, M2CG_MPFLUX_NUMERICAL = 1, M2CG_MPFLUX_LLF = 2 };
 enum { M2CG_MPREC_CONSTANT = 0, M2CG_MPREC_LINEAR = 1 };
 enum { M2CG_PHASECHANGE_RIEMANN = 0, M2CG_PHASECHANGE_EXTRAPOLATION = 1 };
 enum { M2CG_PCDIR_ALL = 0, M2CG_PCDIR_UPWIND = 1 };
+enum { M2CG_RNORMAL_LEVEL_SET = 0, M2CG_RNORMAL_MESH = 1, M2CG_RNORMAL_AVERAGE = 2 };
 /* Time integrator (ExplicitData::Type, IoData.h:931). */
 enum { M2CG_TS_FORWARD_EULER = 0, M2CG_TS_RK2 = 1, M2CG_TS_RK3 = 2 };
 
@@ -140,6 +141,9 @@ typedef struct {
   double ls_minmod_coeff;      /* Reconstruction.GeneralizedMinModCoefficient (1.2) */
   double reinit_frequency_dt;  /* Reinitialization.FrequencyDt: after every step that crosses a multiple of
                                   this time (> 0 takes precedence over Frequency, Utils.cpp:344-349) */
+  int32_t mp_riemann_normal;   /* MultiPhase.RiemannNormal (default Mesh): axis of the interface Riemann
+                                  problems (SpaceOperator.cpp:2186-2415) */
+  int32_t pad5_;
 } m2cg_config;
 
 /* Per-step counters (the reference prints these as warnings; SpaceOperator.cpp:681-683,

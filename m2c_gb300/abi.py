@@ -27,6 +27,7 @@ MPFLUX_EXACT, MPFLUX_NUMERICAL, MPFLUX_LLF = 0, 1, 2
 MPREC_CONSTANT, MPREC_LINEAR = 0, 1
 PHASECHANGE_RIEMANN, PHASECHANGE_EXTRAPOLATION = 0, 1
 PCDIR_ALL, PCDIR_UPWIND = 0, 1
+RNORMAL_LEVEL_SET, RNORMAL_MESH, RNORMAL_AVERAGE = 0, 1, 2
 TS_FORWARD_EULER, TS_RK2, TS_RK3 = 0, 1, 2
 LS_FINITE_VOLUME, LS_FINITE_DIFFERENCE = 0, 1
 LSFLUX_ROE, LSFLUX_LLF, LSFLUX_UPWIND = 0, 1, 2
@@ -69,7 +70,7 @@ class Config(C.Structure):
                 ("pad4_", C.c_int32), ("reinit_cfl", C.c_double), ("reinit_tol", C.c_double),
                 ("ls_solver", C.c_int32), ("ls_flux", C.c_int32), ("ls_delta", C.c_double),
                 ("ls_rec_type", C.c_int32), ("ls_limiter", C.c_int32), ("ls_minmod_coeff", C.c_double),
-                ("reinit_frequency_dt", C.c_double)]
+                ("reinit_frequency_dt", C.c_double), ("mp_riemann_normal", C.c_int32), ("pad5_", C.c_int32)]
 
 
 class Counters(C.Structure):
@@ -132,6 +133,7 @@ def default_config():
     c.ls_solver, c.ls_flux, c.ls_delta = LS_FINITE_DIFFERENCE, LSFLUX_ROE, 0.2
     c.ls_rec_type, c.ls_limiter, c.ls_minmod_coeff = REC_LINEAR, LIM_GENERALIZED_MINMOD, 1.2
     c.reinit_frequency_dt = -1.0
+    c.mp_riemann_normal = RNORMAL_MESH
     return c
 
 

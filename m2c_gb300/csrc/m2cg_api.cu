@@ -217,6 +217,17 @@ m2cg_status m2cg_fill_params(const m2cg_config& c, m2cg::Params& P) {
   for (int s = 0; s < 6; s++) { P.bc[s] = c.bc[s]; P.ls_bc[s] = c.ls_bc[s]; }
   for (int p = 0; p < 5; p++) { P.inlet[p] = c.inlet[p]; P.inlet2[p] = c.inlet2[p]; }
   P.n_ls = c.n_levelsets; P.ls_matid = c.ls_matid;
+  P.lo[0] = c.x0; P.lo[1] = c.y0; P.lo[2] = c.z0;
+  P.riemann_normal = c.mp_riemann_normal;
+  P.phi_n = nullptr;   // the context's phi, set when its arrays exist
+  if (c.mp_riemann_normal < M2CG_RNORMAL_LEVEL_SET || c.mp_riemann_normal > M2CG_RNORMAL_AVERAGE) {
+    set_err("bad MultiPhase.RiemannNormal %d", c.mp_riemann_normal);
+    return M2CG_ERR_INVALID_ARG;
+  }
+  if (c.mp_riemann_normal != M2CG_RNORMAL_MESH && c.n_levelsets == 0) {
+    set_err("RiemannNormal = LevelSet / Average needs a level set");
+    return M2CG_ERR_INVALID_ARG;
+  }
   RiemannPrm& r = P.rp;
   r.maxIts_main = c.maxits_main; r.maxIts_bracket = c.maxits_bracket; r.maxIts_shock = c.maxits_shock;
   r.numSteps = c.numsteps_rarefaction; r.tol_main = c.tol_main; r.tol_shock = c.tol_shock; r.tol_rare = c.tol_rarefaction;
@@ -248,6 +259,9 @@ static m2cg_status ctx_alloc(m2cg_ctx* x) {
   for (int s = 0; s < 3; s++)
     for (int q = 0; q < 6; q++) CK(x->alloc(&x->S[s].q[q], N));
   for (int p = 0; p < 5; p++) { CK(x->alloc(&x->Un[p], N)); CK(x->alloc(&x->Us[p], N)); CK(x->alloc(&x->R[p], N)); }
+  // the stages write phi into S[0] only in the last update, after every
+  // interface solve of the step: S[0]'s phi is phi at the start of the step
+  if (x->P.n_ls > 0) x->P.phi_n = x->S[0].q[5];
   CK(x->alloc(&x->rphi, N));
   CK(x->alloc(&x->id, N));
   CK(x->alloc(&x->id_new, N));
@@ -488,6 +502,7 @@ m2cg_status m2cg_config_default(m2cg_config* c) {
   c->ls_limiter = M2CG_LIM_GENERALIZED_MINMOD;
   c->ls_minmod_coeff = 1.2;
   c->reinit_frequency_dt = -1.0;
+  c->mp_riemann_normal = M2CG_RNORMAL_MESH;
   return M2CG_OK;
 }
 
@@ -1445,6 +1460,10 @@ m2cg_status m2cg_ensemble_create(const m2cg_config* cfgs, int32_t n, m2cg_ensemb
     }
     if (cfgs[d].n_levelsets > 0 && cfgs[d].ls_solver == M2CG_LS_FINITE_VOLUME) {
       set_err("member %d: the batched step advects the level set by finite differences only", d);
+      return M2CG_ERR_INVALID_ARG;
+    }
+    if (cfgs[d].mp_riemann_normal != M2CG_RNORMAL_MESH) {
+      set_err("member %d: the batched step solves interface problems along the mesh axes only", d);
       return M2CG_ERR_INVALID_ARG;
     }
     if (cfgs[d].n_levelsets > 0 && (cfgs[d].reinit_frequency > 0 || cfgs[d].reinit_frequency_dt > 0)) {

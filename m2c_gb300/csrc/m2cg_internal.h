@@ -81,6 +81,9 @@ struct Params {
   int64_t* unres;
   unsigned long long* unres_count;
   int unres_cap;
+  int riemann_normal;   // M2CG_RNORMAL_*: axis of the interface Riemann problems
+  const double* phi_n;  // phi at the start of the step (the normals' input; NULL without a level set)
+  double lo[3];         // domain origin: cell centres at lo + 0.5 h + i h
   int ls_fv;            // finite-volume level set (else finite difference)
   int ls_flux, ls_rec_linear, ls_limiter;
   double ls_delta, ls_minmod;

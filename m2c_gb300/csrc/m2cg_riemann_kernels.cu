@@ -79,6 +79,68 @@ __device__ __forceinline__ void init_solver(ExactRiemannDev& rs, const Mats* md,
   rs.path3.cap = path_cap;
 }
 
+// SpaceOperator::GetNormalForBimaterialRiemann with RiemannNormal = LevelSet or
+// Average and one level set (SpaceOperator.cpp:2186-2415): the gradient of phi
+// at the face between the plus cell c and its minus neighbour along d -- one-
+// sided across the face, the tangential components by central differences in
+// both cells (one-sided next to the ghost layer) interpolated to the face --
+// normalized, reversed when the minus cell is material 0, its d component made
+// non-negative; Average adds the mesh normal and normalizes again.  The
+// reference asserts unless the two materials are 0 and the level set's; such
+// faces keep the mesh normal here.  dir holds the mesh normal on entry.
+__device__ __forceinline__ void riemann_normal_dir(const Params& P, int64_t c, int d, int idm, int idp, double* dir) {
+  const int my_ls = idp == 0 ? idm : idp, nb_ls = idm == 0 ? idp : idm;
+  if (my_ls != P.ls_matid || nb_ls != P.ls_matid || !P.phi_n) return;
+  const Grid& g = P.g;
+  const double* phi = P.phi_n;
+  int64_t r = c;
+  int pos[3];
+  pos[0] = (int)(r % g.px) - 1; r /= g.px;
+  pos[1] = (int)(r % g.py) - 1;
+  pos[2] = (int)(r / g.py) - 1;
+  const int64_t st[3] = {1, g.sy, g.sz};
+  const int nn[3] = {g.nx, g.ny, g.nz};
+  const double h[3] = {g.dx, g.dy, g.dz};
+  auto X = [&](int a, int q) { return P.lo[a] + 0.5 * h[a] + q * h[a]; };   // MeshGenerator.cpp:166-171
+  const int64_t m = c - st[d];
+  double gr[3];
+  gr[d] = (phi[c] - phi[m]) / (X(d, pos[d]) - X(d, pos[d] - 1));
+  const double xmh = X(d, pos[d]) - 0.5 * h[d];
+  const double dxd = X(d, pos[d]) - X(d, pos[d] - 1);
+  const double c1 = (X(d, pos[d]) - xmh) / dxd, c2 = (xmh - X(d, pos[d] - 1)) / dxd;
+  for (int a = 0; a < 3; a++) {
+    if (a == d) continue;
+    const int q = pos[a];
+    double g1, g2;
+    if (q < 0) {
+      g1 = (phi[m + st[a]] - phi[m]) / (X(a, q + 1) - X(a, q));
+      g2 = (phi[c + st[a]] - phi[c]) / (X(a, q + 1) - X(a, q));
+    } else if (q >= nn[a]) {
+      g1 = (phi[m] - phi[m - st[a]]) / (X(a, q) - X(a, q - 1));
+      g2 = (phi[c] - phi[c - st[a]]) / (X(a, q) - X(a, q - 1));
+    } else {   // SpaceOperator.h:223-228
+      const double x0 = X(a, q - 1), x1 = X(a, q), x2 = X(a, q + 1);
+      const double k0 = -(x2 - x1) / ((x1 - x0) * (x2 - x0));
+      const double k1 = 1.0 / (x1 - x0) - 1.0 / (x2 - x1);
+      const double k2 = (x1 - x0) / ((x2 - x0) * (x2 - x1));
+      g1 = k0 * phi[m - st[a]] + k1 * phi[m] + k2 * phi[m + st[a]];
+      g2 = k0 * phi[c - st[a]] + k1 * phi[c] + k2 * phi[c + st[a]];
+    }
+    gr[a] = c1 * g1 + c2 * g2;
+  }
+  double nrm = sqrt(gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2]);
+  if (nrm != 0.0) { const double inv = 1.0 / nrm; for (int a = 0; a < 3; a++) gr[a] *= inv; }
+  if (idm == 0) for (int a = 0; a < 3; a++) gr[a] *= -1.0;
+  if (sqrt(gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2]) == 0.0) gr[d] = 1.0;
+  if (gr[d] < 0.0) gr[d] *= -1.0;
+  if (P.riemann_normal == M2CG_RNORMAL_AVERAGE) {
+    gr[d] += 1.0;
+    const double inv = 1.0 / sqrt(gr[0] * gr[0] + gr[1] * gr[1] + gr[2] * gr[2]);
+    for (int a = 0; a < 3; a++) gr[a] *= inv;
+  }
+  for (int a = 0; a < 3; a++) dir[a] = gr[a];
+}
+
 // Solves interface face s and stores its fluxes; returns 2 without storing
 // anything when the solver's evaluation budget ran out.
 __device__ __forceinline__ int iface_solve(const Params& P, StateSet S, const int32_t* __restrict__ id,
@@ -97,6 +159,7 @@ __device__ __forceinline__ int iface_solve(const Params& P, StateSet S, const in
   }
   double dir[3] = {0.0, 0.0, 0.0};
   dir[d] = 1.0;  // RiemannNormal = Mesh (SpaceOperator.cpp:2186-2203)
+  if (P.riemann_normal != M2CG_RNORMAL_MESH) riemann_normal_dir(P, c, d, idm, idp, dir);
   double Vs[5], Vsm[5], Vsp[5];
   int midid = idm;
   rs.warm_p = warm ? (double)warm[s] : 0.0;

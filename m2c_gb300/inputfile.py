@@ -236,6 +236,7 @@ _MPFLUX = {"Exact": abi.MPFLUX_EXACT, "Numerical": abi.MPFLUX_NUMERICAL, "LocalL
 _MPREC = {"Constant": abi.MPREC_CONSTANT, "Linear": abi.MPREC_LINEAR}
 _PC = {"RiemannSolution": abi.PHASECHANGE_RIEMANN, "Extrapolation": abi.PHASECHANGE_EXTRAPOLATION}
 _PCDIR = {"All": abi.PCDIR_ALL, "Upwind": abi.PCDIR_UPWIND}
+_RNORMAL = {"Mesh": abi.RNORMAL_MESH, "LevelSet": abi.RNORMAL_LEVEL_SET, "Average": abi.RNORMAL_AVERAGE}
 _TS = {"ForwardEuler": abi.TS_FORWARD_EULER, "RungeKutta2": abi.TS_RK2, "RungeKutta3": abi.TS_RK3}
 _EOS = {"StiffenedGas": abi.EOS_SG, "NobleAbelStiffenedGas": abi.EOS_NASG, "MieGruneisen": abi.EOS_MG}
 _LSSOLVER = {"FiniteVolume": abi.LS_FINITE_VOLUME, "FiniteDifference": abi.LS_FINITE_DIFFERENCE}   # IoData.cpp:1544-1547
@@ -400,8 +401,7 @@ class Case:
         c.mp_phasechange = _tok(_PC, mp.get("PhaseChange", "RiemannSolution"), "MultiPhase.PhaseChange")
         c.mp_phasechange_dir = _tok(_PCDIR, mp.get("PhaseChangeDirection", "Upwind"),
                                     "MultiPhase.PhaseChangeDirection")
-        if mp.get("RiemannNormal", "Mesh") != "Mesh":
-            raise NotImplementedError(f"MultiPhase.RiemannNormal = {mp['RiemannNormal']}")
+        c.mp_riemann_normal = _tok(_RNORMAL, mp.get("RiemannNormal", "Mesh"), "MultiPhase.RiemannNormal")
 
         er = t.get("ExactRiemannSolution", {})
         for key, attr, typ in (("MaxIts", "maxits_main", int), ("MaxItsBracketing", "maxits_bracket", int),

@@ -90,6 +90,7 @@ struct Oracle {
   void EndOfStep(std::vector<double>& phi0);
   void UpdateIDByLevelSet(const std::vector<double>& phi_old);
   void FixUnresolvedNodes(const std::vector<std::array<int, 3>>& unresolved);
+  void RiemannNormal(int d, int i, int j, int k, int myid, int nid, double dir[3]) const;
   // level-set reinitialization (full domain, first layer FIXED)
   double reinit_cfl = 0.8;
   int reinit_retries = 0, reinit_failures = 0, reinit_calls = 0, reinit_iters = 0;
@@ -545,6 +546,70 @@ bool Oracle::NumFlux(int dir, const double* Vm, const double* Vp, int id, double
 }
 
 // SpaceOperator.cpp:1432-2076 then 2573-2641.  R is ghosted AoS; only real cells are meaningful.
+// SpaceOperator::GetNormalForBimaterialRiemann (SpaceOperator.cpp:2186-2203)
+// with CalculateGradPhiAtCellInterface (2208-2266, one level set) and
+// CalculateGradientAtCellInterface (2270-2415) on the uniform mesh, for the face
+// between cell (i,j,k) (material myid) and its minus neighbour along d (nid).
+// Phi is phi at the start of the step while the residuals of a step are formed
+// (TimeIntegrator.cpp:350, 403).  Faces whose materials are not 0 and the level
+// set's (where the reference asserts) keep the mesh normal.
+void Oracle::RiemannNormal(int d, int i, int j, int k, int myid, int nid, double dir[3]) const {
+  dir[0] = dir[1] = dir[2] = 0.0;
+  dir[d] = 1.0;
+  const int my_ls = (myid == 0) ? nid : myid, neigh_ls = (nid == 0) ? myid : nid;
+  if (cfg.mp_riemann_normal == M2CG_RNORMAL_MESH || my_ls != cfg.ls_matid || neigh_ls != cfg.ls_matid) return;
+  const double lo[3] = {cfg.x0, cfg.y0, cfg.z0}, h[3] = {dx, dy, dz};
+  const int n[3] = {NX, NY, NZ};
+  auto X = [&](int a, int q) { return lo[a] + 0.5 * h[a] + q * h[a]; };   // coords (MeshGenerator.cpp:166-171)
+  auto P = [&](const int* q) { return Phi[idx(q[0], q[1], q[2])]; };
+  auto central = [](double p0, double p1, double p2, double x0, double x1, double x2) {   // SpaceOperator.h:223-228
+    double c0 = -(x2 - x1) / ((x1 - x0) * (x2 - x0));
+    double c1 = 1.0 / (x1 - x0) - 1.0 / (x2 - x1);
+    double c2 = (x1 - x0) / ((x2 - x0) * (x2 - x1));
+    return c0 * p0 + c1 * p1 + c2 * p2;
+  };
+  const int pc[3] = {i, j, k};
+  int pm[3] = {i, j, k};
+  pm[d] -= 1;
+  double g[3];
+  g[d] = (P(pc) - P(pm)) / (X(d, pc[d]) - X(d, pm[d]));
+  const double x_minus_half = X(d, pc[d]) - 0.5 * h[d];
+  const double dxd = X(d, pc[d]) - X(d, pm[d]);
+  const double c1 = (X(d, pc[d]) - x_minus_half) / dxd;
+  const double c2 = (x_minus_half - X(d, pm[d])) / dxd;
+  for (int a = 0; a < 3; a++) {
+    if (a == d) continue;
+    const int q = pc[a];
+    int mp[3] = {pm[0], pm[1], pm[2]}, mm[3] = {pm[0], pm[1], pm[2]}, cp[3] = {pc[0], pc[1], pc[2]},
+        cmn[3] = {pc[0], pc[1], pc[2]};
+    mp[a] += 1; mm[a] -= 1; cp[a] += 1; cmn[a] -= 1;
+    double g1, g2;
+    if (q < 0) {
+      g1 = (P(mp) - P(pm)) / (X(a, q + 1) - X(a, q));
+      g2 = (P(cp) - P(pc)) / (X(a, q + 1) - X(a, q));
+    } else if (q >= n[a]) {
+      g1 = (P(pm) - P(mm)) / (X(a, q) - X(a, q - 1));
+      g2 = (P(pc) - P(cmn)) / (X(a, q) - X(a, q - 1));
+    } else {
+      g1 = central(P(mm), P(pm), P(mp), X(a, q - 1), X(a, q), X(a, q + 1));
+      g2 = central(P(cmn), P(pc), P(cp), X(a, q - 1), X(a, q), X(a, q + 1));
+    }
+    g[a] = c1 * g1 + c2 * g2;
+  }
+  auto norm = [](const double* v) { return std::sqrt(v[0] * v[0] + v[1] * v[1] + v[2] * v[2]); };
+  double nrm = norm(g);
+  if (nrm != 0.0) { double r = 1.0 / nrm; for (int a = 0; a < 3; a++) g[a] *= r; }   // Vec3D::operator/=
+  if (nid == 0) for (int a = 0; a < 3; a++) g[a] *= -1.0;
+  if (norm(g) == 0.0) g[d] = 1.0;
+  if (g[d] < 0.0) g[d] *= -1.0;
+  if (cfg.mp_riemann_normal == M2CG_RNORMAL_AVERAGE) {
+    g[d] += 1.0;
+    double r = 1.0 / norm(g);
+    for (int a = 0; a < 3; a++) g[a] *= r;
+  }
+  for (int a = 0; a < 3; a++) dir[a] = g[a];
+}
+
 void Oracle::ComputeResidual(const std::vector<double>& v, const std::vector<int>& id, std::vector<double>& R, bool store) {
   std::vector<double> fs[6];
   Reconstruct(v, id, fs);
@@ -583,8 +648,8 @@ void Oracle::ComputeResidual(const std::vector<double>& v, const std::vector<int
                 FluxLLF2(vf[nid], vf[myid], d, Vm, Vp, L1);
                 for (int p = 0; p < 5; p++) L2[p] = L1[p];
               } else {
-                double dirv[3] = {0, 0, 0};
-                dirv[d] = 1.0;  // RiemannNormal = Mesh (SpaceOperator.cpp:2186-2203)
+                double dirv[3];
+                RiemannNormal(d, i, j, k, myid, nid, dirv);
                 double Vmid[5], Vsm[5], Vsp[5];
                 int midid = 0;
                 int err = riemann.Solve(dirv, Vm, nid, Vp, myid, Vmid, midid, Vsm, Vsp);

@@ -1,0 +1,76 @@
+"""MultiPhase.RiemannNormal (SpaceOperator.cpp:2186-2415): the interface
+Riemann problems along the mesh axis (Mesh, the default), along the
+level set's gradient at the face (LevelSet), or along their normalized sum
+(Average).  The oracle is checked through what the normal must give: a plane
+interface perpendicular to x gives the mesh normal (the same step as Mesh to
+rounding), a sphere gives a different step that stays close to it; then the
+GPU is held to the oracle for a step and for five steps."""
+import numpy as np
+import pytest
+
+from helpers import rel_linf
+from m2c_gb300 import abi, inputfile as inf, problems
+from oracle import binding as ob
+
+
+def _oracle_step(cfg, V, ID, phi, nsteps=1):
+    o = ob.OracleSim(cfg)
+    o.upload(V, ID, phi)
+    o.run(nsteps)
+    return o.download(), o.counters()
+
+
+@pytest.mark.parametrize("normal", [abi.RNORMAL_LEVEL_SET, abi.RNORMAL_AVERAGE])
+def test_oracle_plane_interface_gives_the_mesh_normal(normal):
+    cfg, V, ID, phi = problems.riemann1d(nx=64, ny=4, nz=4)
+    (Vm, IDm, pm), _ = _oracle_step(cfg, V, ID, phi, 3)
+    cfg.mp_riemann_normal = normal
+    (Vn, IDn, pn), _ = _oracle_step(cfg, V, ID, phi, 3)
+    np.testing.assert_array_equal(IDn, IDm)
+    assert np.all(rel_linf(Vn, Vm)[[0, 1, 4]] < 1e-12)
+    assert np.abs(Vn[:, 2:4]).max() < 1e-9 * np.abs(Vn[:, 1]).max()
+
+
+@pytest.mark.parametrize("normal", [abi.RNORMAL_LEVEL_SET, abi.RNORMAL_AVERAGE])
+def test_oracle_sphere_normal_changes_the_step_a_little(normal):
+    cfg, V, ID, phi = problems.shock_bubble(n=16)
+    (Vm, IDm, pm), cm = _oracle_step(cfg, V, ID, phi)
+    cfg.mp_riemann_normal = normal
+    (Vn, IDn, pn), cn = _oracle_step(cfg, V, ID, phi)
+    e = rel_linf(Vn, Vm)
+    assert 0.0 < e[0] < 1e-2 and e[4] < 1e-2
+    assert cn["riemann_errors"] == 0 and cn["interface_faces"] == cm["interface_faces"]
+
+
+def test_input_reader_takes_the_normal():
+    base = "under Mesh { NumberOfCellsX = 4; NumberOfCellsY = 4; NumberOfCellsZ = 4; }\n" \
+           "under Equations { under Material[0] { EquationOfState = StiffenedGas; }\n" \
+           "                  under Material[1] { EquationOfState = StiffenedGas; } }\n" \
+           "under Space { under LevelSet[0] { MaterialID = 1; } }\n"
+    for name, val in (("LevelSet", abi.RNORMAL_LEVEL_SET), ("Average", abi.RNORMAL_AVERAGE),
+                      ("Mesh", abi.RNORMAL_MESH)):
+        cs = inf.Case.from_text(base + "under MultiPhase { RiemannNormal = %s; }\n" % name)
+        assert cs.cfg.mp_riemann_normal == val
+    with pytest.raises(NotImplementedError):
+        inf.Case.from_text(base + "under MultiPhase { RiemannNormal = EmbeddedSurface; }\n")
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("nsteps,tol", [(1, 1e-10), (5, 1e-8)])
+@pytest.mark.parametrize("normal", [abi.RNORMAL_LEVEL_SET, abi.RNORMAL_AVERAGE])
+def test_gpu_matches_oracle(normal, nsteps, tol):
+    from m2c_gb300.solver import FluidState, Solver
+    cfg, V, ID, phi = problems.shock_bubble(n=24)
+    cfg.mp_riemann_normal = normal
+    cfg.ts_type = abi.TS_RK3
+    (Vo, IDo, po), co = _oracle_step(cfg, V, ID, phi, nsteps)
+    s = Solver(cfg, FluidState(V, ID, phi))
+    c = s.run(nsteps)
+    g = s.get_state()
+    np.testing.assert_array_equal(g.ID, IDo)
+    e = rel_linf(g.V, Vo)
+    vmax = np.sqrt((Vo[:, 1:4] ** 2).sum(1)).max()
+    e[1:4] = np.abs(g.V[:, 1:4] - Vo[:, 1:4]).max(0) / vmax
+    assert np.all(e < tol), e
+    assert rel_linf(g.Phi, po) < tol
+    assert c["riemann_solves"] == co["riemann_solves"] and c["riemann_errors"] == co["riemann_errors"] == 0
