@@ -33,6 +33,7 @@ def _load_oracle():
         "orc_counters": (None, [_P, C.POINTER(Counters)]),
         "orc_conserved_totals": (None, [_P, _D]),
         "orc_integrate": (None, [_P, _D, _D]),
+        "orc_riemann_normal": (None, [_P, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, C.c_int, _D]),
         "orc_riemann_batch": (None, [C.POINTER(Config), C.c_int64, _D, _I, _D, _I, _D, _D, _I, _D, _D, _I, _I, _D]),
         "orc_flux_batch": (None, [C.POINTER(Config), C.c_int64, _I, _D, _D, _I, _D]),
     }
@@ -110,6 +111,11 @@ class OracleSim:
         out = np.zeros((self.cfg.n_materials, 6))
         b = None if box is None else np.ascontiguousarray(box, np.float64)
         lib().orc_integrate(self.h, dptr(b), dptr(out))
+        return out
+
+    def riemann_normal(self, d, i, j, k, myid, nid):
+        out = np.zeros(3)
+        lib().orc_riemann_normal(self.h, d, i, j, k, myid, nid, dptr(out))
         return out
 
     def download_ghosted(self):

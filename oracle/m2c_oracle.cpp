@@ -1493,6 +1493,12 @@ void orc_counters(void* h, m2cg_counters* c) {
   c->unresolved_fixed = o->cnt.unresolved_fixed;
 }
 
+// The interface Riemann normal of the face between cell (i,j,k) and its minus
+// neighbour along d, from the current level set (unit tests of RiemannNormal).
+void orc_riemann_normal(void* h, int d, int i, int j, int k, int myid, int nid, double* dir) {
+  ((Oracle*)h)->RiemannNormal(d, i, j, k, myid, nid, dir);
+}
+
 void orc_conserved_totals(void* h, double* tot) {
   Oracle* o = (Oracle*)h;
   for (int p = 0; p < 5; p++) tot[p] = 0.0;
