@@ -74,11 +74,13 @@ def test_gpu_matches_oracle(normal, nsteps, tol):
     assert np.all(e < tol), e
     assert rel_linf(g.Phi, po) < tol
     assert c["riemann_solves"] == co["riemann_solves"]
-    # with RK3, gradient normals turn some near-trivial problems (equal pressures, nearly equal normal
-    # velocities) into ones the solver reports as not converged, on both sides (about 7 % of them
-    # here); whether such a solve converges follows the last bits of its face states, while its
-    # star state does not (the states above agree to the tolerance)
-    assert abs(c["riemann_errors"] - co["riemann_errors"]) <= 0.25 * co["riemann_errors"] + 5
+    # with RK3, gradient normals turn some near-trivial problems (equal pressures, normal velocities
+    # equal to rounding) into solves reported as not converged: the oracle 59 of 792 after one step,
+    # the GPU 51.  Whether such a solve converges follows the last bits of its face states (the GPU's
+    # reconstruction contracts to FMA), while its star state does not: the states above agree to the
+    # tolerance.  Both sides report them.
+    assert (c["riemann_errors"] > 0) == (co["riemann_errors"] > 0)
+    assert c["riemann_errors"] <= co["riemann_errors"] + 10
 
 
 @pytest.mark.parametrize("normal", [abi.RNORMAL_LEVEL_SET, abi.RNORMAL_AVERAGE])
