@@ -20,7 +20,7 @@ TOL100 = 1e-8
 def state_err(a, b):
     """Relative L-infinity per variable; the three velocity components are
     normalized by the largest velocity magnitude (a component that is zero
-    everywhere in the oracle would otherwise be judged on rounding noise)."""
+    everywhere in the oracle would otherwise be compared on rounding noise)."""
     e = rel_linf(a, b)
     vmax = np.sqrt((b[:, 1:4] ** 2).sum(1)).max()
     if vmax > 0:
