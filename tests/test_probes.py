@@ -321,3 +321,26 @@ def test_gpu_run_case_matches_oracle_outputs(tmp_path):
         a = np.loadtxt(tmp_path / "o" / name)
         b = np.loadtxt(tmp_path / "g" / name)
         np.testing.assert_allclose(b, a, rtol=1e-7, atol=1e-9 * np.abs(a).max())
+
+
+def test_run_case_time_interval_outputs_step_one_at_a_time(tmp_path):
+    """An output on a time interval is written after every step whose interval
+    (t - dt, t] crosses a multiple of it (Utils.cpp:345-349), so the loop steps
+    one at a time; the final forced write adds the last state unless it was
+    just written."""
+    from m2c_gb300 import driver
+    text = CASE.split("under Output")[0] + RUN.replace("PREFIX", str(tmp_path) + "/t_")
+    cs = inf.Case.from_text(text)
+    sim = _OracleRun(cs)
+    o2 = _OracleRun(cs)
+    times = [0.0]
+    for _ in range(cs.max_its):
+        times.append(o2.run(1)["time"])
+    interval = 2.5 * times[1]
+    cs.probes["frequency"], cs.probes["frequency_dt"] = -100, interval
+    c, written = driver.run_case(cs, sim, snapshots=False)
+    t = np.array(times)
+    crossing = [s for s in range(1, len(t)) if np.floor(t[s] / interval) != np.floor(t[s - 1] / interval)]
+    steps = [int(l.split()[0]) for l in (tmp_path / "t_p.txt").read_text().splitlines()]
+    expect = [0] + crossing + ([cs.max_its] if cs.max_its not in crossing else [])
+    assert steps == expect and len(crossing) >= 1
