@@ -34,8 +34,10 @@ typedef enum {
   M2CG_OK = 0,
   M2CG_ERR_INVALID_ARG = 1,    /* null pointer, bad size, unsupported option */
   M2CG_ERR_CUDA = 2,           /* a CUDA runtime call failed (message via m2cg_last_error) */
-  M2CG_ERR_NONPHYSICAL = 3,    /* a state failed CheckState; the reference calls exit(-1) here */
-  M2CG_ERR_UNRESOLVED = 4,     /* swept cell with no usable Riemann solution and no reinitializer */
+  M2CG_ERR_NONPHYSICAL = 3,    /* reserved: where the reference calls exit(-1) on a failed CheckState the
+                                  library counts the state (m2cg_counters.nonphysical) and goes on */
+  M2CG_ERR_UNRESOLVED = 4,     /* reserved: unresolved swept cells without a reinitializer, where the
+                                  reference stops, are counted (unresolved_cells - unresolved_fixed) */
   M2CG_ERR_NO_DEVICE = 5,      /* no CUDA device visible */
   M2CG_ERR_CAPACITY = 6        /* a fixed-size buffer would overflow */
 } m2cg_status;
