@@ -5,7 +5,7 @@ says so (Utils.cpp:337-357), and a final forced write.
 
 The outputs are the ones of `Output` in the input file: solution snapshots
 (`<prefix><Solution>_NNNN.vtr` + `.pvd`), line plots (`<prefix><FileName>_NNNN.txt`,
-ProbeOutput.cpp:483-597), probe histories and energy integrals.  Steps run in
+ProbeOutput.cpp:483-597), probe histories, energy integrals and material volumes.  Steps run in
 chunks of replayed step graphs up to the next step at which an output is due;
 an output on a time interval makes every step its own chunk.
 
@@ -57,7 +57,8 @@ def run_case(case, sim, prefix=None, snapshots=True, chunk=64):
     lines = [_LineSeries(case, p, pre) for p in case.line_plots]
     probes = inputfile.ProbeOutput(case, prefix=pre)
     energy = inputfile.EnergyIntegrationOutput(case, prefix=pre)
-    written = {"snapshots": 0, "lines": 0, "probes": 0, "energy": 0}
+    volumes = inputfile.MaterialVolumeOutput(case, prefix=pre)
+    written = {"snapshots": 0, "lines": 0, "probes": 0, "energy": 0, "volumes": 0}
     cache = {}
 
     def ghosted():
@@ -81,13 +82,14 @@ def run_case(case, sim, prefix=None, snapshots=True, chunk=64):
             else:
                 written["probes"] += probes.write(time, dt, step, *ghosted(), force=force)
         written["energy"] += energy.write(time, dt, step, sim, force=force)
+        written["volumes"] += volumes.write(time, dt, step, sim, force=force)
 
     c = sim.counters()
     out(c["time"], 0.0, c["steps"], True)                       # Main.cpp:571
     by_time = (sol["frequency_dt"] > 0 and series is not None) or any(p["frequency_dt"] > 0 for p in case.line_plots) \
-        or probes.frequency_dt > 0 or energy.frequency_dt > 0
+        or probes.frequency_dt > 0 or energy.frequency_dt > 0 or (volumes.f is not None and volumes.frequency_dt > 0)
     freqs = ([sol["frequency"]] if series is not None else []) + [p["frequency"] for p in case.line_plots] + \
-        [probes.frequency, energy.frequency]
+        [probes.frequency, energy.frequency] + ([volumes.frequency] if volumes.f is not None else [])
     while c["steps"] < case.max_its and c["time"] < case.max_time * (1.0 - 1e-12):
         n = 1 if by_time else chunk
         for f in freqs:
@@ -103,4 +105,5 @@ def run_case(case, sim, prefix=None, snapshots=True, chunk=64):
     out(c["time"], c["dt"], c["steps"], True)                   # Main.cpp:782
     probes.close()
     energy.close()
+    volumes.close()
     return c, written

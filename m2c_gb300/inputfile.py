@@ -21,6 +21,8 @@ plots that go with them.
 * `ProbeOutput`: time histories at the probe nodes of `Output.Probes`
   (ProbeOutput.cpp:14-350, 599-848; IoData.cpp:3152-3230), written when
   Utils.cpp:337-357 says so, one file per requested field.
+* `MaterialVolumeOutput`: volume of every material over time
+  (`Output.MaterialVolumes`; MaterialVolumeOutput.cpp:11-120).
 * `EnergyIntegrationOutput`: per-material volume, mass and energies in a box
   (`Output.EnergyIntegration`; EnergyIntegrationOutput.cpp:13-245,
   IoData.cpp:3237-3281), from `Solver.integrate` on the device.
@@ -278,6 +280,7 @@ class Case:
         self.line_plots = []
         self.probes = None
         self.energy_integration = None
+        self.material_volumes = None
         self.solution = {"base": "solution", "frequency": 0, "frequency_dt": -1.0}
         self.prefix = ""
         self.max_time = 1e10
@@ -448,6 +451,10 @@ class Case:
             self.probes = _probes(out["Probes"])
         if "EnergyIntegration" in out:
             self.energy_integration = _energy_integration(out["EnergyIntegration"])
+        mv = out.get("MaterialVolumes")
+        if mv:   # MaterialVolumes::MaterialVolumes, IoData.cpp:2924-2938
+            self.material_volumes = {"file": str(mv.get("FileName", "")), "frequency": int(mv.get("Frequency", 10)),
+                                     "frequency_dt": float(mv.get("TimeInterval", -1.0))}
         return self
 
     # -- initial state -------------------------------------------------------
@@ -710,6 +717,48 @@ class ProbeOutput:
     def close(self):
         for f in self.files.values():
             f.close()
+
+
+class MaterialVolumeOutput:
+    """The volume of every material and of the ghost / inactive ID (none on
+    this path: 0) with their sum, one line per output
+    (MaterialVolumeOutput.cpp:11-85).  `write` takes any object with
+    `integrate(box)`."""
+
+    def __init__(self, case, prefix=None):
+        mv = case.material_volumes or {"file": "", "frequency": 10, "frequency_dt": -1.0}
+        self.frequency, self.frequency_dt = mv["frequency"], mv["frequency_dt"]
+        self.last = -1.0
+        self.f = None
+        if mv["file"]:
+            c = case.cfg
+            pre = case.prefix if prefix is None else prefix
+            self.f = open(pre + mv["file"], "w")
+            n = c.n_materials + 1
+            self.f.write("## Number of physical materials: %d (0 - %d); ID for ghost/inactive cells: %d.\n"
+                         % (n - 1, n - 2, n - 1))
+            self.f.write("## Total volume of computational domain: %e.\n"
+                         % ((c.xmax - c.x0) * (c.ymax - c.y0) * (c.zmax - c.z0)))
+            self.f.write("## The last column is the sum over all material subdomains (including ghost/inactive).\n")
+            self.f.flush()
+
+    def write(self, time, dt, step, sim, force=False):
+        if self.f is None or not is_time_to_write(time, dt, step, self.frequency_dt, self.frequency, self.last, force):
+            return False
+        vol = list(sim.integrate(None)[:, 0]) + [0.0]
+        self.f.write("%8d  %16.8e  " % (step, time))
+        total = 0.0
+        for v in vol:
+            self.f.write("%16.8e  " % v)
+            total += v
+        self.f.write("%16.8e\n" % total)
+        self.f.flush()
+        self.last = time
+        return True
+
+    def close(self):
+        if self.f is not None:
+            self.f.close()
 
 
 class EnergyIntegrationOutput:

@@ -253,7 +253,8 @@ RUN = """under Output { Prefix = "PREFIX"; Frequency = 3;
   under LinePlot[0] { FileName = "line"; NumberOfPoints = 9; Frequency = 2; X0 = 0.03; Xmax = 0.97;
                       Y0 = 0.25; Ymax = 0.25; Z0 = 0.1; Zmax = 0.1; }
   under Probes { Frequency = 2; Pressure = "p.txt"; under Node[0] { X = 0.41; Y = 0.26; Z = 0.13; } }
-  under EnergyIntegration { Frequency = 3; Mass = "mass.txt"; } }
+  under EnergyIntegration { Frequency = 3; Mass = "mass.txt"; }
+  under MaterialVolumes { FileName = "volumes.txt"; Frequency = 2; } }
 """
 
 
@@ -294,11 +295,17 @@ def test_run_case_writes_every_output_on_its_schedule(tmp_path):
     (c, written), sim = _run_case(_OracleRun, tmp_path)
     assert c["steps"] == 6
     # snapshots: 0 (initial), 3, 6; lines and probes: 0, 2, 4, 6; energy: 0, 3, 6
-    assert written == {"snapshots": 3, "lines": 4, "probes": 4, "energy": 3}
+    assert written == {"snapshots": 3, "lines": 4, "probes": 4, "energy": 3, "volumes": 4}
     names = sorted(p.name for p in tmp_path.iterdir())
     assert names == ["r_line_0000.txt", "r_line_0001.txt", "r_line_0002.txt", "r_line_0003.txt", "r_mass.txt",
                      "r_p.txt", "r_solution.pvd", "r_solution_0000.vtr", "r_solution_0001.vtr",
-                     "r_solution_0002.vtr"]
+                     "r_solution_0002.vtr", "r_volumes.txt"]
+    vol = (tmp_path / "r_volumes.txt").read_text().splitlines()
+    assert vol[0].startswith("## Number of physical materials: 2 (0 - 1); ID for ghost/inactive cells: 2.")
+    rows = [[float(v) for v in l.split()] for l in vol[3:]]
+    assert [int(r[0]) for r in rows] == [0, 2, 4, 6]
+    for r in rows:   # step, time, material 0, material 1, ghost / inactive, sum = the domain's volume
+        assert len(r) == 6 and r[4] == 0.0 and r[5] == pytest.approx(0.125, rel=1e-12) and r[3] > 0
     head = (tmp_path / "r_line_0003.txt").read_text().splitlines()
     assert head[2].startswith("## Time: ") and head[2].endswith("Time step: 6.")
     assert [int(l.split()[0]) for l in (tmp_path / "r_p.txt").read_text().splitlines()] == [0, 2, 4, 6]
