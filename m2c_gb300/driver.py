@@ -14,6 +14,7 @@ an output on a time interval makes every step its own chunk.
 present).
 """
 import os
+import time as _time
 
 from . import inputfile, output
 
@@ -43,9 +44,12 @@ def _due_steps(freq, step):
     return None if freq <= 0 else freq - step % freq
 
 
-def run_case(case, sim, prefix=None, snapshots=True, chunk=64):
+def run_case(case, sim, prefix=None, snapshots=True, chunk=64, log=None):
     """Runs `case` on `sim` with the case's outputs; returns the final counters
-    and the number of files written per kind."""
+    and the number of files written per kind.  With `log` (e.g. print) the
+    steps run one at a time and each gets the reference's progress line
+    (Main.cpp:699-701)."""
+    start = _time.perf_counter()
     pre = case.prefix if prefix is None else prefix
     d = os.path.dirname(pre)
     if d:
@@ -91,7 +95,7 @@ def run_case(case, sim, prefix=None, snapshots=True, chunk=64):
     freqs = ([sol["frequency"]] if series is not None else []) + [p["frequency"] for p in case.line_plots] + \
         [probes.frequency, energy.frequency] + ([volumes.frequency] if volumes.f is not None else [])
     while c["steps"] < case.max_its and c["time"] < case.max_time * (1.0 - 1e-12):
-        n = 1 if by_time else chunk
+        n = 1 if (by_time or log is not None) else chunk
         for f in freqs:
             k = _due_steps(f, c["steps"])
             if k is not None:
@@ -101,6 +105,9 @@ def run_case(case, sim, prefix=None, snapshots=True, chunk=64):
         c = sim.run(n)
         if c["steps"] == before:   # MaxTime reached
             break
+        if log is not None:
+            log("Step %d: t = %e, dt = %e, cfl = %.4e. Computation time: %.4e s."
+                % (c["steps"], c["time"] - c["dt"], c["dt"], c["cfl"], _time.perf_counter() - start))
         out(c["time"], c["dt"], c["steps"], False)              # Main.cpp:769
     out(c["time"], c["dt"], c["steps"], True)                   # Main.cpp:782
     probes.close()

@@ -351,3 +351,12 @@ def test_run_case_time_interval_outputs_step_one_at_a_time(tmp_path):
     steps = [int(l.split()[0]) for l in (tmp_path / "t_p.txt").read_text().splitlines()]
     expect = [0] + crossing + ([cs.max_its] if cs.max_its not in crossing else [])
     assert steps == expect and len(crossing) >= 1
+
+
+def test_run_case_logs_the_reference_progress_line(tmp_path):
+    from m2c_gb300 import driver
+    cs = inf.Case.from_text(CASE.split("under Output")[0] + RUN.replace("PREFIX", str(tmp_path) + "/l_"))
+    lines = []
+    c, _ = driver.run_case(cs, _OracleRun(cs), snapshots=False, log=lines.append)
+    assert len(lines) == c["steps"] == 6
+    assert lines[0].startswith("Step 1: t = 0.000000e+00, dt = ") and ", cfl = 4.0000e-01. Computation time: " in lines[0]
