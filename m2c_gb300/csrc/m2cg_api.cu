@@ -1462,10 +1462,6 @@ m2cg_status m2cg_ensemble_create(const m2cg_config* cfgs, int32_t n, m2cg_ensemb
       set_err("member %d: the batched step advects the level set by finite differences only", d);
       return M2CG_ERR_INVALID_ARG;
     }
-    if (cfgs[d].mp_riemann_normal != M2CG_RNORMAL_MESH) {
-      set_err("member %d: the batched step solves interface problems along the mesh axes only", d);
-      return M2CG_ERR_INVALID_ARG;
-    }
     if (cfgs[d].n_levelsets > 0 && (cfgs[d].reinit_frequency > 0 || cfgs[d].reinit_frequency_dt > 0)) {
       set_err("member %d: the batched step does not reinitialize level sets (reinit_frequency must be <= 0)", d);
       return M2CG_ERR_INVALID_ARG;

@@ -5,7 +5,7 @@ own CFL step); the sequential baseline agrees too."""
 import numpy as np
 import pytest
 
-from m2c_gb300 import problems
+from m2c_gb300 import abi, problems
 from m2c_gb300.ensemble import Ensemble
 from m2c_gb300.solver import FluidState, Solver
 
@@ -27,8 +27,11 @@ def test_ensemble_problem_shapes():
 
 
 @pytest.mark.gpu
-def test_ensemble_matches_members_run_alone():
+@pytest.mark.parametrize("normal", [abi.RNORMAL_MESH, abi.RNORMAL_AVERAGE])
+def test_ensemble_matches_members_run_alone(normal):
     doms = [problems.bubble_collapse(*d) for d in SMALL]
+    for d in doms:
+        d[0].mp_riemann_normal = normal   # interface normals from each member's own level set
     ens = Ensemble([d[0] for d in doms])
     for i, (c, V, ID, phi) in enumerate(doms):
         ens.member(i).set_state(FluidState(V, ID, phi))
