@@ -75,7 +75,7 @@ def run_case(case, sim, prefix=None, snapshots=True, chunk=64, log=None):
         if series is not None and inputfile.is_time_to_write(time, dt, step, sol["frequency_dt"], sol["frequency"],
                                                              sol_last[0], force):
             st = sim.get_state()
-            series.write(case.cfg, st.V, st.ID, st.Phi, time)
+            series.write(case.cfg, st.V, st.ID, st.Phi, time, sol.get("fields"))
             sol_last[0] = time
             written["snapshots"] += 1
         for ln in lines:

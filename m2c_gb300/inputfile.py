@@ -281,7 +281,7 @@ class Case:
         self.probes = None
         self.energy_integration = None
         self.material_volumes = None
-        self.solution = {"base": "solution", "frequency": 0, "frequency_dt": -1.0}
+        self.solution = {"base": "solution", "frequency": 0, "frequency_dt": -1.0, "fields": []}
         self.prefix = ""
         self.max_time = 1e10
         self.max_its = 2 ** 31 - 1
@@ -446,7 +446,12 @@ class Case:
         self.prefix = str(out.get("Prefix", ""))
         # solution snapshots (OutputData, IoData.cpp:2970-2974, 3027-3031)
         self.solution = {"base": str(out.get("Solution", "solution")), "frequency": int(out.get("Frequency", 0)),
-                         "frequency_dt": float(out.get("TimeInterval", -1.0))}
+                         "frequency_dt": float(out.get("TimeInterval", -1.0)),
+                         # fields switched On (all Off by default, IoData.cpp:2976-2994)
+                         "fields": [name for key, name in (("Density", "density"), ("Velocity", "velocity"),
+                                                           ("Pressure", "pressure"), ("MaterialID", "materialid"),
+                                                           ("LevelSet0", "levelset0"))
+                                    if out.get(key, "Off") == "On"]}
         if "Probes" in out:
             self.probes = _probes(out["Probes"])
         if "EnergyIntegration" in out:

@@ -18,19 +18,24 @@ def _b64(arr):
     return base64.b64encode(struct.pack("<Q", len(raw)) + raw).decode("ascii")
 
 
-def write_vtr(path, cfg, V, ID, phi=None, time=None):
+def write_vtr(path, cfg, V, ID, phi=None, time=None, fields=None):
     """Write one snapshot.  V: (N, 5) primitive state of the real cells
-    (k-major, i fastest), ID: (N,), phi: (N,) or None."""
+    (k-major, i fastest), ID: (N,), phi: (N,) or None.  fields: the point
+    fields to write (names as below; the reference writes those switched On
+    in Output, Output.cpp:268-330), or None for all."""
     nx, ny, nz = cfg.nx, cfg.ny, cfg.nz
     coords = []
     for n, lo, hi in ((nx, cfg.x0, cfg.xmax), (ny, cfg.y0, cfg.ymax), (nz, cfg.z0, cfg.zmax)):
         h = (hi - lo) / n
         coords.append(lo + 0.5 * h + np.arange(n) * h)      # MeshGenerator.cpp:166-171
     V = np.asarray(V, np.float64).reshape(-1, 5)
+    want = None if fields is None else set(fields)
     fields = [("density", V[:, 0], 1), ("velocity", V[:, 1:4], 3), ("pressure", V[:, 4], 1),
               ("materialid", np.asarray(ID, np.float64), 1)]
     if phi is not None and cfg.n_levelsets > 0:
         fields.append(("levelset0", np.asarray(phi, np.float64), 1))
+    if want is not None:
+        fields = [f for f in fields if f[0] in want]
     ext = f"0 {nx - 1} 0 {ny - 1} 0 {nz - 1}"
     with open(path, "w") as f:
         f.write('<?xml version="1.0"?>\n')
@@ -79,9 +84,9 @@ class SolutionSeries:
         self.entries = []
         os.makedirs(prefix or ".", exist_ok=True)
 
-    def write(self, cfg, V, ID, phi, time):
+    def write(self, cfg, V, ID, phi, time, fields=None):
         name = f"{self.base}_{len(self.entries):04d}.vtr"
-        write_vtr(os.path.join(self.prefix, name), cfg, V, ID, phi, time)
+        write_vtr(os.path.join(self.prefix, name), cfg, V, ID, phi, time, fields)
         self.entries.append((time, name))
         write_pvd(os.path.join(self.prefix, self.base + ".pvd"), self.entries)
         return name

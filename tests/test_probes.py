@@ -249,7 +249,7 @@ def test_gpu_integrals_match_oracle():
 # ---------------------------------------------------------------------------
 # The main loop with its outputs (Main.cpp:571-782)
 
-RUN = """under Output { Prefix = "PREFIX"; Frequency = 3;
+RUN = """under Output { Prefix = "PREFIX"; Frequency = 3; Density = On; Pressure = On;
   under LinePlot[0] { FileName = "line"; NumberOfPoints = 9; Frequency = 2; X0 = 0.03; Xmax = 0.97;
                       Y0 = 0.25; Ymax = 0.25; Z0 = 0.1; Zmax = 0.1; }
   under Probes { Frequency = 2; Pressure = "p.txt"; under Node[0] { X = 0.41; Y = 0.26; Z = 0.13; } }
@@ -313,6 +313,7 @@ def test_run_case_writes_every_output_on_its_schedule(tmp_path):
     from m2c_gb300 import output
     snap = output.read_vtr(str(tmp_path / "r_solution_0002.vtr"))   # the final state
     np.testing.assert_array_equal(snap["density"], sim.get_state().V[:, 0])
+    assert sorted(snap) == ["density", "pressure"]   # the fields switched On, as Output.cpp:268-330
     assert "<DataSet timestep" in (tmp_path / "r_solution.pvd").read_text()
 
 
