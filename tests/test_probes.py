@@ -361,3 +361,26 @@ def test_run_case_logs_the_reference_progress_line(tmp_path):
     c, _ = driver.run_case(cs, _OracleRun(cs), snapshots=False, log=lines.append)
     assert len(lines) == c["steps"] == 6
     assert lines[0].startswith("Step 1: t = 0.000000e+00, dt = ") and ", cfl = 4.0000e-01. Computation time: " in lines[0]
+
+
+def test_run_case_writes_the_reference_line_plot_of_test1(tmp_path):
+    """The whole loop on the reference's Tests/RiemannProblems/Test1 input with
+    the oracle: the final line plot is `line_0001.txt` (the initial state is
+    frame 0), with the reference's header, and its columns match the
+    reference's own final line plot (the committed golden columns)."""
+    import json
+    import os
+    from m2c_gb300 import driver
+    golden = json.load(open(os.path.join(os.path.dirname(__file__), "golden", "reference_lines.json")))["Test1"]
+    cs = inf.Case.from_tree(golden["tree"])
+    c, written = driver.run_case(cs, _OracleRun(cs), prefix=str(tmp_path) + "/", snapshots=False)
+    assert c["steps"] == golden["step"] == 109 and written["lines"] == 2
+    lines = (tmp_path / "line_0001.txt").read_text().splitlines()
+    assert lines[0] == "## Line: (2.500000e-03, 0.000000e+00, 0.000000e+00) -> (9.975000e-01, 0.000000e+00, 0.000000e+00)"
+    assert lines[1] == "## Number of points: 200 (h = 5.000000e-03)"
+    assert lines[2] == "## Time: 2.000000e-01, Time step: 109."
+    assert lines[3].startswith("## Coordinate  |  Density  |  Velocity (Vx,Vy,Vz)  |  Pressure  |  Temperature")
+    rows = np.loadtxt(tmp_path / "line_0001.txt")
+    for col, key in ((1, "rho"), (2, "vx"), (5, "p"), (8, "phi")):
+        ref = np.asarray(golden[key])
+        assert np.abs(rows[:, col] - ref).max() <= 1e-6 * np.abs(ref).max(), key
