@@ -12,7 +12,12 @@ uploads {V, ID, phi} from pinned host memory, computes dt, advances one step
 and downloads the new state.
 `--impl reference`: the reference arm -- the oracle's CPU restatement of the
 reference numerics (the reference itself needs MPI and PETSc, absent on the
-box) on a bounded sample of the workload with every host thread.
+box) on the same workload with every host thread.
+`parity` (the CPU-baseline leg): the oracle advances the same workload from
+the same initial state as a fresh GPU context to each checkpoint of
+--parity-steps; both states, counters and conserved totals are compared
+there, beside the oracle compiled with FMA contraction (the reference's own
+rounding sensitivity).  Its wall time gives `cpu_baseline`.
 N > 1 (torchrun): replicas only -- every rank advances its own copy of the
 workload; no data-path collective (the reference's halo exchange has no
 counterpart on one GPU per replica); value = all ranks' cell-stages / max time.
@@ -46,6 +51,14 @@ FP64_PROFILE = {
     "face_flux": {"fp64_pipe_inst_per_cell": 617.5, "fp64_flop_per_cell": 706.8, "dram_bytes_per_cell": 363.0},
     "update": {"fp64_pipe_inst_per_cell": 104.5, "fp64_flop_per_cell": 122.6, "dram_bytes_per_cell": 293.9},
 }
+# DRAM bytes of one whole step graph of the 128^3 case (read + write, ncu
+# --graph-profiling graph, profiles/reinit_graph_shock_bubble_128.txt) per cell-stage.
+STEP_DRAM_BYTES_PER_CELL_STAGE = (2388.8e6 + 1971.9e6) / (128 ** 3 * 2)
+# Algorithmic bytes per cell-stage of the fused ideal (binary64 V and phi, int32
+# ID, ideal halo reuse): a first stage reads W = (V, phi) 48 B + ID 4 B and
+# writes 48 B = 100 B; a later stage also reads W^n = 148 B.  Mean over the
+# integrator's stages: forward Euler 100, RK2 124, RK3 132.
+ALG_BYTES_PER_CELL_STAGE = {1: 100.0, 2: 124.0, 3: 132.0}
 
 
 def parse():
@@ -56,9 +69,13 @@ def parse():
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--size", type=int, default=256)
     ap.add_argument("--e2e-steps", type=int, default=None)
-    ap.add_argument("--cpu-size", type=int, default=96)
-    ap.add_argument("--cpu-steps", type=int, default=2)
+    # reference arm: cells per axis of its sample (0: the workload's own size)
+    ap.add_argument("--cpu-size", type=int, default=0)
     ap.add_argument("--no-cpu", action="store_true")
+    # parity leg (the oracle on the same workload from the same initial state):
+    # checkpoints, and the last checkpoint the FMA-contracted oracle runs to
+    ap.add_argument("--parity-steps", default="1,10,50")
+    ap.add_argument("--parity-fma-steps", type=int, default=10)
     # level-set reinitialization every F steps in the main workload (0: off, as the 256^3 workload runs)
     ap.add_argument("--reinit", type=int, default=0)
     # learned warm start: training / test problems of the study (0 disables it)
@@ -130,35 +147,116 @@ def peaks():
         return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
 
 
-def cpu_port_rate(size, steps, threads=None):
-    """Oracle restatement on the host cores, shock-bubble sample of `size`^3 cells."""
+def cpu_model():
+    """The host CPU's model name and logical core count (lscpu / /proc/cpuinfo)."""
+    name = None
+    try:
+        out = subprocess.run(["lscpu"], capture_output=True, text=True, timeout=10).stdout
+        for line in out.splitlines():
+            if line.split(":")[0].strip() == "Model name":
+                name = line.split(":", 1)[1].strip()
+                break
+    except Exception:
+        pass
+    if not name:
+        try:
+            for line in open("/proc/cpuinfo"):
+                if line.lower().startswith(("model name", "cpu part")):
+                    name = line.split(":", 1)[1].strip()
+                    break
+        except Exception:
+            pass
+    return {"model": name or "unknown", "logical_cpus": os.cpu_count()}
+
+
+def oracle_leg(args, cfg, V, ID, phi, stages):
+    """The CPU-baseline leg: the oracle (the CPU restatement of the reference
+    numerics, every host thread) advances the benchmarked workload itself from
+    the same initial state as a fresh GPU context, to each parity checkpoint.
+    Its wall time over all checkpoints is the all-core CPU rate; one step of a
+    64^3 sample on one thread gives the single-thread rate.  At every
+    checkpoint the GPU state is compared with the oracle's, and -- up to
+    --parity-fma-steps -- the oracle compiled with fused multiply-add
+    contraction is compared with the oracle too: how far the reference's own
+    numerics move under a contracting compiler, the yardstick for the GPU's
+    FMA-contracting kernels."""
     from m2c_gb300 import problems
+    from m2c_gb300.solver import FluidState, Solver
     from oracle import binding as ob
-    lib = ob.lib()
-    if threads:
-        lib.orc_set_threads(threads)
-    used = lib.orc_max_threads()
-    cfg, V, ID, phi = problems.shock_bubble(n=size)
-    sim = ob.OracleSim(cfg)
-    sim.upload(V, ID, phi)
-    sim.run(1)
-    t0 = time.perf_counter()
-    sim.run(steps)
-    t = time.perf_counter() - t0
-    cells = size ** 3
-    return cells * 2 * steps / t, used, t
+    from oracle import parity
+    threads = os.cpu_count()
+    for fma in (False, True):
+        ob.lib(fma).orc_set_threads(threads)
+    used = ob.lib().orc_max_threads()
+    cells = cfg.nx * cfg.ny * cfg.nz
+    shape = (cfg.nz, cfg.ny, cfg.nx)
+    cps = sorted({int(x) for x in str(args.parity_steps).split(",") if x.strip()})
+    g = Solver(cfg, FluidState(V, ID, phi))
+    o = ob.OracleSim(cfg)
+    o.upload(V, ID, phi)
+    f = ob.OracleSim(cfg, fma=True) if args.parity_fma_steps > 0 else None
+    if f is not None:
+        f.upload(V, ID, phi)
+    t0g, t0o = g.conserved_totals(), o.conserved_totals()
+    out = {"workload": "the benchmarked workload, GPU (fresh context, graph-replayed steps) and oracle from the same "
+                       "initial state", "checkpoints": []}
+    done, t_orc = 0, 0.0
+    for c in cps:
+        g.run(c - done)
+        t = time.perf_counter()
+        o.run(c - done)
+        t_orc += time.perf_counter() - t
+        if f is not None and c <= args.parity_fma_steps:
+            f.run(c - done)
+        done = c
+        gs = g.get_state()
+        Vo, IDo, pho = o.download()
+        cp = {"step": c}
+        cp.update(parity.compare(gs.V, gs.ID, gs.Phi, Vo, IDo, pho, shape))
+        cp["counters"] = parity.counters_pair(g.counters(), o.counters())
+        tg, to = g.conserved_totals(), o.conserved_totals()
+        cp["conserved_gpu"] = parity.totals_dict(t0g, tg, ref=to)
+        cp["conserved_oracle"] = parity.totals_dict(t0o, to)
+        if f is not None and c <= args.parity_fma_steps:
+            Vf, IDf, phf = f.download()
+            y = parity.compare(Vf, IDf, phf, Vo, IDo, pho, shape)
+            cf = f.counters()
+            y["riemann_errors"] = int(cf["riemann_errors"])
+            y["riemann_iterations"] = int(cf["riemann_iterations"])
+            cp["oracle_fma_vs_oracle"] = y
+        out["checkpoints"].append(cp)
+    g.close()
+    del o, f
+    rate = cells * stages * done / t_orc
+    # one thread, one step of a 64^3 sample of the same problem
+    ob.lib().orc_set_threads(1)
+    c1, V1, I1, p1 = problems.shock_bubble(n=64)
+    o1 = ob.OracleSim(c1)
+    o1.upload(V1, I1, p1)
+    t = time.perf_counter()
+    o1.run(1)
+    t1 = time.perf_counter() - t
+    ob.lib().orc_set_threads(threads)
+    cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port",
+           "sample": f"oracle CPU restatement on the benchmarked workload itself ({cfg.nx}^3), {done} RK2 steps from "
+                     f"the initial state, {t_orc:.1f} s on {used} threads",
+           "single_thread": {"value": 64 ** 3 * stages / t1, "unit": UNIT, "cores": 1,
+                             "sample": f"shock-bubble 64^3, 1 RK2 step, {t1:.2f} s"},
+           "cpu": cpu_model()}
+    return cpu, out
 
 
 def run_reference(args):
     rank, world, _ = dist_info()
     if rank != 0:
         return 0
-    # each step: one RK2 step of the oracle on a bounded sample of the workload
+    # each step: one RK2 step of the oracle on the benchmarked workload (or a
+    # smaller sample of it when --cpu-size says so)
     threads = os.cpu_count()
     from oracle import binding as ob
     from m2c_gb300 import problems
     ob.lib().orc_set_threads(threads)
-    size = args.cpu_size
+    size = args.cpu_size or args.size
     cfg, V, ID, phi = problems.shock_bubble(n=size)
     sim = ob.OracleSim(cfg)
     sim.upload(V, ID, phi)
@@ -170,7 +268,7 @@ def run_reference(args):
     cells = size ** 3
     value = cells * 2 * args.steps / t
     c = sim.counters()
-    sample = (f"shock-bubble {size}^3 cells (same physics, IC and numerics as the {args.size}^3 workload), "
+    sample = (f"shock-bubble {size}^3 cells (the workload's physics, initial state and numerics), "
               f"{args.steps} RK2 steps after {args.warmup} warm-up")
     out = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": args.gpus,
            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
@@ -178,7 +276,8 @@ def run_reference(args):
            "config": {"workload": f"shock-bubble {args.size}^3, SG/SG, MUSCL-van Albada, HLLC, exact interface "
                                   f"Riemann @1e-10, RK2, CFL 0.4", "cells": cells, "sample": sample,
                       "parallelism": "replicas" if args.gpus > 1 else "single"},
-           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample},
+           "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample,
+                            "cpu": cpu_model()},
            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
            "riemann": {"mean_iters_per_solve": c["riemann_iterations"] / max(c["riemann_solves"], 1),
                        "solves": c["riemann_solves"]},
@@ -367,26 +466,40 @@ def run_gb300(args):
              "riemann_stragglers"]
     phase = {n: float(v) / nph for n, v in zip(names, ph)}
     dom = max(("reconstruct", "face_flux", "update"), key=lambda n: phase[n])
-    # algorithmic bytes per cell-stage for each stage kernel (binary64 state, int32 IDs)
-    #   reconstruct: read V (40) + ID (4), write 6 face states (240)            = 284
-    #   face_flux:   read 2 face states per face (3 faces: 240) + IDs (8), write 3 fluxes (120) = 368
-    #   update:      read 6 face fluxes (3 own + 3 neighbour faces, 240) + Un/Us (80) + ID (4) +
-    #                phi (8) + V own (40); write V (40) + phi (8) + U (40)       = 460
-    alg_bytes = {"reconstruct": 284, "face_flux": 368, "update": 460}
     pk, pk_kind = peaks()
     per_launch_ms = phase[dom] / stages
-    achieved_gbs = alg_bytes[dom] * cells / (per_launch_ms * 1e-3) / 1e9
     prof = FP64_PROFILE.get(dom)
+    # achieved = algorithmic bytes of the cell-stages one launch advances (the
+    # fused ideal's bytes per cell-stage x cells) / the launch's event-timed
+    # duration; traffic = the kernel's own DRAM bytes per launch (ncu, 128^3
+    # case, scaled by cells)
+    alg = ALG_BYTES_PER_CELL_STAGE[stages]
+    achieved_gbs = alg * cells / (per_launch_ms * 1e-3) / 1e9
+    # the kernels' own (unfused) bytes per cell: what each reads and writes
+    #   reconstruct: V 40 + ID 4 in, 6 face states 240 out                     = 284
+    #   face_flux:   2 face states per face (3 faces: 240) + IDs 8 in, 3 fluxes 120 out = 368
+    #   update:      6 fluxes 240 + Un/Us 80 + ID 4 + phi 8 + V 40 in, V 40 + phi 8 + U 40 out = 460
+    own_bytes = {"reconstruct": 284, "face_flux": 368, "update": 460}
+    step_ms = t_ms / args.steps
     roof = {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": achieved_gbs / pk["hbm_gbs"],
             "traffic": prof["dram_bytes_per_cell"] * cells if prof else None, "peak_source": pk_kind,
-            "alg_bytes_per_cell": alg_bytes[dom], "launch_ms": per_launch_ms}
+            "alg_bytes_per_cell_stage": alg, "launch_ms": per_launch_ms,
+            "kernel_own_bytes_per_cell": own_bytes[dom],
+            "step": {"alg_bytes_per_cell_stage": alg,
+                     "dram_bytes_per_cell_stage": STEP_DRAM_BYTES_PER_CELL_STAGE,
+                     "dram_over_alg": STEP_DRAM_BYTES_PER_CELL_STAGE / alg,
+                     "achieved_gbs": alg * cells * stages / (step_ms * 1e-3) / 1e9,
+                     "frac": alg * cells * stages / (step_ms * 1e-3) / 1e9 / pk["hbm_gbs"],
+                     "dram_source": "ncu whole-graph capture of the 128^3 step (profiles/)"}}
     # the binding bound of the stage kernels: GB300's FP64 pipe.  Peak = binary64
     # FMAs/s of this GPU measured now (m2cg_fp64_peak); achieved = the kernel's
     # FP64-pipe instructions per launch (per-cell count from the ncu profile x
-    # cells) / its event-timed duration.
+    # cells) / its event-timed duration.  The ceiling: the measured peak / the
+    # FP64-pipe instructions of one cell-stage summed over the stage kernels.
     dfma = C.c_double()
     fp64 = None
+    slots = sum(v["fp64_pipe_inst_per_cell"] for v in FP64_PROFILE.values())
     if lib.m2cg_fp64_peak(1 << 15, C.byref(dfma), None) == 0 and prof:
         inst = prof["fp64_pipe_inst_per_cell"] * cells / (per_launch_ms * 1e-3)
         flops = prof["fp64_flop_per_cell"] * cells / (per_launch_ms * 1e-3)
@@ -396,10 +509,14 @@ def run_gb300(args):
                 "fp64_pipe_inst_per_cell": prof["fp64_pipe_inst_per_cell"],
                 "fp64_flop_per_cell": prof["fp64_flop_per_cell"],
                 "peak_source": "measured now: m2cg_fp64_peak (independent binary64 FMA chains)",
-                "counts_source": "ncu, profiles/fp64_stage_kernels_shock_bubble_128.txt"}
+                "counts_source": "ncu, profiles/fp64_stage_kernels_shock_bubble_128.txt",
+                "step_fp64_pipe_inst_per_cell_stage": {k: v["fp64_pipe_inst_per_cell"] for k, v in FP64_PROFILE.items()},
+                "ceiling_cell_stage_per_s": dfma.value / slots,
+                "value_over_ceiling": value / (dfma.value / slots)}
     elif dfma.value > 0:
         fp64 = {"bound": "fp64", "peak": dfma.value / 1e9, "unit": "G FP64-pipe inst/s", "achieved": None,
-                "frac": None, "peak_source": "measured now: m2cg_fp64_peak"}
+                "frac": None, "peak_source": "measured now: m2cg_fp64_peak",
+                "ceiling_cell_stage_per_s": dfma.value / slots}
 
     # e2e through the C ABI with host buffers
     e2e_steps = args.e2e_steps or max(2, min(args.steps, 5))
@@ -472,12 +589,11 @@ def run_gb300(args):
 
     if rank != 0:
         return 0
-    cpu = None
+    cpu, parity = None, None
     if not args.no_cpu:
-        rate, used, tcpu = cpu_port_rate(args.cpu_size, args.cpu_steps)
-        cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port",
-               "sample": f"oracle CPU restatement, shock-bubble {args.cpu_size}^3, {args.cpu_steps} RK2 steps "
-                         f"({tcpu:.1f} s)"}
+        if largeres is None:
+            s.close()   # the parity leg runs its own context from the initial state
+        cpu, parity = oracle_leg(args, cfg, V, ID, phi, stages)
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
@@ -501,6 +617,7 @@ def run_gb300(args):
            "ensemble": ensres,
            "large": largeres,
            "phase_ms_per_step": phase,
+           "parity": parity,
            "counters": {k: c1[k] for k in ("clipped_cells", "nonphysical", "swept_cells", "unresolved_cells")}}
     print(json.dumps(out))
     return 0

@@ -20,6 +20,7 @@ COMMON = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "-Xcompiler",
           "-I", os.path.join(HERE, "..", "include")]
 UNITS = {
     "m2cg_kernels.cu": [],
+    "m2cg_tile.cu": [],
     "m2cg_riemann_kernels.cu": ["-fmad=false"],
     "m2cg_api.cu": [],
     "m2cg_noalloc.cu": ["-fmad=false"],

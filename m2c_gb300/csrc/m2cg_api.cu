@@ -9,6 +9,7 @@
 #include <vector>
 #include <string>
 #include <algorithm>
+#include <cmath>
 #include <cuda_bf16.h>
 #include "m2cg_internal.h"
 #include "m2cg_ens.h"
@@ -42,7 +43,7 @@ void launch_riemann_interfaces(cudaStream_t, const Params&, const Mats*, const S
                                unsigned long long*, const float*, unsigned long long*, const DevScalars*);
 void launch_riemann_stragglers(cudaStream_t, const Params&, const Mats*, const StateSet&, const int32_t*,
                                double* const*, const IfaceList&, int, double*, int, int, size_t, const int32_t*,
-                               const unsigned long long*, const float*, unsigned long long*, const DevScalars*);
+                               const unsigned long long*, const float*, unsigned long long*, const DevScalars*, int);
 cudaError_t riemann_stragglers_reserve(size_t bytes);
 void mlp_warm_faces(m2cg_mlp*, cudaStream_t, int, const Params&, const StateSet&, const int32_t*, const IfaceList&,
                     __nv_bfloat16*, float*, float*, float*, const DevScalars*);
@@ -127,6 +128,13 @@ struct m2cg_ctx {
   // blocks are placed on empty SMs before the reconstruction kernel's.
   int eval_limit = 16;
   int sblocks = 0;             // straggler blocks of 128 threads (one SM each; idle ones exit at once)
+  int strag_lanes = 1;         // straggler faces packed per warp (1: one face per warp)
+  // Fused reconstruction + face flux (m2cg_tile.cu) for each state set, when
+  // the configuration allows it; the split kernels otherwise (or with
+  // M2CG_STAGE_KERNELS=split, for comparisons).
+  bool tile_ok = false;
+  int tile_z = 16;             // planes per CTA of the fused kernel (M2CG_TILE_Z)
+  TileMaps tmaps[3];
   size_t sreserve = 0;         // their dynamic shared-memory request
   int32_t* strag = nullptr;
   unsigned long long* strag_count = nullptr;
@@ -302,11 +310,21 @@ static m2cg_status ctx_alloc(m2cg_ctx* x) {
   CK(x->alloc(&x->strag_count, 1));
   x->sblocks = std::max(1, std::min(x->nsm, x->rblocks));
   // tuning overrides: M2CG_RIEMANN_EVAL_LIMIT (first-pass budget, 0 = none),
-  // M2CG_RIEMANN_STRAGGLER_SMS (blocks of the second pass, one SM each) and
-  // M2CG_RIEMANN_HOLD_CYCLES (head start of the second pass, SM clock cycles)
+  // M2CG_RIEMANN_STRAGGLER_SMS (blocks of the second pass, one SM each),
+  // M2CG_RIEMANN_HOLD_CYCLES (head start of the second pass, SM clock cycles) and
+  // M2CG_RIEMANN_STRAGGLER_LANES (second-pass faces per warp, 1..32)
   if (const char* e = getenv("M2CG_RIEMANN_EVAL_LIMIT")) x->eval_limit = std::max(0, atoi(e));
   if (const char* e = getenv("M2CG_RIEMANN_STRAGGLER_SMS")) x->sblocks = std::min(x->rblocks, std::max(1, atoi(e)));
   if (const char* e = getenv("M2CG_RIEMANN_HOLD_CYCLES")) x->hold_cycles = std::max(0ll, atoll(e));
+  if (const char* e = getenv("M2CG_RIEMANN_STRAGGLER_LANES")) x->strag_lanes = std::min(32, std::max(1, atoi(e)));
+  {
+    const char* e = getenv("M2CG_STAGE_KERNELS");
+    bool want = !(e && strcmp(e, "split") == 0);
+    if (const char* z = getenv("M2CG_TILE_Z")) x->tile_z = std::max(1, atoi(z));
+    x->tile_ok = want && tile_supported(x->P) && tile_prepare() == cudaSuccess;
+    for (int s = 0; s < 3 && x->tile_ok; s++) x->tile_ok = tile_maps(x->P, x->S[s], &x->tmaps[s]);
+    cudaGetLastError();
+  }
   {
     int dev = 0, optin = 0;
     cudaGetDevice(&dev);
@@ -371,6 +389,21 @@ static StageArgs stage_args(m2cg_ctx* x, int stage, bool last, const StateSet& i
   return A;
 }
 
+// Reconstruction and same-material face fluxes of a stage input: the fused
+// tile kernel where available, else the split kernels.  Returns launches.
+static int64_t enqueue_recon_flux(m2cg_ctx* x, cudaStream_t s, const StateSet& in) {
+  if (x->tile_ok) {
+    for (int k = 0; k < 3; k++)
+      if (in.q[0] == x->S[k].q[0]) {
+        PHASE(PH_FLUX, launch_recon_flux_tile(s, x->tmaps[k], x->P, in, x->id, x->d_F, x->cnt, x->tile_z));
+        return 2;
+      }
+  }
+  PHASE(PH_RECON, launch_reconstruct(s, x->P, in, x->id, x->d_fs, x->cnt));
+  PHASE(PH_FLUX, launch_face_flux(s, x->P, x->id, x->d_fs, x->d_F, x->cnt));
+  return 3;
+}
+
 // Enqueue one Runge-Kutta stage.
 static int64_t enqueue_stage(m2cg_ctx* x, int stage, bool last, const StateSet& in, const StateSet& out) {
   cudaStream_t s = x->stream;
@@ -400,13 +433,13 @@ static int64_t enqueue_stage(m2cg_ctx* x, int stage, bool last, const StateSet& 
   PHASE_ON(PH_RIEMANN_B, x->stream2,
            launch_riemann_stragglers(x->stream2, P, x->d_mats, in, x->id, x->d_fs, x->L, stage == 0, x->scratch,
                                      x->path_cap, x->sblocks, x->sreserve, x->strag, x->strag_count, warm, x->cnt,
-                                     x->sc));
+                                     x->sc, x->strag_lanes));
   cudaEventRecord(x->ev_join, x->stream2);
   n += 2;
   cudaStreamWaitEvent(s, x->ev_a, 0);
   if (x->hold_cycles > 0) { launch_hold(s, x->hold_cycles); n++; }
-  if (!after_recon) { PHASE(PH_RECON, launch_reconstruct(s, P, in, x->id, x->d_fs, x->cnt)); n += 2; }
-  PHASE(PH_FLUX, launch_face_flux(s, P, x->id, x->d_fs, x->d_F, x->cnt)); n++;
+  if (!after_recon) n += enqueue_recon_flux(x, s, in);
+  else { PHASE(PH_FLUX, launch_face_flux(s, P, x->id, x->d_fs, x->d_F, x->cnt)); n++; }
   cudaStreamWaitEvent(s, x->ev_join, 0);
   StageArgs A = stage_args(x, stage, last, in, out);
   if (P.ls_fv) {   // the finite-volume level-set residual of the stage input
@@ -740,8 +773,7 @@ m2cg_status m2cg_compute_residual(m2cg_ctx* x, double* R) {
   cudaStream_t s = x->stream;
   CK(cudaMemsetAsync(x->L.count, 0, sizeof(unsigned long long), s));
   launch_compact(s, x->P, x->id, x->L, x->cnt, nullptr);
-  launch_reconstruct(s, x->P, x->S[0], x->id, x->d_fs, x->cnt);
-  launch_face_flux(s, x->P, x->id, x->d_fs, x->d_F, x->cnt);
+  x->launches += enqueue_recon_flux(x, s, x->S[0]) - 3;
   const float* warm = nullptr;
   if (x->mlp) {
     mlp_warm_faces(x->mlp, s, x->nsm, x->P, x->S[0], x->id, x->L, x->w_X, x->w_t, x->w_ref, x->w_p, nullptr);
@@ -751,7 +783,7 @@ m2cg_status m2cg_compute_residual(m2cg_ctx* x, double* R) {
   launch_riemann_interfaces(s, x->P, x->d_mats, x->S[0], x->id, x->d_fs, x->L, 1, x->scratch, x->path_cap, x->rblocks,
                             x->rthreads, x->eval_limit, x->strag, x->strag_count, warm, x->cnt, nullptr);
   launch_riemann_stragglers(s, x->P, x->d_mats, x->S[0], x->id, x->d_fs, x->L, 1, x->scratch, x->path_cap, x->sblocks,
-                            x->sreserve, x->strag, x->strag_count, warm, x->cnt, nullptr);
+                            x->sreserve, x->strag, x->strag_count, warm, x->cnt, nullptr, x->strag_lanes);
   StageArgs A;
   memset(&A, 0, sizeof(A));
   A.in = x->S[0];
@@ -1022,10 +1054,14 @@ m2cg_status m2cg_conserved_totals(m2cg_ctx* x, double totals[5]) {
   CK(cudaMemcpyAsync(h.data(), x->partial, h.size() * sizeof(double), cudaMemcpyDeviceToHost, x->stream));
   CK(cudaStreamSynchronize(x->stream));
   double vol = x->P.g.dx * x->P.g.dy * x->P.g.dz;
-  for (int p = 0; p < 5; p++) {
-    double t = 0.0;
-    for (int b = 0; b < nb; b++) t += h[(size_t)b * 5 + p];
-    totals[p] = t * vol;
+  for (int p = 0; p < 5; p++) {   // compensated (Neumaier) sum of the block partials
+    double t = 0.0, comp = 0.0;
+    for (int b = 0; b < nb; b++) {
+      const double v = h[(size_t)b * 5 + p], u = t + v;
+      comp += (std::fabs(t) >= std::fabs(v)) ? (t - u) + v : (v - u) + t;
+      t = u;
+    }
+    totals[p] = (t + comp) * vol;
   }
   return M2CG_OK;
 }
@@ -1238,7 +1274,7 @@ void launch_k_swept_update_ens(cudaStream_t, int64_t, const k_swept_update_args*
 void launch_k_commit_ids_ens(cudaStream_t, int64_t, const k_commit_ids_args*, const int64_t*, int);
 void launch_reset_counters_ens(cudaStream_t, const CounterResetArgs*, int);
 void launch_riemann_ens(cudaStream_t, const RiemannEnsArgs*, int, int64_t*, double*, int, int, int, int64_t*,
-                        unsigned long long*, int, size_t);
+                        unsigned long long*, int, size_t, int);
 cudaError_t riemann_stragglers_ens_reserve(size_t bytes);
 }  // namespace m2cg
 
@@ -1249,6 +1285,7 @@ struct m2cg_ensemble {
   cudaEvent_t e0 = nullptr, e1 = nullptr;
   double* scratch = nullptr;  // Riemann integration-path pool shared by the members
   int path_cap = 1024, rblocks = 0, sblocks = 0, eval_limit = 16;
+  int strag_lanes = 1;         // straggler faces per warp (see m2cg_ctx::strag_lanes)
   size_t sreserve = 0;
   int64_t* strag = nullptr;
   unsigned long long* strag_count = nullptr;
@@ -1368,7 +1405,7 @@ static m2cg_status ens_enqueue_step(m2cg_ensemble* e, int64_t* nl) {
     };
     if (after_recon) { m2cg_status st = recon(); if (st != M2CG_OK) return st; }
     if (!e->building) launch_riemann_ens(s, ra_d, D, e->off, e->scratch, e->path_cap, e->rblocks, e->eval_limit, e->strag,
-                       e->strag_count, e->sblocks, e->sreserve);
+                       e->strag_count, e->sblocks, e->sreserve, e->strag_lanes);
     n += 3;
     if (!after_recon) { m2cg_status st = recon(); if (st != M2CG_OK) return st; }
     { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_faces, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_face_flux_ens(s, nb_, ff_d, bo_, D); }
@@ -1475,6 +1512,7 @@ m2cg_status m2cg_ensemble_create(const m2cg_config* cfgs, int32_t n, m2cg_ensemb
   cudaDeviceGetAttribute(&e->nsm, cudaDevAttrMultiProcessorCount, dev);
   e->rblocks = e->nsm * 2;
   e->sblocks = e->nsm;
+  if (const char* v = getenv("M2CG_RIEMANN_STRAGGLER_LANES")) e->strag_lanes = std::min(32, std::max(1, atoi(v)));
   if (cudaStreamCreateWithFlags(&e->stream, cudaStreamNonBlocking) != cudaSuccess ||
       cudaEventCreate(&e->e0) != cudaSuccess || cudaEventCreate(&e->e1) != cudaSuccess ||
       cudaMalloc(&e->scratch, (size_t)6 * e->path_cap * e->rblocks * 128 * sizeof(double)) != cudaSuccess ||

@@ -433,12 +433,17 @@ M2CG_DEV double gen_minmod(double alpha, double dq0, double dq1) {
   return 0.0;
 }
 // van Albada with the sign / magnitude tests on the integer pipe and one
-// reciprocal (same value as van_albada to an ulp)
-M2CG_DEV double van_albada_fast(double dq0, double dq1) {
-  double pr = dq0 * dq1;
+// reciprocal (same value as van_albada to an ulp).  a = dq0^2 and b = dq1^2
+// come in precomputed (a difference shared by two neighbouring cells is squared
+// once); every operation is pinned (no contraction), so the split and fused
+// stage kernels produce the same bits.
+M2CG_DEV double van_albada_sq(double dq0, double dq1, double a, double b) {
+  double pr = __dmul_rn(dq0, dq1);
   if (le_zero_bits(pr) || abs_lt_bits(pr, 1e-16)) return 0.0;
-  double a = dq0 * dq0, b = dq1 * dq1;
-  return fma(dq1, a, dq0 * b) * rcp_fast(a + b);
+  return __dmul_rn(fma(dq1, a, __dmul_rn(dq0, b)), rcp_fast(__dadd_rn(a, b)));
+}
+M2CG_DEV double van_albada_fast(double dq0, double dq1) {
+  return van_albada_sq(dq0, dq1, __dmul_rn(dq0, dq0), __dmul_rn(dq1, dq1));
 }
 // k = 2 on a uniform mesh (Reconstructor.cpp:103-121 with A = B = 1)
 M2CG_DEV double van_albada(double dq0, double dq1) {

@@ -1,6 +1,7 @@
 // Internal definitions shared by the kernels and the host API of libm2cg.
 #pragma once
 #include <cstdint>
+#include <cuda.h>   // CUtensorMap (encoded through the runtime's driver entry point)
 #include <cuda_runtime.h>
 #include "m2cg_device.cuh"
 #include "m2cg_riemann.cuh"
@@ -52,7 +53,7 @@ M2CG_DEV bool ghost_face_cell(const Grid& g, int64_t t, int& side, int& i, int& 
 enum {
   CNT_IFACE = 0, CNT_RERR, CNT_RITER, CNT_RSOLVE, CNT_CLIPCELL, CNT_CLIPFACE, CNT_BAD, CNT_SWEPT, CNT_UNRES,
   CNT_IF_OVERFLOW, CNT_PATH_CAPPED, CNT_SWEPT_OVERFLOW, CNT_BADID, CNT_FALLBACK, CNT_UNRES_FIXED,
-  CNT_UNRES_OVERFLOW, CNT_UNRES_REPAIRS, CNT_N
+  CNT_UNRES_OVERFLOW, CNT_UNRES_REPAIRS, CNT_TILE_TIMEOUT, CNT_N
 };
 
 // Scalars that live on the device for the whole run (no host round trip per step).
@@ -215,5 +216,17 @@ struct StageArgs {
   const double* rls_pre;      // level-set residual computed beforehand (finite volume), else NULL
   int residual_only;
 };
+
+// Tensor maps of the five primitive arrays of one state set for the fused
+// reconstruction + flux kernel (m2cg_tile.cu): 3D (x, y, z) over the ghosted
+// arrays, box 36 x 7 x 1.
+struct TileMaps {
+  CUtensorMap v[5];
+};
+bool tile_supported(const Params& P);
+bool tile_maps(const Params& P, const StateSet& S, TileMaps* out);
+cudaError_t tile_prepare();
+void launch_recon_flux_tile(cudaStream_t s, const TileMaps& maps, const Params& P, const StateSet& S,
+                            const int32_t* id, double* const* F, unsigned long long* cnt, int zchunk);
 
 }  // namespace m2cg

@@ -214,6 +214,21 @@ __global__ void k_riemann_interfaces(Params P, const Mats* __restrict__ md, Stat
   iface_counts(cnt, acc);
 }
 
+// Warps the second pass spreads its n faces over: all W launched warps (one
+// face per warp) when lanes <= 1, else just enough warps to hold `lanes` faces
+// each.  Lanes of a warp that follow different faces take turns only where
+// their control flow differs; the stalled solves that reach this pass mostly
+// run the same secant loop, so packing several into one warp costs little
+// latency and frees the SMs the pass would otherwise hold.  Face k runs on
+// warp k mod W, lane k / W (k / W < 32 for every k < n).
+__device__ __forceinline__ int64_t straggler_warps(int64_t n, int64_t W, int lanes) {
+  if (lanes <= 1 || n <= 0) return W;
+  int64_t need = (n + lanes - 1) / lanes;
+  int64_t floor32 = (n + 31) / 32;   // never fewer warps than 32 lanes can hold
+  need = need < floor32 ? floor32 : need;
+  return need < W ? need : W;
+}
+
 // Second pass: the listed faces solved without a budget.  Each is one long
 // chain of dependent binary64 operations, so the faces are dealt round-robin
 // over the warps (lane-major), which puts as few as possible in one warp: lanes
@@ -230,11 +245,11 @@ __global__ void __launch_bounds__(128) k_riemann_stragglers(Params P, const Mats
                                                             IfaceList L, int store, double* scratch, int path_cap,
                                                             size_t reserve_bytes, const int32_t* __restrict__ strag,
                                                             const unsigned long long* strag_count, const float* warm,
-                                                            unsigned long long* cnt, const DevScalars* sc) {
+                                                            unsigned long long* cnt, const DevScalars* sc, int lanes) {
   extern __shared__ __align__(16) double s_path[];
   if (sc && !sc->active) return;
   int64_t n = (int64_t)min((unsigned long long)L.cap, *strag_count);
-  const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t W = straggler_warps(n, (int64_t)gridDim.x * (blockDim.x >> 5), lanes);
   const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int64_t lane = threadIdx.x & 31;
   int64_t T = (int64_t)gridDim.x * blockDim.x;
@@ -249,7 +264,8 @@ __global__ void __launch_bounds__(128) k_riemann_stragglers(Params P, const Mats
     rs.path3.stride = 1;
   }
   unsigned long long acc[6] = {0, 0, 0, 0, 0, 0};
-  for (int64_t k = lane * W + w; k < n; k += 32 * W) iface_solve(P, S, id, fs, L, store, warm, strag[k], rs, acc);
+  if (w < W)
+    for (int64_t k = lane * W + w; k < n; k += 32 * W) iface_solve(P, S, id, fs, L, store, warm, strag[k], rs, acc);
   iface_counts(cnt, acc);
 }
 
@@ -325,10 +341,10 @@ __global__ void k_riemann_interfaces_ens(const RiemannEnsArgs* __restrict__ a, i
 __global__ void __launch_bounds__(128) k_riemann_stragglers_ens(const RiemannEnsArgs* __restrict__ a, double* scratch,
                                                                 int path_cap, size_t reserve_bytes,
                                                                 const int64_t* __restrict__ strag,
-                                                                const unsigned long long* strag_count) {
+                                                                const unsigned long long* strag_count, int lanes) {
   extern __shared__ __align__(16) double s_path[];
   const int64_t n = (int64_t)*strag_count;
-  const int64_t W = (int64_t)gridDim.x * (blockDim.x >> 5);
+  const int64_t W = straggler_warps(n, (int64_t)gridDim.x * (blockDim.x >> 5), lanes);
   const int64_t w = (int64_t)blockIdx.x * (blockDim.x >> 5) + (threadIdx.x >> 5);
   const int64_t lane = threadIdx.x & 31;
   int64_t T = (int64_t)gridDim.x * blockDim.x;
@@ -343,7 +359,7 @@ __global__ void __launch_bounds__(128) k_riemann_stragglers_ens(const RiemannEns
     rs.path3.stride = 1;
   }
   unsigned long long acc[6] = {0, 0, 0, 0, 0, 0};
-  for (int64_t k = lane * W + w; k < n; k += 32 * W) {
+  for (int64_t k = lane * W + w; w < W && k < n; k += 32 * W) {
     int64_t v = strag[k];
     int d = (int)(v >> 40);
     int64_t s = v & ((1ll << 40) - 1);
@@ -357,10 +373,11 @@ __global__ void __launch_bounds__(128) k_riemann_stragglers_ens(const RiemannEns
 
 void launch_riemann_ens(cudaStream_t s, const RiemannEnsArgs* a, int D, int64_t* off, double* scratch, int path_cap,
                         int blocks, int eval_limit, int64_t* strag, unsigned long long* strag_count, int sblocks,
-                        size_t reserve_smem) {
+                        size_t reserve_smem, int lanes) {
   k_ens_iface_prefix<<<1, 1, 0, s>>>(a, D, off, strag_count);
   k_riemann_interfaces_ens<<<blocks, 128, 0, s>>>(a, D, off, scratch, path_cap, eval_limit, strag, strag_count);
-  k_riemann_stragglers_ens<<<sblocks, 128, reserve_smem, s>>>(a, scratch, path_cap, reserve_smem, strag, strag_count);
+  k_riemann_stragglers_ens<<<sblocks, 128, reserve_smem, s>>>(a, scratch, path_cap, reserve_smem, strag, strag_count,
+                                                              lanes);
 }
 cudaError_t riemann_stragglers_ens_reserve(size_t bytes) {
   return cudaFuncSetAttribute(k_riemann_stragglers_ens, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
@@ -463,9 +480,9 @@ void launch_riemann_stragglers(cudaStream_t s, const Params& P, const Mats* md, 
                                double* const* fs, const IfaceList& L, int store, double* scratch, int path_cap,
                                int blocks, size_t reserve_smem, const int32_t* strag,
                                const unsigned long long* strag_count, const float* warm, unsigned long long* cnt,
-                               const DevScalars* sc) {
+                               const DevScalars* sc, int lanes) {
   k_riemann_stragglers<<<blocks, 128, reserve_smem, s>>>(P, md, S, id, fs, L, store, scratch, path_cap, reserve_smem,
-                                                         strag, strag_count, warm, cnt, sc);
+                                                         strag, strag_count, warm, cnt, sc, lanes);
 }
 // One block that holds one SM for a fixed number of clock cycles (bounded
 // loop, waits on nothing).  Launched on the main stream between the first

@@ -13,9 +13,9 @@ _D = C.POINTER(C.c_double)
 _I = C.POINTER(C.c_int32)
 
 
-def _load_oracle():
+def _load_oracle(fma=False):
     from oracle import build as ob
-    lib = C.CDLL(ob.build())
+    lib = C.CDLL(ob.build(fma=fma))
     sig = {
         "orc_create": (_P, [C.POINTER(Config)]),
         "orc_destroy": (None, [_P]),
@@ -43,14 +43,16 @@ def _load_oracle():
     return lib
 
 
-_orc = None
+_orc = {}
 
 
-def lib():
-    global _orc
-    if _orc is None:
-        _orc = _load_oracle()
-    return _orc
+def lib(fma=False):
+    """The oracle library; fma=True: the same source compiled with fused
+    multiply-add contraction (the reference's rounding under a contracting
+    compiler)."""
+    if fma not in _orc:
+        _orc[fma] = _load_oracle(fma)
+    return _orc[fma]
 
 
 def ref_lib():
@@ -71,37 +73,38 @@ def ref_lib():
 class OracleSim:
     """The oracle's finite-volume state, mirroring the product context."""
 
-    def __init__(self, cfg):
+    def __init__(self, cfg, fma=False):
         self.cfg = cfg
         self.n = cfg.nx * cfg.ny * cfg.nz
-        self.h = lib().orc_create(C.byref(cfg))
+        self.L = lib(fma)
+        self.h = self.L.orc_create(C.byref(cfg))
 
     def __del__(self):
         if getattr(self, "h", None):
-            lib().orc_destroy(self.h)
+            self.L.orc_destroy(self.h)
             self.h = None
 
     def upload(self, V, ID, phi=None):
         V = np.ascontiguousarray(V, np.float64)
         ID = np.ascontiguousarray(ID, np.int32)
         phi = None if phi is None else np.ascontiguousarray(phi, np.float64)
-        lib().orc_upload(self.h, dptr(V), iptr(ID), dptr(phi))
+        self.L.orc_upload(self.h, dptr(V), iptr(ID), dptr(phi))
 
     def download(self):
         V = np.zeros((self.n, 5))
         ID = np.zeros(self.n, np.int32)
         phi = np.zeros(self.n)
-        lib().orc_download(self.h, dptr(V), iptr(ID), dptr(phi))
+        self.L.orc_download(self.h, dptr(V), iptr(ID), dptr(phi))
         return V, ID, phi
 
     def residual(self):
         R = np.zeros((self.n, 5))
-        lib().orc_residual(self.h, dptr(R))
+        self.L.orc_residual(self.h, dptr(R))
         return R
 
     def levelset_residual(self):
         R = np.zeros(self.n)
-        lib().orc_levelset_residual(self.h, dptr(R))
+        self.L.orc_levelset_residual(self.h, dptr(R))
         return R
 
     def integrate(self, box=None):
@@ -110,12 +113,12 @@ class OracleSim:
         ymax, zmin, zmax)."""
         out = np.zeros((self.cfg.n_materials, 6))
         b = None if box is None else np.ascontiguousarray(box, np.float64)
-        lib().orc_integrate(self.h, dptr(b), dptr(out))
+        self.L.orc_integrate(self.h, dptr(b), dptr(out))
         return out
 
     def riemann_normal(self, d, i, j, k, myid, nid):
         out = np.zeros(3)
-        lib().orc_riemann_normal(self.h, d, i, j, k, myid, nid, dptr(out))
+        self.L.orc_riemann_normal(self.h, d, i, j, k, myid, nid, dptr(out))
         return out
 
     def download_ghosted(self):
@@ -124,35 +127,35 @@ class OracleSim:
         V = np.zeros(5 * n)
         ID = np.zeros(n, np.int32)
         phi = np.zeros(n)
-        lib().orc_download_ghosted(self.h, dptr(V), iptr(ID), dptr(phi))
+        self.L.orc_download_ghosted(self.h, dptr(V), iptr(ID), dptr(phi))
         return V.reshape(5, n), ID, phi
 
     def reinitialize(self):
         """One full-domain reinitialization; returns (found_interface, stats dict)."""
         st = np.zeros(5)
-        r = lib().orc_reinitialize(self.h, dptr(st))
+        r = self.L.orc_reinitialize(self.h, dptr(st))
         return bool(r), dict(calls=int(st[0]), iterations=int(st[1]), retries=int(st[2]), failures=int(st[3]),
                              cfl=float(st[4]))
 
     def compute_dt(self):
         dt, cfl = C.c_double(), C.c_double()
-        lib().orc_compute_dt(self.h, C.byref(dt), C.byref(cfl))
+        self.L.orc_compute_dt(self.h, C.byref(dt), C.byref(cfl))
         return dt.value, cfl.value
 
     def advance(self, dt):
-        lib().orc_advance(self.h, dt)
+        self.L.orc_advance(self.h, dt)
 
     def run(self, nsteps):
-        return lib().orc_run(self.h, nsteps)
+        return self.L.orc_run(self.h, nsteps)
 
     def counters(self):
         c = Counters()
-        lib().orc_counters(self.h, C.byref(c))
+        self.L.orc_counters(self.h, C.byref(c))
         return c.as_dict()
 
     def conserved_totals(self):
         t = np.zeros(5)
-        lib().orc_conserved_totals(self.h, dptr(t))
+        self.L.orc_conserved_totals(self.h, dptr(t))
         return t
 
 
