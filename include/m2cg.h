@@ -310,11 +310,17 @@ m2cg_status m2cg_flux_batch(m2cg_ctx* ctx, int64_t n, const int32_t* dir,
  * pointer (materials and ExactRiemannSolution fields are read); stream is a
  * cudaStream_t (NULL: default stream).  path_cap is the integration-path cache
  * capacity per wave, 2..1024 (M2CG_ERR_CAPACITY beyond); m2cg_riemann_batch
- * uses 1024.  Solver concurrency is 32 MiB / (48 * path_cap) threads.  An
- * invalid material ID gives err = -2 for that problem.  Asynchronous on
- * `stream`.  All calls share the scratch array: calls that overlap on one GPU
- * race, so serialize them.  The first call on a device looks up the array's
- * address; make it before any stream capture. */
+ * uses 1024, and results equal m2cg_riemann_batch's bit for bit at 1024 (a
+ * smaller cache can cap a long rarefaction path; capped solves are not
+ * reported separately here).  Solver concurrency is 32 MiB / (48 * path_cap)
+ * threads: 682 threads (5 blocks of 128) at 1024, while path_cap <= 32 gives
+ * 21,845 threads, enough for every SM of a 152-SM GB300.  A row with an
+ * invalid material ID is not solved: id = -1, err = -2 (when err is given),
+ * iters = 0 and NaN in its Vs, Vsm and Vsp.  Asynchronous on `stream`.  All
+ * calls share the scratch array: calls that overlap on one GPU race, so
+ * serialize them.  The first call on a device looks up the array's address;
+ * make it before any stream capture.  After a device reset the next call looks
+ * the address up again in the new context. */
 m2cg_status m2cg_riemann_batch_noalloc(const m2cg_config* cfg, int64_t n,
                                        const double* Vm, const int32_t* idm,
                                        const double* Vp, const int32_t* idp, const double* dir,
@@ -353,6 +359,11 @@ m2cg_status m2cg_mlp_train(m2cg_mlp* mlp, int32_t epochs, int32_t batch, float l
 /* One forward + backward pass over X (n x 16) and targets t without an update:
  * gradient of the mean squared error (M2CG_MLP_PARAMS floats) and the loss. */
 m2cg_status m2cg_mlp_grad(m2cg_mlp* mlp, int64_t n, const float* X, const float* t, float* grad, float* loss);
+/* One Adam update of the parameters with the given gradient (M2CG_MLP_PARAMS
+ * floats, host), the moments and step count that m2cg_mlp_train keeps
+ * (beta1 0.9, beta2 0.999, eps 1e-8, bias-corrected; m2cg_mlp_set_params
+ * resets them), at learning rate lr. */
+m2cg_status m2cg_mlp_adam_step(m2cg_mlp* mlp, const float* grad, float lr);
 /* Network output t for features X (n x 16). */
 m2cg_status m2cg_mlp_forward(m2cg_mlp* mlp, int64_t n, const float* X, float* t);
 /* Predicted star pressures (0 where the prediction is not positive) for

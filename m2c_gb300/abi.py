@@ -224,6 +224,7 @@ def load(path=None):
         "m2cg_mlp_set_data": (C.c_int, [_P, C.c_int64, _D, _D, _D]),
         "m2cg_mlp_train": (C.c_int, [_P, C.c_int32, C.c_int32, C.c_float, C.c_uint64, _F, _F]),
         "m2cg_mlp_grad": (C.c_int, [_P, C.c_int64, _F, _F, _F, _F]),
+        "m2cg_mlp_adam_step": (C.c_int, [_P, _F, C.c_float]),
         "m2cg_mlp_forward": (C.c_int, [_P, C.c_int64, _F, _F]),
         "m2cg_mlp_predict": (C.c_int, [_P, C.c_int64, _D, _D, _D, _F]),
         "m2cg_set_warm_start": (C.c_int, [_P, _P]),

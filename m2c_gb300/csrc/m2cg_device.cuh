@@ -273,9 +273,15 @@ M2CG_DEV void side_eos(const DevMat& M, const double* V, int dir, Side& S) {
   S.sr = S.rho * y;
   S.inv_rho = y * y;
   if (M.type == M2CG_EOS_SG) {
+    // c^2 = dp/drho + p/rho Gamma = gamma (p + p_inf) / rho (VarFcnSG.h:64-68,
+    // VarFcnBase.h:219-223), the same value to rounding without the
+    // cancellation of the two terms near p = -p_inf
     S.e = (S.p + M.gamPs) * M.invgam1 * S.inv_rho;
     S.dpdrho = M.gam1 * S.e;
     S.Gamma = M.gam1;
+    S.c2 = M.gam * (S.p + M.Pstiff) * S.inv_rho;
+    S.c = (S.c2 > 0.0) ? S.c2 * rsqrt_fast(S.c2) : 0.0;
+    return;
   } else if (M.type == M2CG_EOS_NASG) {
     double vb = S.inv_rho - M.b;
     S.e = M.invgam1 * (S.p + M.gamPs) * vb + M.q;
@@ -323,30 +329,64 @@ M2CG_DEV bool flux_hllc_fast(const DevMat& M, int dir, const double* Vm, const d
   double dp = B.p - A.p;
   double diff = (B.vn - A.vn) * inv_s;
   double p_over_rho_hat = (A.sr * (A.p * A.inv_rho) + B.sr * (B.p * B.inv_rho)) * inv_s + 0.5 * diff * diff;
-  double de = B.e - A.e;
   double e_hat = (A.sr * A.e + B.sr * B.e) * inv_s;
-  double inv_e = rcp_fast(e_hat);
-  double w_rho = drho * drho * irr;
-  double de_e = de * inv_e;
-  double w_e = de_e * de_e;
-  double inv_den = rcp_fast(w_rho + w_e + eps);
-  double dpdrho_avg = (A.sr * A.dpdrho + B.sr * B.dpdrho) * inv_s;
-  double Gamma_avg = (A.sr * A.Gamma + B.sr * B.Gamma) * inv_s;
-  double dpdrho_hat = ((w_e + eps) * dpdrho_avg + (dp - Gamma_avg * rho_hat * de) * drho * irr) * inv_den;
-  double Gamma_hat = ((w_rho + eps) * Gamma_avg + (dp - dpdrho_avg * drho) * de_e * inv_e * (A.inv_rho * B.sr * B.inv_rho * A.sr)) * inv_den;
-  double c2_hat = dpdrho_hat + Gamma_hat * p_over_rho_hat;
+  double c2_hat;
+  if (M.type == M2CG_EOS_SG) {
+    // Stiffened gas: p is linear in rho e with the constant Gamma = gamma - 1,
+    // and the Roe-averaged jumps satisfy d(rho e) = rho_hat de + e_hat drho
+    // exactly, so the generalized averages of FluxFcnHLLC.h:99-119 reduce to
+    // Gamma_hat = gamma - 1 and dp/drho_hat = (gamma - 1) e_hat: the same value
+    // without the weights w_rho, w_e and two reciprocals (the reference's form
+    // carries its rounding through a cancellation when dp ~ Gamma rho_hat de).
+    c2_hat = M.gam1 * (e_hat + p_over_rho_hat);
+  } else {
+    double de = B.e - A.e;
+    double inv_e = rcp_fast(e_hat);
+    double w_rho = drho * drho * irr;
+    double de_e = de * inv_e;
+    double w_e = de_e * de_e;
+    double inv_den = rcp_fast(w_rho + w_e + eps);
+    double dpdrho_avg = (A.sr * A.dpdrho + B.sr * B.dpdrho) * inv_s;
+    double Gamma_avg = (A.sr * A.Gamma + B.sr * B.Gamma) * inv_s;
+    double dpdrho_hat = ((w_e + eps) * dpdrho_avg + (dp - Gamma_avg * rho_hat * de) * drho * irr) * inv_den;
+    double Gamma_hat = ((w_rho + eps) * Gamma_avg + (dp - dpdrho_avg * drho) * de_e * inv_e * (A.inv_rho * B.sr * B.inv_rho * A.sr)) * inv_den;
+    c2_hat = dpdrho_hat + Gamma_hat * p_over_rho_hat;
+  }
   double c_hat = (c2_hat <= 0.0) ? eps : c2_hat * rsqrt_fast(c2_hat);
   double vh = (A.sr * A.vn + B.sr * B.vn) * inv_s;
   double Sm = fmin(A.vn - A.c, vh - c_hat);
   double Sp = fmax(B.vn + B.c, vh + c_hat);
   bool ok = !(A.c2 < 0.0) && !(B.c2 < 0.0);
-  if (0.0 <= Sm) phys_flux_side(dir, Vm, A, F);
-  else if (0.0 >= Sp) phys_flux_side(dir, Vp, B, F);
-  else {
-    double am = A.rho * (Sm - A.vn), bp = B.rho * (Sp - B.vn);
-    double Sstar = (dp + am * A.vn - bp * B.vn) * rcp_fast(am - bp);
-    if (Sstar >= 0.0) hllc_fstar_side(dir, Vm, A, Sm, Sstar, F);
-    else hllc_fstar_side(dir, Vp, B, Sp, Sstar, F);
+  // FluxFcnHLLC.h:226-241: F_L, F_R, F*_L or F*_R.  The side is selected
+  // first and its flux evaluated once, so lanes of a warp whose faces pick
+  // different sides do not run both branches (the same operations as
+  // phys_flux_side / hllc_fstar_side on the chosen side).
+  const bool sup_l = 0.0 <= Sm, sup_r = 0.0 >= Sp;
+  const double am = A.rho * (Sm - A.vn), bp = B.rho * (Sp - B.vn);
+  const double Sstar = (dp + am * A.vn - bp * B.vn) * rcp_fast(am - bp);
+  const bool left = sup_l || (!sup_r && Sstar >= 0.0);
+  // value selects (no pointer to either side, which would put them in memory)
+  Side K;
+  K.rho = left ? A.rho : B.rho;
+  K.vn = left ? A.vn : B.vn;
+  K.p = left ? A.p : B.p;
+  K.inv_rho = left ? A.inv_rho : B.inv_rho;
+  K.e = left ? A.e : B.e;
+  double V[5];
+#pragma unroll
+  for (int i = 0; i < 5; i++) V[i] = left ? Vm[i] : Vp[i];
+  phys_flux_side(dir, V, K, F);
+  if (!sup_l && !sup_r) {
+    const double Sw = left ? Sm : Sp;
+    double t = Sw - K.vn;
+    double rhostar = K.rho * t * rcp_fast(Sw - Sstar);
+    double k2 = V[1] * V[1] + V[2] * V[2] + V[3] * V[3];
+    double Eo = K.e + 0.5 * k2;   // U[4] / rho
+    double U[5] = {K.rho, K.rho * V[1], K.rho * V[2], K.rho * V[3], K.rho * Eo};
+    double Us[5] = {1.0, V[1], V[2], V[3], Eo + (Sstar - K.vn) * (Sstar + K.p * K.inv_rho * rcp_fast(t))};
+    Us[1 + dir] = Sstar;
+#pragma unroll
+    for (int i = 0; i < 5; i++) F[i] = fma(Sw, fma(Us[i], rhostar, -U[i]), F[i]);
   }
   return ok;
 }

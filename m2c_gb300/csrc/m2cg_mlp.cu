@@ -611,6 +611,19 @@ m2cg_status m2cg_mlp_set_params(m2cg_mlp* m, const float* params) {
   return M2CG_OK;
 }
 
+m2cg_status m2cg_mlp_adam_step(m2cg_mlp* m, const float* grad, float lr) {
+  if (!m || !grad || !(lr > 0.f)) { m2cg_set_error("null argument or non-positive rate"); return M2CG_ERR_INVALID_ARG; }
+  const float b1 = 0.9f, b2 = 0.999f, eps = 1e-8f;   // as m2cg_mlp_train
+  MCK(cudaMemcpyAsync(m->grad, grad, NPARAM * sizeof(float), cudaMemcpyHostToDevice, m->stream));
+  m->step++;
+  const float bc1 = 1.f - std::pow(b1, (float)m->step), bc2 = 1.f - std::pow(b2, (float)m->step);
+  k_adam<<<(NPARAM + 255) / 256, 256, 0, m->stream>>>(m->prm, m->grad, m->adam_m, m->adam_v, lr, b1, b2, eps, bc1, bc2);
+  k_pack_bf16<<<(NH * NH + 255) / 256, 256, 0, m->stream>>>(m->prm, m->wbf);
+  MCK(cudaGetLastError());
+  MCK(cudaStreamSynchronize(m->stream));
+  return M2CG_OK;
+}
+
 m2cg_status m2cg_mlp_get_params(m2cg_mlp* m, float* params) {
   if (!m || !params) { m2cg_set_error("null argument"); return M2CG_ERR_INVALID_ARG; }
   MCK(cudaMemcpyAsync(params, m->prm, NPARAM * sizeof(float), cudaMemcpyDeviceToHost, m->stream));

@@ -17,7 +17,9 @@
 // writes every cache entry before it reads it).  Calls that overlap on one GPU,
 // for example on two streams, race on the array: serialize them.  The first
 // call on a device looks up the array's device address; make that first call
-// before any stream capture.
+// before any stream capture.  A device reset (cudaDeviceReset) ends the
+// context the address belongs to; the next call notices the new context and
+// looks the address up again.
 //
 // Compiled without floating-point contraction, like the other interface kernels,
 // so its results equal m2cg_riemann_batch's for the same path-cache capacity.
@@ -62,6 +64,8 @@ __global__ void __launch_bounds__(128) k_riemann_batch_noalloc(
       if (err) err[q] = -2;
       if (iters) iters[q] = 0;
       id[q] = -1;
+      const double nan = __longlong_as_double(0x7ff8000000000000ll);
+      for (int p = 0; p < 5; p++) { Vs[q * 5 + p] = nan; Vsm[q * 5 + p] = nan; Vsp[q * 5 + p] = nan; }
       continue;
     }
     int oid = 0;
@@ -78,6 +82,36 @@ using namespace m2cg;
 
 static std::mutex g_noalloc_mutex;
 static double* g_noalloc_ptr[M2CG_NOALLOC_MAX_DEVICES];
+// the context the cached address belongs to: a device reset destroys the
+// primary context, and the array's address must be looked up again in the new
+// one (context IDs are unique within a process, handles may be reused)
+static unsigned long long g_noalloc_ctx[M2CG_NOALLOC_MAX_DEVICES];
+
+typedef CUresult (*CtxGetCurrentFn)(CUcontext*);
+typedef CUresult (*CtxGetIdFn)(CUcontext, unsigned long long*);
+
+// ID of the calling thread's current context, or 0 when the driver cannot tell.
+static unsigned long long current_context_id() {
+  static CtxGetCurrentFn get_current = nullptr;
+  static CtxGetIdFn get_id = nullptr;
+  if (!get_current || !get_id) {
+    void* f = nullptr;
+    void* g = nullptr;
+    cudaDriverEntryPointQueryResult q1, q2;
+    if (cudaGetDriverEntryPointByVersion("cuCtxGetCurrent", &f, 4000, cudaEnableDefault, &q1) != cudaSuccess ||
+        cudaGetDriverEntryPointByVersion("cuCtxGetId", &g, 12000, cudaEnableDefault, &q2) != cudaSuccess ||
+        q1 != cudaDriverEntryPointSuccess || q2 != cudaDriverEntryPointSuccess || !f || !g) {
+      cudaGetLastError();
+      return 0;
+    }
+    get_current = (CtxGetCurrentFn)f;
+    get_id = (CtxGetIdFn)g;
+  }
+  CUcontext c = nullptr;
+  unsigned long long idv = 0;
+  if (get_current(&c) != CUDA_SUCCESS || !c || get_id(c, &idv) != CUDA_SUCCESS) return 0;
+  return idv;
+}
 
 extern "C" m2cg_status m2cg_riemann_batch_noalloc(const m2cg_config* cfg, int64_t n, const double* Vm,
                                                   const int32_t* idm, const double* Vp, const int32_t* idp,
@@ -104,12 +138,21 @@ extern "C" m2cg_status m2cg_riemann_batch_noalloc(const m2cg_config* cfg, int64_
     m2cg_set_error("cudaGetDevice failed or device index %d unsupported", dev);
     return M2CG_ERR_CUDA;
   }
+  // make the device's primary context current (created here if the process
+  // has not used the device yet), so that the lookup below runs in it
+  e = cudaSetDevice(dev);
+  if (e != cudaSuccess) {
+    m2cg_set_error("cudaSetDevice(%d) failed: %s", dev, cudaGetErrorString(e));
+    return M2CG_ERR_CUDA;
+  }
+  const unsigned long long ctx_id = current_context_id();
   double* scratch;
   {
-    // first call on this device: host code cannot use the array's name as a
-    // device address, so fetch the address once with the device current
+    // first call on this device (or in a new context after a device reset):
+    // host code cannot use the array's name as a device address, so fetch the
+    // address once with the device current
     std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_ptr[dev]) {
+    if (!g_noalloc_ptr[dev] || g_noalloc_ctx[dev] != ctx_id) {
       void* p = nullptr;
       e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
       if (e != cudaSuccess || !p) {
@@ -117,6 +160,7 @@ extern "C" m2cg_status m2cg_riemann_batch_noalloc(const m2cg_config* cfg, int64_
         return M2CG_ERR_CUDA;
       }
       g_noalloc_ptr[dev] = (double*)p;
+      g_noalloc_ctx[dev] = ctx_id;
     }
     scratch = g_noalloc_ptr[dev];
   }

@@ -32,7 +32,7 @@ namespace tile {
 constexpr int TX = 32, TY = 4;           // cells per plane of a tile (one thread each)
 constexpr int BX = 36, BY = 7;           // staged box: x from real i0-3, y from real j0-2
 constexpr int VSTRIDE = 256;             // doubles per staged array (box 252, padded to 2 KiB)
-constexpr int RING = 5;                  // planes k-2 .. k+1 in use, k+2 in flight
+constexpr int RING = 4;                  // planes k-1 .. k+1 in use, k+2 in flight (k0-2 .. k0+1 at the start)
 constexpr int PLANE = 5 * VSTRIDE;       // doubles per ring slot
 constexpr uint32_t PLANE_BYTES = 5u * BX * BY * sizeof(double);   // bytes one plane's copies deliver
 constexpr long long WAIT_POLLS = 1ll << 22;
@@ -88,7 +88,7 @@ struct SmemCells {
   // a cell: tile x index (i - i0 + 3), tile y index (j - j0 + 2), real k
   struct C { int x, y, k; };
   M2CG_DEV double q(int p, C c) const {
-    return ring[((c.k + 2) % tile::RING) * tile::PLANE + p * tile::VSTRIDE + c.y * tile::BX + c.x];
+    return ring[((c.k + 2) & (tile::RING - 1)) * tile::PLANE + p * tile::VSTRIDE + c.y * tile::BX + c.x];
   }
   M2CG_DEV int idv(C c) const { return id[g.at(c.x - 3 + i0, c.y - 2 + j0, c.k)]; }
   M2CG_DEV C nb(C c, int d, int s) const {
@@ -179,14 +179,90 @@ __device__ __forceinline__ void warp_count(unsigned long long* c, int v) {
 }
 
 // ---------------------------------------------------------------------------
+// Face states of one cell in direction d (Reconstructor.cpp:426-716): one
+// limited slope per variable gives the minus (vl / vb / vk) and plus (vr / vt /
+// vf) states; then the cell's revert chain (the first nonphysical state in the
+// order vl, vr, vb, vt, vk, vf reverts to the cell value; `done` carries the
+// chain across directions, Reconstructor.cpp:722-778) and
+// CheckReconstructedStates (SpaceOperator.cpp:2446-2484), counted as
+// k_reconstruct + store_faces count them.  The same arithmetic as k_reconstruct.
+__device__ __forceinline__ void cell_faces_dir(const Params& P, const DevMat& M, const SmemCells& a, SmemCells::C c,
+                                               int d, const double* q, int myid, double* vm, double* vp,
+                                               bool& done, int& nclip, int& nbad) {
+  if (P.rec_type == M2CG_REC_CONSTANT) {
+#pragma unroll
+    for (int p = 0; p < 5; p++) { vm[p] = q[p]; vp[p] = q[p]; }
+  } else {
+    const SmemCells::C cm = a.nb(c, d, -1), cp = a.nb(c, d, 1);
+    const bool zero = P.slope_zero && (a.idv(cm) != myid || a.idv(cp) != myid);
+#pragma unroll
+    for (int p = 0; p < 5; p++) {
+      const double dq0 = q[p] - a.q(p, cm);
+      const double dq1 = a.q(p, cp) - q[p];
+      double sl = slope(P, dq0, dq1, __dmul_rn(dq0, dq0), __dmul_rn(dq1, dq1));
+      if (zero) sl = 0.0;
+      vm[p] = fma(-0.5, sl, q[p]);
+      vp[p] = fma(0.5, sl, q[p]);
+    }
+    if (!done && eos_bad5_fast(M, vm)) {
+#pragma unroll
+      for (int p = 0; p < 5; p++) vm[p] = q[p];
+      done = true;
+    }
+    if (!done && eos_bad5_fast(M, vp)) {
+#pragma unroll
+      for (int p = 0; p < 5; p++) vp[p] = q[p];
+      done = true;
+    }
+  }
+  double t[5] = {vm[0], vm[1], vm[2], vm[3], vm[4]};
+  if (eos_clip_fast(M, t)) {
+#pragma unroll
+    for (int p = 0; p < 5; p++) vm[p] = q[p];
+    nclip++;
+  }
+  nbad += eos_bad5_fast(M, vm);
+#pragma unroll
+  for (int p = 0; p < 5; p++) t[p] = vp[p];
+  if (eos_clip_fast(M, t)) {
+#pragma unroll
+    for (int p = 0; p < 5; p++) vp[p] = q[p];
+    nclip++;
+  }
+  nbad += eos_bad5_fast(M, vp);
+}
+
+// One checked face state of a cell outside the tile's own cells (a halo cell,
+// or the cell below the chunk): raw state plus the checks of check_face, not
+// counted (its own tile counts it).
+__device__ __forceinline__ void halo_face(const Params& P, const SmemCells& a, SmemCells::C c, int f, double* V) {
+  const int hid = a.idv(c);
+  raw_face(P, a, c, f, hid, V);
+  int dc = 0, db = 0;
+  check_face(P, a, c, f, hid, V, dc, db);
+}
+
+// ---------------------------------------------------------------------------
 // Interior faces of the z-chunk [k0, k1) of one 32 x 4 column.  F[d*5+p][c]:
 // flux of the face at the minus side of cell c in direction d (same-material
 // faces only; interface faces come from the Riemann pass).
-__global__ void __launch_bounds__(128) k_recon_flux_tile(const __grid_constant__ TileMaps maps, Params P,
+//
+// Per plane: two warps first evaluate the states the tile's first column and
+// row need from the cells just outside it; then, direction by direction, every
+// thread reconstructs its own cell (one limited slope per variable, the
+// k_reconstruct arithmetic), hands the plus state to the neighbour that needs
+// it -- vr by a warp shuffle (x runs along the warp), vt through shared memory
+// (y runs across the warps), vf in registers until the next plane -- and
+// evaluates the flux of its minus face in that direction.  Holding one
+// direction's states at a time keeps the register count down.
+__global__ void __launch_bounds__(128, 4) k_recon_flux_tile(const __grid_constant__ TileMaps maps, Params P,
                                                         const int32_t* __restrict__ id, double* const* F,
                                                         unsigned long long* cnt, int zchunk) {
   extern __shared__ __align__(128) double ring_raw[];
   __shared__ __align__(8) uint64_t bars[tile::RING];
+  __shared__ double s_vt[tile::TY][5][tile::TX];      // vt of the tile's rows (read by the next row)
+  __shared__ double s_vt_halo[5][tile::TX];           // vt of row j0-1
+  __shared__ double s_vr_halo[5][tile::TY];           // vr of column i0-1
   // TMA destinations on 128-byte boundaries (the launch adds 128 bytes of slack)
   double* ring = ring_raw + ((128u - (s_addr(ring_raw) & 127u)) & 127u) / sizeof(double);
   const Grid& g = P.g;
@@ -195,11 +271,13 @@ __global__ void __launch_bounds__(128) k_recon_flux_tile(const __grid_constant__
   const int k0 = blockIdx.z * zchunk, k1 = min(g.nz, k0 + zchunk);
   const int i = i0 + tx, j = j0 + ty;
   const bool active = i < g.nx && j < g.ny;
-  // plane kk (real index, may be k0-2 .. k1) of the ring: slot (kk + 2) % RING,
-  // its n-th load into that slot completes phase n
+  // plane kk (real index, k0-2 .. k1) of the ring: slot (kk + 2) % RING; its
+  // n-th load into that slot completes phase n
+  static_assert((tile::RING & (tile::RING - 1)) == 0, "ring slots: a power of two");
+  auto slot = [](int kk) { return (kk + 2) & (tile::RING - 1); };
   auto issue = [&](int kk) {
-    double* dst = ring + ((kk + 2) % tile::RING) * tile::PLANE;
-    uint64_t* b = &bars[(kk + 2) % tile::RING];
+    double* dst = ring + slot(kk) * tile::PLANE;
+    uint64_t* b = &bars[slot(kk)];
     bar_expect(b, tile::PLANE_BYTES);
 #pragma unroll
     for (int p = 0; p < 5; p++) tma_box(dst + p * tile::VSTRIDE, &maps.v[p], b, i0 - 2, j0 - 1, kk + 1);
@@ -212,58 +290,107 @@ __global__ void __launch_bounds__(128) k_recon_flux_tile(const __grid_constant__
   __syncthreads();
   if (threadIdx.x == 0)
     for (int kk = k0 - 2; kk <= min(k0 + 1, k1); kk++) issue(kk);
-  SmemCells a{ring, id, g, i0, j0};
+  const SmemCells a{ring, id, g, i0, j0};
+  const int64_t sy = g.sy, sz = g.sz;
   int nclip = 0, nbad = 0;
+  double vf_prev[5];   // checked vf of the cell below (the minus state of the z face)
   bool ok = true;
   for (int k = k0; k < k1; k++) {
-    __syncthreads();   // every thread is done with plane k-3's slot
-    if (threadIdx.x == 0 && k + 2 <= k1) issue(k + 2);
+    __syncthreads();   // every thread is done with plane k-2's slot and with s_vt
+    if (threadIdx.x == 0 && k > k0 && k + 2 <= k1) issue(k + 2);
     bool w = true;
     if (k == k0)
-      for (int kk = k0 - 2; kk < k0 && w; kk++) w = bar_wait(&bars[(kk + 2) % tile::RING], parity(kk), tile::WAIT_POLLS);
-    w = w && bar_wait(&bars[(k + 2) % tile::RING], parity(k), tile::WAIT_POLLS);
-    w = w && bar_wait(&bars[(k + 3) % tile::RING], parity(k + 1), tile::WAIT_POLLS);
+      for (int kk = k0 - 2; kk < k0 && w; kk++) w = bar_wait(&bars[slot(kk)], parity(kk), tile::WAIT_POLLS);
+    w = w && bar_wait(&bars[slot(k)], parity(k), tile::WAIT_POLLS);
+    w = w && bar_wait(&bars[slot(k + 1)], parity(k + 1), tile::WAIT_POLLS);
     ok = __syncthreads_and(w);   // one decision for the whole CTA
     if (!ok) break;
-    if (!active) continue;
-    const int64_t c = g.at(i, j, k);
-    const int myid = id[c];
-    const int pos[3] = {i, j, k};
-    const int64_t st[3] = {1, g.sy, g.sz};
     const SmemCells::C cc{tx + 3, ty + 2, k};
+    if (k == k0) {
+      // the first plane of the chunk: vf of the cell below, the one use of plane
+      // k0-2, whose slot then takes plane k0+2
+      if (k > 0 && active) halo_face(P, a, a.nb(cc, 2, -1), 5, vf_prev);
+      __syncthreads();
+      if (threadIdx.x == 0 && k + 2 <= k1) issue(k + 2);
+    }
+    // states from the cells just outside the tile: vt of row j0-1 (warp 3),
+    // vr of column i0-1 (warp 2, one lane per row)
+    if (ty == 3 && j0 > 0 && i < g.nx) {
+      double V[5];
+      halo_face(P, a, SmemCells::C{tx + 3, 1, k}, 3, V);
+#pragma unroll
+      for (int p = 0; p < 5; p++) s_vt_halo[p][tx] = V[p];
+    }
+    if (ty == 2 && tx < tile::TY && i0 > 0 && j0 + tx < g.ny) {
+      double V[5];
+      halo_face(P, a, SmemCells::C{2, tx + 2, k}, 1, V);
+#pragma unroll
+      for (int p = 0; p < 5; p++) s_vr_halo[p][tx] = V[p];
+    }
+    int myid = 0;
+    double q[5] = {0, 0, 0, 0, 0};
+    if (active) {
+      myid = id[g.at(i, j, k)];
+#pragma unroll
+      for (int p = 0; p < 5; p++) q[p] = a.q(p, cc);
+    }
+    const DevMat& M = P.mats.m[myid];
+    const int64_t c = g.at(i, j, k);
+    bool done = false;   // the cell's revert chain, carried across directions
     int bad = 0;
+    // x: own vl, vr; vr of the left neighbour by shuffle (lane 0: the halo)
+    {
+      double vl[5], vr[5] = {0, 0, 0, 0, 0};
+      if (active) cell_faces_dir(P, M, a, cc, 0, q, myid, vl, vr, done, nclip, nbad);
+      double vrl[5];
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-      if (pos[d] == 0) continue;   // boundary face: k_boundary_faces
-      const int idm = id[c - st[d]];
-      const SmemCells::C cm = a.nb(cc, d, -1);
-      double Vm[5], Vp[5];
-      if (P.rec_type == M2CG_REC_CONSTANT) {
+      for (int p = 0; p < 5; p++) vrl[p] = __shfl_up_sync(0xffffffffu, vr[p], 1);
+      __syncthreads();   // the halo states are written
+      if (active && i > 0) {
+        if (tx == 0)
 #pragma unroll
-        for (int p = 0; p < 5; p++) { Vm[p] = a.q(p, cm); Vp[p] = a.q(p, cc); }
-      } else {
-        const SmemCells::C cmm = a.nb(cm, d, -1), cp = a.nb(cc, d, 1);
-        const bool zm = P.slope_zero && (a.idv(cmm) != idm || myid != idm);
-        const bool zp = P.slope_zero && (idm != myid || a.idv(cp) != myid);
+          for (int p = 0; p < 5; p++) vrl[p] = s_vr_halo[p][ty];
+        if (id[c - 1] == myid) {
+          double Fl[5];
+          bad += !tile_flux(P, 0, vrl, vl, myid, Fl);
 #pragma unroll
-        for (int p = 0; p < 5; p++) {
-          const double q0 = a.q(p, cmm), q1 = a.q(p, cm), q2 = a.q(p, cc), q3 = a.q(p, cp);
-          const double d0 = q1 - q0, d1 = q2 - q1, d2 = q3 - q2;
-          const double s0 = __dmul_rn(d0, d0), s1 = __dmul_rn(d1, d1), s2 = __dmul_rn(d2, d2);
-          double sm = slope(P, d0, d1, s0, s1), sp = slope(P, d1, d2, s1, s2);
-          if (zm) sm = 0.0;
-          if (zp) sp = 0.0;
-          Vm[p] = fma(0.5, sm, q1);
-          Vp[p] = fma(-0.5, sp, q2);
+          for (int p = 0; p < 5; p++) F[p][c] = Fl[p];
         }
       }
-      check_face(P, a, cm, 2 * d + 1, idm, Vm, nclip, nbad);
-      check_face(P, a, cc, 2 * d, myid, Vp, nclip, nbad);
-      if (idm != myid) continue;   // material interface: the Riemann pass
-      double Fl[5];
-      bad += !tile_flux(P, d, Vm, Vp, myid, Fl);
+    }
+    // y: own vb, vt; vt of the row below from shared memory (row 0: the halo)
+    {
+      double vb[5], vt[5];
+      if (active) {
+        cell_faces_dir(P, M, a, cc, 1, q, myid, vb, vt, done, nclip, nbad);
 #pragma unroll
-      for (int p = 0; p < 5; p++) F[d * 5 + p][c] = Fl[p];
+        for (int p = 0; p < 5; p++) s_vt[ty][p][tx] = vt[p];
+      }
+      __syncthreads();   // every row's vt is written
+      if (active && j > 0) {
+        double vtm[5];
+#pragma unroll
+        for (int p = 0; p < 5; p++) vtm[p] = ty > 0 ? s_vt[ty - 1][p][tx] : s_vt_halo[p][tx];
+        if (id[c - sy] == myid) {
+          double Fl[5];
+          bad += !tile_flux(P, 1, vtm, vb, myid, Fl);
+#pragma unroll
+          for (int p = 0; p < 5; p++) F[5 + p][c] = Fl[p];
+        }
+      }
+    }
+    // z: own vk, vf; vf of the cell below kept from the previous plane
+    if (active) {
+      double vk[5], vf[5];
+      cell_faces_dir(P, M, a, cc, 2, q, myid, vk, vf, done, nclip, nbad);
+      if (k > 0 && id[c - sz] == myid) {
+        double Fl[5];
+        bad += !tile_flux(P, 2, vf_prev, vk, myid, Fl);
+#pragma unroll
+        for (int p = 0; p < 5; p++) F[10 + p][c] = Fl[p];
+      }
+#pragma unroll
+      for (int p = 0; p < 5; p++) vf_prev[p] = vf[p];
     }
     nbad += bad;
   }
@@ -283,7 +410,8 @@ __global__ void __launch_bounds__(128) k_recon_flux_tile(const __grid_constant__
 
 // ---------------------------------------------------------------------------
 // The faces on the domain boundary (one thread each, six sides): the real
-// cell's face state on the boundary side with its checks, the ghost's face
+// cell's face state on the boundary side with its checks (counted by the
+// tile kernel, which evaluates all six states of every cell), the ghost's face
 // state by boundary condition (Reconstructor.cpp:807-889) with the boundary
 // branch of CheckReconstructedStates (SpaceOperator.cpp:2486-2535), then the
 // flux, stored at the face's plus cell like every other face (the ghost on
@@ -299,11 +427,15 @@ __global__ void k_boundary_faces(Params P, StateSet S, const int32_t* __restrict
   GlobalCells a{&S, id, g};
   const int rid = id[r], gid = id[gc];
   int nclip = 0, nbad = 0;
-  // the real cell's state on this side: vl/vb/vk (lower) or vr/vt/vf (upper)
+  // the real cell's state on this side: vl/vb/vk (lower) or vr/vt/vf (upper),
+  // counted where the tile kernel evaluates the cell's six states
   const int f = 2 * d + (upper ? 1 : 0);
   double Vr[5];
   raw_face(P, a, r, f, rid, Vr);
-  check_face(P, a, r, f, rid, Vr, nclip, nbad);
+  {
+    int dc = 0, db = 0;
+    check_face(P, a, r, f, rid, Vr, dc, db);
+  }
   // the ghost's state facing the domain
   double t[5];
   const int bc = P.bc[side];

@@ -436,6 +436,11 @@ class Case:
         self._initial_state(ic, inlet)
         out = t.get("Output", {})
         for k, d in sorted(out.get("LinePlot", {}).items()):
+            if int(d.get("NumberOfPoints", 0)) == 1:
+                # the reference spaces the points (x1 - x0) / (N - 1) apart
+                # (ProbeOutput.cpp:335-337): one point has no defined position
+                raise ValueError("Output.LinePlot[%s].NumberOfPoints = 1: a line plot needs 0 (off) or at "
+                                 "least 2 points" % k)
             self.line_plots.append({"index": k, "FileName": d.get("FileName", ""),
                                     "NumberOfPoints": int(d.get("NumberOfPoints", 0)),
                                     "frequency": int(d.get("Frequency", -100)),

@@ -172,6 +172,12 @@ class WarmStartMLP:
                                                    C.byref(loss)), "m2cg_mlp_grad")
         return g, loss.value
 
+    def adam_step(self, grad, lr):
+        """One Adam update with the given gradient (the training loop's update)."""
+        g = np.ascontiguousarray(grad, np.float32)
+        assert g.shape == (abi.MLP_PARAMS,)
+        abi.check(self.lib, self.lib.m2cg_mlp_adam_step(self.h, abi.fptr(g), float(lr)), "m2cg_mlp_adam_step")
+
     def forward(self, X):
         X = np.ascontiguousarray(X, np.float32)
         t = np.zeros(len(X), np.float32)

@@ -1,7 +1,7 @@
 """Compile the reference's own EOS, flux and exact-Riemann sources into
 oracle/_ref/libm2cref.so (test infrastructure only).
 
-Only this container has the reference tree; the GPU machine skips this step.
+Where the reference tree is absent (the GPU machine) this step is skipped.
 Sources compiled straight from the reference tree with g++: IoData.cpp,
 parser/AssignerCore.C, parser/Dictionary.C, ExactRiemannSolverBase.cpp (with
 -DWITHOUT_BOOST, the reference's own Boost-free Hugoniot root finder) plus the
@@ -15,7 +15,9 @@ import subprocess
 import sys
 
 HERE = os.path.dirname(os.path.abspath(__file__))
-REF = os.environ.get("M2C_REFERENCE_DIR", "/root/reference")
+# The reference checkout: $M2C_REFERENCE_DIR, else a directory named
+# "reference" beside this repository's root.
+REF = os.environ.get("M2C_REFERENCE_DIR") or os.path.normpath(os.path.join(HERE, "..", "..", "reference"))
 OUT = os.path.join(HERE, "_ref")
 SHIM = os.path.join(HERE, "ref_shim")
 FLAGS = ["-std=c++17", "-O2", "-fPIC", "-ffp-contract=off", "-DWITHOUT_BOOST", "-include", "cfloat",

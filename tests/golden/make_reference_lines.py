@@ -9,7 +9,7 @@ by the reference (ProbeOutput.cpp:483-597): time, time step and the columns
 density, velocity x, pressure, material ID and level set at the line's points.
 Writes reference_lines.json beside this script.
 
-Usage: python tests/golden/make_reference_lines.py [reference_dir]
+Usage: python tests/golden/make_reference_lines.py <reference_dir>   (or M2C_REFERENCE_DIR)
 """
 import json
 import os
@@ -20,7 +20,9 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, os.path.join(HERE, "..", ".."))
 from m2c_gb300.inputfile import parse  # noqa: E402
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("M2C_REFERENCE_DIR")
+if not REF:
+    sys.exit("usage: %s <reference_dir> (or set M2C_REFERENCE_DIR)" % sys.argv[0])
 
 
 def main():

@@ -8,14 +8,16 @@ parameters, and the star states (rho*_L, rho*_R, u*, p*) read at the contact
 (the row with xi = u*, and the row before it at xi = u* - max(1e-6, 1e-3|u*|),
 ExactRiemannSolverBase.cpp:366-368).  Test7 (JWL equation of state) is skipped.
 
-Usage: python tests/golden/make_riemann_golden.py [reference_dir]
+Usage: python tests/golden/make_riemann_golden.py <reference_dir>   (or M2C_REFERENCE_DIR)
 """
 import json
 import os
 import re
 import sys
 
-REF = sys.argv[1] if len(sys.argv) > 1 else "/root/reference"
+REF = sys.argv[1] if len(sys.argv) > 1 else os.environ.get("M2C_REFERENCE_DIR")
+if not REF:
+    sys.exit("usage: %s <reference_dir> (or set M2C_REFERENCE_DIR)" % sys.argv[0])
 HERE = os.path.dirname(os.path.abspath(__file__))
 # IoData defaults (IoData.cpp:708-722 for Mie-Gruneisen)
 MG_DEFAULT = dict(rho0=8.96e-3, c0=3.933e6, Gamma0=1.99, s=1.5, e0=0.0)

@@ -112,6 +112,14 @@ def test_case_configuration_and_initial_state():
     assert len(cs.line_plots) == 1 and cs.line_plots[0]["NumberOfPoints"] == 5
 
 
+def test_single_point_line_plot_is_refused():
+    text = ("under Mesh { NumberOfCellsX = 4; NumberOfCellsY = 1; NumberOfCellsZ = 1; }\n"
+            "under Equations { under Material[0] { EquationOfState = StiffenedGas; } }\n"
+            "under Output { under LinePlot[0] { FileName = \"line\"; NumberOfPoints = 1; } }\n")
+    with pytest.raises(ValueError, match="NumberOfPoints = 1"):
+        inf.Case.from_text(text)
+
+
 def test_unsupported_keys_are_refused():
     for bad in ("under Space { under LevelSet[0] { Bandwidth = 6; } }",
                 "under Equations { under Material[0] { EquationOfState = JonesWilkinsLee; } }",

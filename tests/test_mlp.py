@@ -169,6 +169,31 @@ def test_forward_and_gradients_match_reference():
 
 
 @gpu
+def test_adam_step_matches_numpy():
+    # two updates: moments, bias corrections (1 - beta^t) and the parameter step
+    rng = np.random.default_rng(29)
+    net = ws.WarmStartMLP(5)
+    p = rng.normal(0, 0.2, abi.MLP_PARAMS).astype(np.float32)
+    net.params = p
+    b1, b2, eps, lr = np.float32(0.9), np.float32(0.999), np.float32(1e-8), np.float32(3e-3)
+    m = np.zeros_like(p)
+    v = np.zeros_like(p)
+    for t in (1, 2):
+        g = rng.normal(0, 1, abi.MLP_PARAMS).astype(np.float32) * np.float32(10.0) ** rng.uniform(-6, 1, abi.MLP_PARAMS).astype(np.float32)
+        net.adam_step(g, lr)
+        m = b1 * m + (np.float32(1) - b1) * g
+        v = b2 * v + (np.float32(1) - b2) * g * g
+        bc1 = np.float32(1) - b1 ** np.float32(t)
+        bc2 = np.float32(1) - b2 ** np.float32(t)
+        step = lr * (m / bc1) / (np.sqrt(v / bc2) + eps)
+        p = p - step
+        got = net.params
+        # float32 arithmetic on both sides; the device contracts to FMA
+        assert np.all(np.abs(got - p) <= 1e-5 * np.abs(step) + 2e-7 * np.abs(p)), t
+    net.close()
+
+
+@gpu
 def test_training_and_warm_start():
     """The trained network predicts the star pressure better than the acoustic
     estimate the reference starts from on the problems with a strong acoustic

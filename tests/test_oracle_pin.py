@@ -136,3 +136,68 @@ def test_oracle_equals_reference_build_fluxes(ref, flux):
     _make_physical(cfg, Vp, ids, rng)
     dirs = rng.integers(0, 3, n).astype(np.int32)
     np.testing.assert_array_equal(ob.flux_batch(cfg, dirs, Vm, Vp, ids), ob.ref_flux_batch(ref, cfg, dirs, Vm, Vp, ids))
+
+
+def _assert_same_solutions(o, r):
+    np.testing.assert_array_equal(o["err"], r["err"])
+    np.testing.assert_array_equal(o["id"], r["id"])
+    for k in ("Vsm", "Vsp", "Vs"):
+        np.testing.assert_array_equal(o[k], r[k])
+
+
+def test_oracle_equals_reference_build_on_tilted_directions(ref):
+    # the LevelSet and Average interface normals (SpaceOperator.cpp:2186-2415)
+    # hand the solver directions off the mesh axes: random unit vectors here
+    rng = np.random.default_rng(17)
+    for trial in range(3):
+        cfg = _random_two_material_cfg(rng)
+        n = 200
+        Vm = random_sg_states(rng, n)
+        Vp = random_sg_states(rng, n)
+        idm = rng.integers(0, 3, n).astype(np.int32)
+        idp = rng.integers(0, 3, n).astype(np.int32)
+        _make_physical(cfg, Vm, idm, rng)
+        _make_physical(cfg, Vp, idp, rng)
+        dirs = rng.normal(size=(n, 3))
+        dirs /= np.linalg.norm(dirs, axis=1, keepdims=True)
+        _assert_same_solutions(ob.riemann_batch(cfg, Vm, idm, Vp, idp, dirs),
+                               ob.ref_riemann_batch(ref, cfg, Vm, idm, Vp, idp, dirs))
+
+
+def test_oracle_equals_reference_build_on_shock_bubble_interface_problems(ref):
+    # every interface problem of a 24^3 shock-bubble after two RK3 steps with
+    # level-set normals: mostly near-trivial gas/water states (equal
+    # pressures, velocities differing in the last bits) along tilted normals,
+    # many of which stall and go through the non-adaptive retry
+    from m2c_gb300 import problems
+    cfg, V, ID, phi = problems.shock_bubble(n=24)
+    cfg.ts_type = abi.TS_RK3
+    cfg.mp_riemann_normal = abi.RNORMAL_LEVEL_SET
+    o = ob.OracleSim(cfg)
+    o.upload(V, ID, phi)
+    o.run(2)
+    V, ID, _ = o.download()
+    n = cfg.nx
+    I3 = ID.reshape(n, n, n)
+    rows = []
+    for d, st in enumerate((1, n, n * n)):
+        for k in range(n):
+            for j in range(n):
+                for i in range(n):
+                    pos = (i, j, k)
+                    if pos[d] == 0:
+                        continue
+                    c = (k * n + j) * n + i
+                    m = c - st
+                    if ID[m] != ID[c]:
+                        rows.append((d, i, j, k, c, m))
+    assert len(rows) > 200
+    Vm = np.array([V[m] for *_, m in rows])
+    Vp = np.array([V[c] for *_, c, m in rows])
+    idm = np.array([ID[m] for *_, m in rows], np.int32)
+    idp = np.array([ID[c] for *_, c, m in rows], np.int32)
+    dirs = np.array([o.riemann_normal(d, i, j, k, ID[c], ID[m]) for d, i, j, k, c, m in rows])
+    assert (np.abs(dirs).max(1) < 1.0 - 1e-6).mean() > 0.5   # mostly off the mesh axes
+    res = ob.riemann_batch(cfg, Vm, idm, Vp, idp, dirs)
+    assert (res["err"] != 0).sum() > 0   # stalled solves included
+    _assert_same_solutions(res, ob.ref_riemann_batch(ref, cfg, Vm, idm, Vp, idp, dirs))

@@ -88,3 +88,23 @@ def test_noalloc_golden_cases_and_limits():
     with pytest.raises(RuntimeError, match="CAPACITY"):
         _noalloc(lib, cfg, z + 1, np.zeros(1, np.int32), z + 1, np.zeros(1, np.int32), np.array([[1.0, 0, 0]]),
                  path_cap=4096)
+
+
+def test_noalloc_invalid_material_rows_are_marked():
+    # a row whose material ID is outside the configuration is not solved: id -1,
+    # err -2 and NaN star states, while the other rows match the allocating path
+    cfg, Vm, idm, Vp, idp, dirs = _problems()
+    n = 64
+    Vm, idm, Vp, idp, dirs = Vm[:n], idm[:n].copy(), Vp[:n], idp[:n].copy(), dirs[:n]
+    idm[5] = 7
+    idp[9] = -1
+    lib = abi.load()
+    got = _noalloc(lib, cfg, Vm, idm, Vp, idp, dirs)
+    for r in (5, 9):
+        assert got["err"][r] == -2 and got["id"][r] == -1 and got["iters"][r] == 0
+        for k in ("Vs", "Vsm", "Vsp"):
+            assert np.isnan(got[k][r]).all()
+    good = np.ones(n, bool)
+    good[[5, 9]] = False
+    ref = Solver(cfg).riemann_batch(Vm[good], idm[good], Vp[good], idp[good], dirs[good])
+    _compare({k: v[good] for k, v in got.items()}, ref)
