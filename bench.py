@@ -51,9 +51,20 @@ FP64_PROFILE = {
     "face_flux": {"fp64_pipe_inst_per_cell": 617.5, "fp64_flop_per_cell": 706.8, "dram_bytes_per_cell": 363.0},
     "update": {"fp64_pipe_inst_per_cell": 104.5, "fp64_flop_per_cell": 122.6, "dram_bytes_per_cell": 293.9},
 }
+# The fused reconstruction + face-flux kernel (k_recon_flux_tile, the default
+# path) and the stage update: FP64-pipe slots, binary64 FLOPs (2 DFMA + DMUL +
+# DADD, thread level) and DRAM bytes per cell and launch, ncu on the 128^3 case
+# (profiles/k_recon_flux_tile_shock_bubble_128.txt; mean of the two stages).
+FP64_PROFILE_FUSED = {
+    "face_flux": {"fp64_pipe_inst_per_cell": 610.7, "fp64_flop_per_cell": 645.7, "dram_bytes_per_cell": 150.8},
+    "update": {"fp64_pipe_inst_per_cell": 104.0, "fp64_flop_per_cell": 117.5, "dram_bytes_per_cell": 295.3},
+}
 # DRAM bytes of one whole step graph of the 128^3 case (read + write, ncu
-# --graph-profiling graph, profiles/reinit_graph_shock_bubble_128.txt) per cell-stage.
+# --graph-profiling graph) per cell-stage: split kernels
+# (profiles/reinit_graph_shock_bubble_128.txt) and fused
+# (profiles/step_graph_shock_bubble_128.txt).
 STEP_DRAM_BYTES_PER_CELL_STAGE = (2388.8e6 + 1971.9e6) / (128 ** 3 * 2)
+STEP_DRAM_BYTES_PER_CELL_STAGE_FUSED = None
 # Algorithmic bytes per cell-stage of the fused ideal (binary64 V and phi, int32
 # ID, ideal halo reuse): a first stage reads W = (V, phi) 48 B + ID 4 B and
 # writes 48 B = 100 B; a later stage also reads W^n = 148 B.  Mean over the
@@ -82,11 +93,14 @@ def parse():
     ap.add_argument("--ws-train", type=int, default=1 << 20)
     ap.add_argument("--ws-test", type=int, default=1 << 17)
     ap.add_argument("--ws-epochs", type=int, default=60)
-    # batched ensemble of uneven bubble-collapse domains (0 disables it)
-    ap.add_argument("--ens-domains", type=int, default=64)
-    ap.add_argument("--ens-steps", type=int, default=10)
-    # large production-shaped run (8 gas bubbles in NASG water, 5e8 Pa shock, RK3): off by default
-    ap.add_argument("--large", type=int, default=0, help="cells per axis of the large run (e.g. 512)")
+    # batched ensemble of uneven bubble-collapse domains (0 disables it): batched
+    # steps, and steps of the per-domain-launch baseline
+    ap.add_argument("--ens-domains", type=int, default=512)
+    ap.add_argument("--ens-steps", type=int, default=100)
+    ap.add_argument("--ens-seq-steps", type=int, default=10)
+    # large production-shaped run (8 gas bubbles in NASG water, 5e8 Pa shock, RK3,
+    # reinitialization every 10 steps; 0 disables it)
+    ap.add_argument("--large", type=int, default=512, help="cells per axis of the large run")
     ap.add_argument("--large-steps", type=int, default=10)
     return ap.parse_args()
 
@@ -287,12 +301,14 @@ def run_reference(args):
     return 0
 
 
-def ensemble_bench(n_domains, steps):
+def ensemble_bench(n_domains, steps, seq_steps):
     """Batched ensemble (edges per axis from {32,48,64,96,128}, bubble radius
     [0.1,0.3] of the box, water 1e6..1e8 Pa, gas 1e4 Pa, RK2): the same steps
     from the same initial states, batched (one launch per kernel and stage for
-    all members, device-timed) and with per-domain launches one member after
-    another (wall-timed, each member's own CUDA graph)."""
+    all members, persistent cell and face kernels; device-timed) and with
+    per-domain launches one member after another (wall-timed, each member's own
+    CUDA graph).  Before timing, the interface-solve budget and the block shape
+    per size class are tuned on real steps."""
     from m2c_gb300 import problems
     from m2c_gb300.ensemble import Ensemble
     from m2c_gb300.solver import FluidState
@@ -301,32 +317,36 @@ def ensemble_bench(n_domains, steps):
     ens = Ensemble([d[0] for d in doms])
     out = {"workload": f"{n_domains} bubble-collapse domains, edges per axis from {{32,48,64,96,128}}, "
                        f"SG gas / SG water, MUSCL-van Albada, HLLC, exact interface Riemann @1e-10, RK2, CFL 0.4",
-           "domains": n_domains, "cells": cells, "steps": steps}
+           "domains": n_domains, "cells": cells}
     def reset():
         for i, (c, V, ID, phi) in enumerate(doms):
             ens.member(i).set_state(FluidState(V, ID, phi))
 
-    # the batched step's interface-solve budget, tuned on real steps first
     reset()
-    budget, tuned_ms = ens.autotune(steps=2)
-    out["autotune"] = {"first_pass_eval_budget": budget, "ms_per_step": tuned_ms,
-                       "candidates": [4, 8, 16, 32, 64, 1 << 20]}
-    for mode in ("batched", "sequential"):
+    t0 = time.perf_counter()
+    budget, tuned_ms = ens.autotune(steps=1, budgets=(4, 8, 16, 64))
+    shapes = ((0, 0, 0), (32, 4, 1), (16, 8, 1), (16, 4, 2))
+    chosen, tile_ms = ens.autotune_tiles(steps=1, shapes=shapes)
+    out["autotune"] = {"first_pass_eval_budget": budget, "budget_ms_per_step": tuned_ms,
+                       "budget_candidates": [4, 8, 16, 64],
+                       "block_shape_by_nx": {str(k): list(v) for k, v in sorted(chosen.items())},
+                       "shape_candidates": [list(x) for x in shapes], "tuning_s": time.perf_counter() - t0}
+    for mode, n in (("batched", steps), ("sequential", seq_steps)):
         run = ens.run if mode == "batched" else ens.run_sequential
         reset()
         run(1)  # graph capture
         reset()
         l0 = ens.kernel_launches()
-        ms = run(steps)
-        out[mode] = {"ms": ms, "value": cells * 2 * steps / (ms * 1e-3), "unit": UNIT}
+        ms = run(n)
+        out[mode] = {"steps": n, "ms": ms, "ms_per_step": ms / n, "value": cells * 2 * n / (ms * 1e-3), "unit": UNIT}
         if mode == "batched":
-            out[mode]["gpu_launches_per_step"] = (ens.kernel_launches() - l0) / max(steps, 1)
-    out["speedup"] = out["sequential"]["ms"] / out["batched"]["ms"]
+            out[mode]["gpu_launches_per_step"] = (ens.kernel_launches() - l0) / max(n, 1)
+    out["speedup"] = out["sequential"]["ms_per_step"] / out["batched"]["ms_per_step"]
     ens.close()
     return out
 
 
-def large_bench(n, steps, warmup=2, ws_train=1 << 20):
+def large_bench(n, steps, warmup=2, ws_train=1 << 20, net=None):
     """n^3 bubble cluster in NASG water hit by a 5e8 Pa shock, RK3, level set
     reinitialized every 10 steps: device-timed cell-stage updates/s (the
     reinitializations inside the timed steps included) and the interface-solve
@@ -342,10 +362,11 @@ def large_bench(n, steps, warmup=2, ws_train=1 << 20):
     out = {"workload": f"{n}^3 cluster of 8 SG gas bubbles in NASG water, 5e8 Pa planar shock, MUSCL-van Albada, "
                        f"HLLC, exact interface Riemann @1e-10, RK3, CFL 0.4, level-set reinitialization every 10 steps",
            "cells": cells, "steps": steps, "stages_per_step": 3}
-    net = None
+    own = net is None
     for mode in ("cold", "warm"):
         if mode == "warm":
-            _, net = ws.study(n_train=ws_train, n_test=1 << 12, epochs=60, keep_net=True)
+            if net is None:
+                _, net = ws.study(n_train=ws_train, n_test=1 << 12, epochs=60, keep_net=True)
             s.set_warm_start(net)
         s.set_state(FluidState(V, ID, phi))
         s.run(warmup)
@@ -387,7 +408,7 @@ def large_bench(n, steps, warmup=2, ws_train=1 << 20):
                            "ms_per_iteration": ms.value / max(it, 1)}
     s.set_warm_start(None)
     s.close()
-    if net is not None:
+    if own and net is not None:
         net.close()
     return out
 
@@ -466,9 +487,11 @@ def run_gb300(args):
              "riemann_stragglers"]
     phase = {n: float(v) / nph for n, v in zip(names, ph)}
     dom = max(("reconstruct", "face_flux", "update"), key=lambda n: phase[n])
+    fused = phase["reconstruct"] == 0.0   # the fused reconstruction + face-flux kernel ran
+    profile = FP64_PROFILE_FUSED if fused else FP64_PROFILE
     pk, pk_kind = peaks()
     per_launch_ms = phase[dom] / stages
-    prof = FP64_PROFILE.get(dom)
+    prof = profile.get(dom)
     # achieved = algorithmic bytes of the cell-stages one launch advances (the
     # fused ideal's bytes per cell-stage x cells) / the launch's event-timed
     # duration; traffic = the kernel's own DRAM bytes per launch (ncu, 128^3
@@ -479,16 +502,19 @@ def run_gb300(args):
     #   reconstruct: V 40 + ID 4 in, 6 face states 240 out                     = 284
     #   face_flux:   2 face states per face (3 faces: 240) + IDs 8 in, 3 fluxes 120 out = 368
     #   update:      6 fluxes 240 + Un/Us 80 + ID 4 + phi 8 + V 40 in, V 40 + phi 8 + U 40 out = 460
-    own_bytes = {"reconstruct": 284, "face_flux": 368, "update": 460}
+    #   fused reconstruction + face flux: V 40 + ID 4 in, 3 fluxes 120 out          = 164
+    own_bytes = {"reconstruct": 284, "face_flux": 164 if fused else 368, "update": 460}
     step_ms = t_ms / args.steps
-    roof = {"bound": "hbm", "kernel": dom, "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
+    step_dram = (STEP_DRAM_BYTES_PER_CELL_STAGE_FUSED if fused else STEP_DRAM_BYTES_PER_CELL_STAGE)
+    roof = {"bound": "hbm", "kernel": "recon_flux_tile (fused)" if fused and dom == "face_flux" else dom,
+            "achieved": achieved_gbs, "peak": pk["hbm_gbs"], "unit": "GB/s",
             "frac": achieved_gbs / pk["hbm_gbs"],
             "traffic": prof["dram_bytes_per_cell"] * cells if prof else None, "peak_source": pk_kind,
             "alg_bytes_per_cell_stage": alg, "launch_ms": per_launch_ms,
             "kernel_own_bytes_per_cell": own_bytes[dom],
             "step": {"alg_bytes_per_cell_stage": alg,
-                     "dram_bytes_per_cell_stage": STEP_DRAM_BYTES_PER_CELL_STAGE,
-                     "dram_over_alg": STEP_DRAM_BYTES_PER_CELL_STAGE / alg,
+                     "dram_bytes_per_cell_stage": step_dram,
+                     "dram_over_alg": step_dram / alg if step_dram else None,
                      "achieved_gbs": alg * cells * stages / (step_ms * 1e-3) / 1e9,
                      "frac": alg * cells * stages / (step_ms * 1e-3) / 1e9 / pk["hbm_gbs"],
                      "dram_source": "ncu whole-graph capture of the 128^3 step (profiles/)"}}
@@ -499,7 +525,7 @@ def run_gb300(args):
     # FP64-pipe instructions of one cell-stage summed over the stage kernels.
     dfma = C.c_double()
     fp64 = None
-    slots = sum(v["fp64_pipe_inst_per_cell"] for v in FP64_PROFILE.values())
+    slots = sum(v["fp64_pipe_inst_per_cell"] for v in profile.values())
     if lib.m2cg_fp64_peak(1 << 15, C.byref(dfma), None) == 0 and prof:
         inst = prof["fp64_pipe_inst_per_cell"] * cells / (per_launch_ms * 1e-3)
         flops = prof["fp64_flop_per_cell"] * cells / (per_launch_ms * 1e-3)
@@ -509,8 +535,9 @@ def run_gb300(args):
                 "fp64_pipe_inst_per_cell": prof["fp64_pipe_inst_per_cell"],
                 "fp64_flop_per_cell": prof["fp64_flop_per_cell"],
                 "peak_source": "measured now: m2cg_fp64_peak (independent binary64 FMA chains)",
-                "counts_source": "ncu, profiles/fp64_stage_kernels_shock_bubble_128.txt",
-                "step_fp64_pipe_inst_per_cell_stage": {k: v["fp64_pipe_inst_per_cell"] for k, v in FP64_PROFILE.items()},
+                "counts_source": "ncu, profiles/" + ("k_recon_flux_tile_shock_bubble_128.txt" if fused
+                                                     else "fp64_stage_kernels_shock_bubble_128.txt"),
+                "step_fp64_pipe_inst_per_cell_stage": {k: v["fp64_pipe_inst_per_cell"] for k, v in profile.items()},
                 "ceiling_cell_stage_per_s": dfma.value / slots,
                 "value_over_ceiling": value / (dfma.value / slots)}
     elif dfma.value > 0:
@@ -551,6 +578,7 @@ def run_gb300(args):
     # learned warm start: batch study (interface problems drawn from the
     # warm-start distribution) and the same step with the network in the loop
     wsres = None
+    ws_net = None
     if args.ws_train > 0 and rank == 0:
         from m2c_gb300 import warmstart as ws
         res, net = ws.study(n_train=args.ws_train, n_test=args.ws_test, epochs=args.ws_epochs, keep_net=True)
@@ -576,16 +604,18 @@ def run_gb300(args):
                           "mean_iters_per_solve_cold": iters / max(solves, 1),
                           "warm_solves": wsolves, "cold_solves": solves,
                           "note": "the same steps from the same initial state, cold and with the network"}
-        net.close()
         wsres = res
+        ws_net = net
 
     ensres = None
     if args.ens_domains > 0 and rank == 0:
-        ensres = ensemble_bench(args.ens_domains, args.ens_steps)
+        ensres = ensemble_bench(args.ens_domains, args.ens_steps, args.ens_seq_steps)
     largeres = None
     if args.large > 0 and rank == 0:
         s.close()  # the large run needs the device memory of the 256^3 context
-        largeres = large_bench(args.large, args.large_steps)
+        largeres = large_bench(args.large, args.large_steps, net=ws_net)
+    if ws_net is not None:
+        ws_net.close()
 
     if rank != 0:
         return 0

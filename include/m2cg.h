@@ -226,6 +226,20 @@ m2cg_status m2cg_integrate(m2cg_ctx* ctx, const double* box, double* out);
  * R: N x 5 doubles (real cells), may be NULL to keep the residual on device. */
 m2cg_status m2cg_compute_residual(m2cg_ctx* ctx, double* R);
 
+/* The interface Riemann solutions the last m2cg_compute_residual (or the first
+ * stage of the last step) stored: what ComputeResidual's RiemannSolutions
+ * argument receives (SpaceOperator.h:144-149, filled at SpaceOperator.cpp:
+ * 1661-1666, 1821-1826, 1980-1985).  Row r: the face between cell
+ * (i - e_d) and cell (i, j, k) = ijkd[4r .. 4r+2] in direction d = ijkd[4r+3]
+ * (0 x, 1 y, 2 z); vsm[5r..] the star state on the minus side with material
+ * ids[2r] -- the reference's left / bottom / back entry of cell (i, j, k) --
+ * and vsp[5r..] on the plus side with material ids[2r+1] -- the right / top /
+ * front entry of cell (i, j, k) - e_d.  Only solves that succeeded are listed,
+ * as in the reference; the IDs are the cells' current ones.  At most cap rows
+ * are written; *n receives the number of stored solutions (host arrays). */
+m2cg_status m2cg_riemann_solutions(m2cg_ctx* ctx, int64_t cap, int32_t* ijkd, double* vsm, double* vsp,
+                                   int32_t* ids, int64_t* n);
+
 /* LevelSetOperator::ComputeResidual, finite-difference solver
  * (LevelSetOperator.cpp:768-870). Rphi: N doubles. */
 m2cg_status m2cg_levelset_residual(m2cg_ctx* ctx, double* Rphi);
@@ -380,8 +394,9 @@ m2cg_status m2cg_set_warm_start(m2cg_ctx* ctx, m2cg_mlp* mlp);
  * member domains, each an ordinary context (m2cg_ensemble_member returns it;
  * upload / download / counters work on it as on any context), advanced
  * together with one launch per kernel and Runge-Kutta stage for all members
- * (one block row per member, the interface Riemann solves of all members as
- * one pool) inside one CUDA graph.  Members may differ in mesh, materials,
+ * (persistent cell and face kernels whose blocks take the members' blocks in
+ * turn, the interface Riemann solves of all members as one pool) inside one
+ * CUDA graph.  Members may differ in mesh, materials,
  * boundary conditions and state; they must share the time integrator (RK2 or
  * RK3), the level-set count and the interface reconstruction.  Each member
  * keeps its own CFL time step.  m2cg_ensemble_run_sequential advances the
@@ -402,6 +417,16 @@ int64_t m2cg_ensemble_kernel_launches(const m2cg_ensemble* ens);
  * calls.  best / ms_per_step (optional) receive the choice and its time. */
 m2cg_status m2cg_ensemble_autotune(m2cg_ensemble* ens, int32_t steps, int32_t n_cand, const int32_t* cand,
                                    int32_t* best, float* ms_per_step);
+/* No reference counterpart: tunes the block shape of the batched cell and face
+ * kernels per size class (members with the same cell count along x).  shapes:
+ * n_shapes rows {tx, ty, tz} with tx * ty * tz = 128 cells per block, or
+ * {0, 0, 0} for 128 consecutive cells in x-fastest order (the default).  For
+ * each class in turn, every shape runs `steps` real batched steps with the
+ * other classes at their choice so far, and the fastest is kept; the shape
+ * changes the schedule, not the results.  member_shape (optional, one entry
+ * per member) receives the chosen row; ms_per_step the last class's best. */
+m2cg_status m2cg_ensemble_autotune_tiles(m2cg_ensemble* ens, int32_t steps, int32_t n_shapes,
+                                         const int32_t* shapes, int32_t* member_shape, float* ms_per_step);
 
 /* ---- timing on the context stream -------------------------------------- */
 m2cg_status m2cg_sync(m2cg_ctx* ctx);

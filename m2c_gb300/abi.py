@@ -104,6 +104,7 @@ def default_config():
     for s in range(6):
         c.bc[s] = BC_OUTLET
         c.ls_bc[s] = LSBC_ZERO_NEUMANN
+    c.inlet[0] = c.inlet2[0] = 1.0e-6   # StateVariable's density (IoData.cpp:29-41)
     c.n_materials = 1
     for m in range(MAX_MATERIALS):
         set_material(c.mat[m], EOS_SG, gamma=1.4, pc=0.0)
@@ -192,6 +193,7 @@ def load(path=None):
         "m2cg_download_state": (C.c_int, [_P, _D, _I, _D]),
         "m2cg_compute_dt": (C.c_int, [_P, _D, _D]),
         "m2cg_compute_residual": (C.c_int, [_P, _D]),
+        "m2cg_riemann_solutions": (C.c_int, [_P, C.c_int64, _I, _D, _D, _I, C.POINTER(C.c_int64)]),
         "m2cg_levelset_residual": (C.c_int, [_P, _D]),
         "m2cg_advance": (C.c_int, [_P, C.c_double]),
         "m2cg_run": (C.c_int, [_P, C.c_int32, C.POINTER(Counters)]),
@@ -236,6 +238,7 @@ def load(path=None):
         "m2cg_ensemble_run_sequential": (C.c_int, [_P, C.c_int32, _F]),
         "m2cg_ensemble_kernel_launches": (C.c_int64, [_P]),
         "m2cg_ensemble_autotune": (C.c_int, [_P, C.c_int32, C.c_int32, _I, _I, _F]),
+        "m2cg_ensemble_autotune_tiles": (C.c_int, [_P, C.c_int32, C.c_int32, _I, _I, _F]),
     }
     for name, (res, args) in sig.items():
         f = getattr(lib, name)

@@ -499,6 +499,7 @@ m2cg_status m2cg_config_default(m2cg_config* c) {
   c->nx = c->ny = c->nz = 1;
   c->xmax = c->ymax = c->zmax = 1.0;
   for (int s = 0; s < 6; s++) { c->bc[s] = M2CG_BC_OUTLET; c->ls_bc[s] = M2CG_LSBC_ZERO_NEUMANN; }
+  c->inlet[0] = c->inlet2[0] = 1.0e-6;   // StateVariable's density (IoData.cpp:29-41)
   c->n_materials = 1;
   for (int m = 0; m < M2CG_MAX_MATERIALS; m++) {
     m2cg_material& t = c->mat[m];
@@ -802,6 +803,52 @@ m2cg_status m2cg_compute_residual(m2cg_ctx* x, double* R) {
   }
   CK(cudaStreamSynchronize(s));
   CK(cudaGetLastError());
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_riemann_solutions(m2cg_ctx* x, int64_t cap, int32_t* ijkd, double* vsm, double* vsp, int32_t* ids,
+                                   int64_t* n_out) {
+  if (!x || !n_out || cap < 0 || (cap > 0 && (!ijkd || !vsm || !vsp || !ids))) {
+    set_err("bad argument");
+    return M2CG_ERR_INVALID_ARG;
+  }
+  cudaStream_t s = x->stream;
+  unsigned long long cnt = 0;
+  CK(cudaMemcpyAsync(&cnt, x->L.count, sizeof(cnt), cudaMemcpyDeviceToHost, s));
+  CK(cudaStreamSynchronize(s));
+  const int64_t n = std::min<int64_t>((int64_t)cnt, x->L.cap);
+  std::vector<int64_t> face(n);
+  std::vector<int32_t> err(n), idh;
+  std::vector<double> m(5 * n), p(5 * n);
+  if (n > 0) {
+    CK(cudaMemcpyAsync(face.data(), x->L.face, n * sizeof(int64_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaMemcpyAsync(err.data(), x->L.err, n * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    for (int q = 0; q < 5; q++) {
+      CK(cudaMemcpyAsync(m.data() + q * n, x->L.vsm[q], n * sizeof(double), cudaMemcpyDeviceToHost, s));
+      CK(cudaMemcpyAsync(p.data() + q * n, x->L.vsp[q], n * sizeof(double), cudaMemcpyDeviceToHost, s));
+    }
+    idh.resize(x->P.g.ntot);
+    CK(cudaMemcpyAsync(idh.data(), x->id, idh.size() * sizeof(int32_t), cudaMemcpyDeviceToHost, s));
+    CK(cudaStreamSynchronize(s));
+  }
+  const Grid& g = x->P.g;
+  const int64_t st[3] = {1, g.sy, g.sz};
+  int64_t r = 0, stored = 0;
+  for (int64_t f = 0; f < n; f++) {
+    if (err[f] != 0) continue;   // not stored (SpaceOperator.cpp:1661)
+    stored++;
+    if (r >= cap) continue;
+    const int64_t c = face[f] >> 2;
+    const int d = (int)(face[f] & 3);
+    const int64_t kk = c / g.sz, rem = c - kk * g.sz, jj = rem / g.sy, ii = rem - jj * g.sy;
+    ijkd[4 * r + 0] = (int32_t)ii - 1; ijkd[4 * r + 1] = (int32_t)jj - 1; ijkd[4 * r + 2] = (int32_t)kk - 1;
+    ijkd[4 * r + 3] = d;
+    for (int q = 0; q < 5; q++) { vsm[5 * r + q] = m[q * n + f]; vsp[5 * r + q] = p[q * n + f]; }
+    ids[2 * r] = idh[c - st[d]];
+    ids[2 * r + 1] = idh[c];
+    r++;
+  }
+  *n_out = stored;
   return M2CG_OK;
 }
 
@@ -1309,6 +1356,15 @@ struct m2cg_ensemble {
 };
 
 static int64_t ens_cells(const m2cg_ctx* x) { return (int64_t)x->P.g.nx * x->P.g.ny * x->P.g.nz; }
+// threads of the cell / face kernels under the member's block shape
+static int64_t ens_cell_threads(const m2cg_ctx* x) {
+  const Grid& g = x->P.g;
+  return shaped_blocks(g, g.nx, g.ny, g.nz) * 128;
+}
+static int64_t ens_face_threads(const m2cg_ctx* x) {
+  const Grid& g = x->P.g;
+  return shaped_blocks(g, g.nx + 1, g.ny + 1, g.nz + 1) * 128;
+}
 static int64_t ens_faces(const m2cg_ctx* x) {
   return (int64_t)(x->P.g.nx + 1) * (x->P.g.ny + 1) * (x->P.g.nz + 1);
 }
@@ -1398,7 +1454,7 @@ static m2cg_status ens_enqueue_step(m2cg_ensemble* e, int64_t* nl) {
     ENS_TABLE(k_bc_args, bc);
     const bool after_recon = (x0->P.mp_recon != M2CG_MPREC_CONSTANT);
     auto recon = [&]() -> m2cg_status {
-      { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_cells, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_reconstruct_ens(s, nb_, rc_d, bo_, D); }
+      { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_cell_threads, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_reconstruct_ens(s, nb_, rc_d, bo_, D); }
       { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_ghosts, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_reconstruct_ghosts_ens(s, nb_, rg_d, bo_, D); }
       n += 2;
       return M2CG_OK;
@@ -1408,8 +1464,8 @@ static m2cg_status ens_enqueue_step(m2cg_ensemble* e, int64_t* nl) {
                        e->strag_count, e->sblocks, e->sreserve, e->strag_lanes);
     n += 3;
     if (!after_recon) { m2cg_status st = recon(); if (st != M2CG_OK) return st; }
-    { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_faces, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_face_flux_ens(s, nb_, ff_d, bo_, D); }
-    { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_cells, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_update_ens(s, nb_, up_d, bo_, D); }
+    { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_face_threads, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_face_flux_ens(s, nb_, ff_d, bo_, D); }
+    { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_cell_threads, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_update_ens(s, nb_, up_d, bo_, D); }
     n += 2;
     if (!last) { { int64_t nb_; int64_t* bo_ = ens_boff(e, ens_ghosts, 128, &nb_); if (!bo_) { set_err("ensemble table"); return M2CG_ERR_CUDA; } if (!e->building) launch_k_bc_ens(s, nb_, bc_d, bo_, D); } n++; }
   }
@@ -1621,6 +1677,60 @@ m2cg_status m2cg_ensemble_autotune(m2cg_ensemble* e, int32_t steps, int32_t n_ca
   if (st != M2CG_OK) return st;
   if (best) *best = best_limit;
   if (ms_per_step) *ms_per_step = best_ms / steps;
+  return M2CG_OK;
+}
+
+m2cg_status m2cg_ensemble_autotune_tiles(m2cg_ensemble* e, int32_t steps, int32_t n_shapes, const int32_t* shapes,
+                                         int32_t* member_shape, float* ms_per_step) {
+  if (!e || steps < 1 || n_shapes < 1 || !shapes) { set_err("bad tile autotune arguments"); return M2CG_ERR_INVALID_ARG; }
+  for (int c = 0; c < n_shapes; c++) {
+    const int32_t* t = shapes + 3 * c;
+    const bool linear = t[0] == 0 && t[1] == 0 && t[2] == 0;
+    if (!linear && (t[0] < 1 || t[1] < 1 || t[2] < 1 || t[0] * t[1] * t[2] != 128)) {
+      set_err("tile shape %d: %d x %d x %d is neither 0 x 0 x 0 nor 128 cells", c, t[0], t[1], t[2]);
+      return M2CG_ERR_INVALID_ARG;
+    }
+  }
+  auto rebuild = [&]() -> m2cg_status {
+    CK(cudaStreamSynchronize(e->stream));
+    if (e->graph) { cudaGraphExecDestroy(e->graph); e->graph = nullptr; }
+    for (void* p : e->dev) cudaFree(p);
+    e->dev.clear();
+    e->tab_i = 0;
+    return M2CG_OK;
+  };
+  auto set_shape = [&](m2cg_ctx* x, int c) {
+    for (int a = 0; a < 3; a++) x->P.g.tile[a] = shapes[3 * c + a];
+  };
+  // size classes: members with the same extent along x (the contiguous axis)
+  std::vector<int> cls;
+  for (m2cg_ctx* x : e->m)
+    if (std::find(cls.begin(), cls.end(), x->P.g.nx) == cls.end()) cls.push_back(x->P.g.nx);
+  std::vector<int> best(e->m.size(), 0);
+  for (size_t d = 0; d < e->m.size(); d++) set_shape(e->m[d], 0);
+  float last_best = 0.0f;
+  for (int nx : cls) {
+    float best_ms = 0.0f;
+    int best_c = 0;
+    for (int c = 0; c < n_shapes; c++) {
+      for (size_t d = 0; d < e->m.size(); d++)
+        if (e->m[d]->P.g.nx == nx) set_shape(e->m[d], c);
+      m2cg_status st = rebuild();
+      if (st != M2CG_OK) return st;
+      float ms = 0.0f;
+      st = m2cg_ensemble_run(e, steps, &ms);
+      if (st != M2CG_OK) return st;
+      if (c == 0 || ms < best_ms) { best_ms = ms; best_c = c; }
+    }
+    for (size_t d = 0; d < e->m.size(); d++)
+      if (e->m[d]->P.g.nx == nx) { set_shape(e->m[d], best_c); best[d] = best_c; }
+    last_best = best_ms;
+  }
+  m2cg_status st = rebuild();
+  if (st != M2CG_OK) return st;
+  if (member_shape)
+    for (size_t d = 0; d < e->m.size(); d++) member_shape[d] = best[d];
+  if (ms_per_step) *ms_per_step = last_best / steps;
   return M2CG_OK;
 }
 

@@ -16,8 +16,32 @@ struct Grid {
   int px, py, pz;
   int64_t sy, sz, ntot;  // sx = 1
   double dx, dy, dz;
+  // Block shape of the cell and face kernels: tile[0] x tile[1] x tile[2] cells
+  // per block of 128 threads (x fastest), or all zero: 128 consecutive cells of
+  // the x-fastest order.  Set per ensemble member by the tile autotuner.
+  int tile[3];
   M2CG_DEV int64_t at(int i, int j, int k) const { return ((int64_t)(k + 1) * py + (j + 1)) * px + (i + 1); }
 };
+
+// Cell (i, j, k) of thread th in block bx of an nx x ny x nz index space
+// covered by tiles t[0] x t[1] x t[2] (x fastest, then the tiles in x, y, z).
+M2CG_DEV bool tiled_index(int nx, int ny, int nz, const int* t, int64_t bx, int th, int& i, int& j, int& k) {
+  const int ntx = (nx + t[0] - 1) / t[0], nty = (ny + t[1] - 1) / t[1];
+  const int64_t per = (int64_t)ntx * nty;
+  const int bz = (int)(bx / per);
+  const int64_t r = bx - (int64_t)bz * per;
+  const int by = (int)(r / ntx), bxx = (int)(r - (int64_t)by * ntx);
+  i = bxx * t[0] + th % t[0];
+  j = by * t[1] + (th / t[0]) % t[1];
+  k = bz * t[2] + th / (t[0] * t[1]);
+  return i < nx && j < ny && k < nz;
+}
+// Blocks of 128 threads covering an nx x ny x nz index space with the grid's shape.
+inline int64_t shaped_blocks(const Grid& g, int nx, int ny, int nz) {
+  if (g.tile[0] == 0) return ((int64_t)nx * ny * nz + 127) / 128;
+  return (int64_t)((nx + g.tile[0] - 1) / g.tile[0]) * ((ny + g.tile[1] - 1) / g.tile[1]) *
+         ((nz + g.tile[2] - 1) / g.tile[2]);
+}
 
 // Face-ghost cells: position and image (SpaceOperator.cpp:493-519).
 M2CG_DEV bool ghost_face_cell(const Grid& g, int64_t t, int& side, int& i, int& j, int& k,

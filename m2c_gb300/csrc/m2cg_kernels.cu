@@ -5,6 +5,7 @@
 // One thread per cell (or per face-owning cell); every face flux is evaluated
 // exactly once.  All arithmetic is binary64; the FP64 pipe, not HBM, bounds
 // these kernels on GB300.
+#include <algorithm>
 #include "m2cg_internal.h"
 #include "m2cg_ens.h"
 
@@ -38,6 +39,12 @@ __device__ __forceinline__ bool real_cell(const Grid& g, int64_t t, int& i, int&
   return true;
 }
 
+// Real cell of this thread in block bx of a cell kernel (the grid's block shape).
+__device__ __forceinline__ bool block_cell(const Grid& g, int64_t bx, int& i, int& j, int& k) {
+  if (g.tile[0] == 0) return real_cell(g, bx * blockDim.x + threadIdx.x, i, j, k);
+  return tiled_index(g.nx, g.ny, g.nz, g.tile, bx, threadIdx.x, i, j, k);
+}
+
 // CheckReconstructedStates (SpaceOperator.cpp:2446-2484): a face state that
 // clipping would change reverts to the cell value; then the six face states
 // are stored.
@@ -68,7 +75,7 @@ __device__ __forceinline__ void store_faces(const DevMat& M, const double* q, do
 // (SpaceOperator.cpp:2446-2484).  fs[f*5+p]: f = vl, vr, vb, vt, vk, vf.
 __device__ __forceinline__ void k_reconstruct_body(const Params& P, const StateSet& S, const int32_t* __restrict__ id, double* const* fs, unsigned long long* cnt, unsigned bx_, unsigned gx_) {
   int i, j, k;
-  if (!real_cell(P.g, (int64_t)bx_ * blockDim.x + threadIdx.x, i, j, k)) return;
+  if (!block_cell(P.g, bx_, i, j, k)) return;
   const Grid& g = P.g;
   int64_t c = g.at(i, j, k);
   double q[5];
@@ -118,10 +125,13 @@ __global__ void __launch_bounds__(128) k_reconstruct(Params P, StateSet S, const
                                                      double* const* fs, unsigned long long* cnt) { k_reconstruct_body(P, S, id, fs, cnt, blockIdx.x, gridDim.x); }
 // batched: the launch's blocks are the members' blocks back to back
 // (boff: exclusive prefix of the members' block counts)
-__global__ void __launch_bounds__(128) k_reconstruct_ens(const k_reconstruct_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
-  const int d = ens_member(boff, D, blockIdx.x);
-  const k_reconstruct_args& e = ea[d];
-  k_reconstruct_body(e.P, e.S, e.id, e.fs, e.cnt, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
+__global__ void __launch_bounds__(128) k_reconstruct_ens(const k_reconstruct_args* __restrict__ ea, const int64_t* __restrict__ boff, int D, int64_t nvb) {
+  // persistent: the launch's blocks take the members' blocks in turn
+  for (int64_t b = blockIdx.x; b < nvb; b += gridDim.x) {
+    const int d = ens_member(boff, D, b);
+    const k_reconstruct_args& e = ea[d];
+    k_reconstruct_body(e.P, e.S, e.id, e.fs, e.cnt, (unsigned)(b - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
+  }
 }
 
 
@@ -362,13 +372,19 @@ __device__ __forceinline__ bool num_flux(const Params& P, int dir, const double*
 // 1852-1861, 2011-2020).  The thread of cell c owns the faces at its minus side.
 __device__ __forceinline__ void k_face_flux_body(const Params& P, const int32_t* __restrict__ id, double* const* fs, double* const* F, unsigned long long* cnt, unsigned bx_, unsigned gx_) {
   const Grid& g = P.g;
-  int64_t t = (int64_t)bx_ * blockDim.x + threadIdx.x;
-  int64_t ex = g.nx + 1, ey = g.ny + 1;
-  int64_t n = ex * ey * (g.nz + 1);
-  if (t >= n) return;
-  int k = (int)(t / (ex * ey));
-  int64_t r = t - (int64_t)k * ex * ey;
-  int j = (int)(r / ex), i = (int)(r - (int64_t)j * ex);
+  int i, j, k;
+  if (g.tile[0]) {
+    if (!tiled_index(g.nx + 1, g.ny + 1, g.nz + 1, g.tile, bx_, threadIdx.x, i, j, k)) return;
+  } else {
+    int64_t t = (int64_t)bx_ * blockDim.x + threadIdx.x;
+    int64_t ex = g.nx + 1, ey = g.ny + 1;
+    int64_t n = ex * ey * (g.nz + 1);
+    if (t >= n) return;
+    k = (int)(t / (ex * ey));
+    int64_t r = t - (int64_t)k * ex * ey;
+    j = (int)(r / ex);
+    i = (int)(r - (int64_t)j * ex);
+  }
   int64_t c = g.at(i, j, k);
   const int64_t st[3] = {1, g.sy, g.sz};
   bool has[3] = {j < g.ny && k < g.nz, i < g.nx && k < g.nz, i < g.nx && j < g.ny};
@@ -392,10 +408,13 @@ __global__ void __launch_bounds__(128) k_face_flux(Params P, const int32_t* __re
                             unsigned long long* cnt) { k_face_flux_body(P, id, fs, F, cnt, blockIdx.x, gridDim.x); }
 // batched: the launch's blocks are the members' blocks back to back
 // (boff: exclusive prefix of the members' block counts)
-__global__ void __launch_bounds__(128) k_face_flux_ens(const k_face_flux_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
-  const int d = ens_member(boff, D, blockIdx.x);
-  const k_face_flux_args& e = ea[d];
-  k_face_flux_body(e.P, e.id, e.fs, e.F, e.cnt, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
+__global__ void __launch_bounds__(128) k_face_flux_ens(const k_face_flux_args* __restrict__ ea, const int64_t* __restrict__ boff, int D, int64_t nvb) {
+  // persistent: the launch's blocks take the members' blocks in turn
+  for (int64_t b = blockIdx.x; b < nvb; b += gridDim.x) {
+    const int d = ens_member(boff, D, b);
+    const k_face_flux_args& e = ea[d];
+    k_face_flux_body(e.P, e.id, e.fs, e.F, e.cnt, (unsigned)(b - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
+  }
 }
 
 
@@ -445,7 +464,7 @@ __device__ __forceinline__ double ls_residual(const Params& P, const double* __r
 // MultiPhaseOperator::UpdateMaterialIDByLevelSet (MultiPhaseOperator.cpp:177-222).
 __device__ __forceinline__ void k_update_body(const Params& P, const StageArgs& A, const int32_t* __restrict__ id, int32_t* __restrict__ id_new, double* const* F, const IfaceList& L, const DevScalars* __restrict__ sc, int64_t* __restrict__ swept, unsigned long long* swept_count, int64_t swept_cap, unsigned long long* cnt, unsigned bx_, unsigned gx_) {
   int i, j, k;
-  if (!real_cell(P.g, (int64_t)bx_ * blockDim.x + threadIdx.x, i, j, k)) return;
+  if (!block_cell(P.g, bx_, i, j, k)) return;
   if (!sc->active && !A.residual_only) return;
   const Grid& g = P.g;
   int64_t c = g.at(i, j, k);
@@ -553,10 +572,13 @@ __global__ void k_update(Params P, StageArgs A, const int32_t* __restrict__ id, 
                          unsigned long long* cnt) { k_update_body(P, A, id, id_new, F, L, sc, swept, swept_count, swept_cap, cnt, blockIdx.x, gridDim.x); }
 // batched: the launch's blocks are the members' blocks back to back
 // (boff: exclusive prefix of the members' block counts)
-__global__ void k_update_ens(const k_update_args* __restrict__ ea, const int64_t* __restrict__ boff, int D) {
-  const int d = ens_member(boff, D, blockIdx.x);
-  const k_update_args& e = ea[d];
-  k_update_body(e.P, e.A, e.id, e.id_new, e.F, e.L, e.sc, e.swept, e.swept_count, e.swept_cap, e.cnt, (unsigned)(blockIdx.x - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
+__global__ void k_update_ens(const k_update_args* __restrict__ ea, const int64_t* __restrict__ boff, int D, int64_t nvb) {
+  // persistent: the launch's blocks take the members' blocks in turn
+  for (int64_t b = blockIdx.x; b < nvb; b += gridDim.x) {
+    const int d = ens_member(boff, D, b);
+    const k_update_args& e = ea[d];
+    k_update_body(e.P, e.A, e.id, e.id_new, e.F, e.L, e.sc, e.swept, e.swept_count, e.swept_cap, e.cnt, (unsigned)(b - boff[d]), (unsigned)(boff[d + 1] - boff[d]));
+  }
 }
 
 
@@ -1074,7 +1096,7 @@ void launch_reconstruct(cudaStream_t s, const Params& P, const StateSet& S, cons
                         unsigned long long* cnt) {
   int64_t n = (int64_t)P.g.nx * P.g.ny * P.g.nz;
   if (P.rec_type == M2CG_REC_CONSTANT || P.rec_var == M2CG_VAR_PRIMITIVE)
-    k_reconstruct<<<nblk(n, 128), 128, 0, s>>>(P, S, id, fs, cnt);
+    k_reconstruct<<<(unsigned)shaped_blocks(P.g, P.g.nx, P.g.ny, P.g.nz), 128, 0, s>>>(P, S, id, fs, cnt);
   else if (P.rec_var == M2CG_VAR_CONSERVATIVE)
     k_reconstruct_var<M2CG_VAR_CONSERVATIVE><<<nblk(n, 128), 128, 0, s>>>(P, S, id, fs, cnt);
   else if (P.rec_var == M2CG_VAR_PRIMITIVE_CHARACTERISTIC)
@@ -1086,14 +1108,13 @@ void launch_reconstruct(cudaStream_t s, const Params& P, const StateSet& S, cons
 }
 void launch_face_flux(cudaStream_t s, const Params& P, const int32_t* id, double* const* fs, double* const* F,
                       unsigned long long* cnt) {
-  int64_t n = (int64_t)(P.g.nx + 1) * (P.g.ny + 1) * (P.g.nz + 1);
-  k_face_flux<<<nblk(n, 128), 128, 0, s>>>(P, id, fs, F, cnt);
+  k_face_flux<<<(unsigned)shaped_blocks(P.g, P.g.nx + 1, P.g.ny + 1, P.g.nz + 1), 128, 0, s>>>(P, id, fs, F, cnt);
 }
 void launch_update(cudaStream_t s, const Params& P, const StageArgs& A, const int32_t* id, int32_t* id_new,
                    double* const* F, const IfaceList& L, const DevScalars* sc, int64_t* swept,
                    unsigned long long* swept_count, int64_t swept_cap, unsigned long long* cnt) {
-  int64_t n = (int64_t)P.g.nx * P.g.ny * P.g.nz;
-  k_update<<<nblk(n, 128), 128, 0, s>>>(P, A, id, id_new, F, L, sc, swept, swept_count, swept_cap, cnt);
+  k_update<<<(unsigned)shaped_blocks(P.g, P.g.nx, P.g.ny, P.g.nz), 128, 0, s>>>(P, A, id, id_new, F, L, sc, swept,
+                                                                                swept_count, swept_cap, cnt);
 }
 void launch_ls_residual(cudaStream_t s, const Params& P, const StateSet& S, double* out) {
   int64_t n = (int64_t)P.g.nx * P.g.ny * P.g.nz;
@@ -1164,10 +1185,29 @@ __global__ void k_reset_counters_ens(const CounterResetArgs* __restrict__ ea) {
   void launch_##K##_ens(cudaStream_t s, int64_t blocks, const K##_args* t, const int64_t* boff, int D) { \
     if (blocks > 0 && D > 0) K##_ens<<<(unsigned)blocks, B, 0, s>>>(t, boff, D);                       \
   }
-M2CG_ENS_LAUNCHER(k_reconstruct, 128)
+// The per-stage cell and face kernels of a batch run persistent: as many
+// blocks as fit on the GPU at once (occupancy x SMs), each looping over the
+// members' blocks (a work queue in member order, boff).
+template <class KF>
+static int persistent_grid(KF kernel, int block) {
+  int dev = 0, nsm = 0, per = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per, kernel, block, 0) != cudaSuccess || per < 1) {
+    cudaGetLastError();
+    per = 1;
+  }
+  return std::max(1, nsm * per);
+}
+#define M2CG_ENS_PERSISTENT_LAUNCHER(K, B)                                                             \
+  void launch_##K##_ens(cudaStream_t s, int64_t blocks, const K##_args* t, const int64_t* boff, int D) { \
+    static const int grid = persistent_grid(K##_ens, B);                                                \
+    if (blocks > 0 && D > 0) K##_ens<<<(unsigned)std::min<int64_t>(blocks, grid), B, 0, s>>>(t, boff, D, blocks); \
+  }
+M2CG_ENS_PERSISTENT_LAUNCHER(k_reconstruct, 128)
 M2CG_ENS_LAUNCHER(k_reconstruct_ghosts, 128)
-M2CG_ENS_LAUNCHER(k_face_flux, 128)
-M2CG_ENS_LAUNCHER(k_update, 128)
+M2CG_ENS_PERSISTENT_LAUNCHER(k_face_flux, 128)
+M2CG_ENS_PERSISTENT_LAUNCHER(k_update, 128)
 M2CG_ENS_LAUNCHER(k_bc, 128)
 M2CG_ENS_LAUNCHER(k_dt_reduce, 256)
 M2CG_ENS_LAUNCHER(k_dt_finalize, 1)

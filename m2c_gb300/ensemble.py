@@ -51,6 +51,24 @@ class Ensemble:
                                                             C.byref(best), C.byref(ms)), "m2cg_ensemble_autotune")
         return best.value, ms.value
 
+    # block shapes tried by autotune_tiles: 128 consecutive cells, or tiles of
+    # 128 cells over (x, y, z)
+    TILE_SHAPES = ((0, 0, 0), (32, 4, 1), (32, 2, 2), (16, 8, 1), (16, 4, 2), (8, 4, 4))
+
+    def autotune_tiles(self, steps=1, shapes=TILE_SHAPES):
+        """Pick the cell / face kernels' block shape per size class (members
+        with the same cell count along x) by timing `steps` real batched steps
+        per class and shape (the states advance); returns ({nx: shape},
+        ms per step of the last class's choice)."""
+        import numpy as np
+        sh = np.ascontiguousarray(np.asarray(shapes, np.int32).reshape(-1, 3))
+        mshape = np.zeros(len(self.cfgs), np.int32)
+        ms = C.c_float()
+        abi.check(self.lib, self.lib.m2cg_ensemble_autotune_tiles(self.h, int(steps), len(sh), abi.iptr(sh),
+                                                                  abi.iptr(mshape), C.byref(ms)),
+                  "m2cg_ensemble_autotune_tiles")
+        return {int(c.nx): tuple(int(v) for v in sh[mshape[i]]) for i, c in enumerate(self.cfgs)}, ms.value
+
     def kernel_launches(self):
         return self.lib.m2cg_ensemble_kernel_launches(self.h)
 

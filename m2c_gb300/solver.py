@@ -119,6 +119,21 @@ class Solver:
         abi.check(self.lib, self.lib.m2cg_compute_residual(self.ctx, abi.dptr(R)), "m2cg_compute_residual")
         return R
 
+    def RiemannSolutions(self, cap=None):
+        """The interface Riemann solutions of the last ComputeResidual (what the
+        reference's RiemannSolutions argument receives): dict of ijkd (n x 4:
+        plus cell i, j, k and direction), Vsm, Vsp (n x 5) and ids (n x 2)."""
+        n = C.c_int64()
+        abi.check(self.lib, self.lib.m2cg_riemann_solutions(self.ctx, 0, None, None, None, None, C.byref(n)),
+                  "m2cg_riemann_solutions")
+        m = n.value if cap is None else min(cap, n.value)
+        ijkd = np.zeros((m, 4), np.int32)
+        vsm, vsp = np.zeros((m, 5)), np.zeros((m, 5))
+        ids = np.zeros((m, 2), np.int32)
+        abi.check(self.lib, self.lib.m2cg_riemann_solutions(self.ctx, m, abi.iptr(ijkd), abi.dptr(vsm), abi.dptr(vsp),
+                                                            abi.iptr(ids), C.byref(n)), "m2cg_riemann_solutions")
+        return dict(ijkd=ijkd, Vsm=vsm, Vsp=vsp, ids=ids)
+
     def LevelSetResidual(self):
         R = np.zeros(self.n)
         abi.check(self.lib, self.lib.m2cg_levelset_residual(self.ctx, abi.dptr(R)), "m2cg_levelset_residual")

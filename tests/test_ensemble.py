@@ -81,3 +81,30 @@ def test_autotuned_ensemble_matches_members_run_alone():
         assert np.array_equal(a.Phi, b.Phi), i
         solo.close()
     ens.close()
+
+
+@pytest.mark.gpu
+def test_tile_shapes_change_the_schedule_not_the_results():
+    """The persistent batched kernels under every block shape the tile
+    autotuner tries: after tuning (whose trial steps are real steps) every
+    member ends bit for bit where it ends advanced alone, and the chosen shape
+    is one of the candidates for every size class."""
+    doms = [problems.bubble_collapse(*d) for d in SMALL]
+    ens = Ensemble([d[0] for d in doms])
+    for i, (c, V, ID, phi) in enumerate(doms):
+        ens.member(i).set_state(FluidState(V, ID, phi))
+    shapes = Ensemble.TILE_SHAPES
+    chosen, ms = ens.autotune_tiles(steps=1, shapes=shapes)
+    assert ms > 0 and set(chosen) == {d[0].nx for d in doms}
+    assert all(s in shapes for s in chosen.values())
+    ntrial = len(set(chosen)) * len(shapes)
+    ens.run(2)
+    for i, (c, V, ID, phi) in enumerate(doms):
+        solo = Solver(c, FluidState(V, ID, phi))
+        solo.run(ntrial + 2)
+        a, b = ens.member(i).get_state(), solo.get_state()
+        assert np.array_equal(a.ID, b.ID), i
+        assert np.array_equal(a.V, b.V), i
+        assert np.array_equal(a.Phi, b.Phi), i
+        solo.close()
+    ens.close()

@@ -179,3 +179,31 @@ def test_run_loop_matches_oracle():
     assert abs(c["time"] - o.counters()["time"]) <= 1e-12 * c["time"]
     assert np.all(state_err(g.V, Vo) < TOL100)
     np.testing.assert_array_equal(g.ID, IDo)
+
+
+def test_riemann_solutions_of_the_residual_match_oracle_solves():
+    # what ComputeResidual's RiemannSolutions receives: one entry per interface
+    # face whose solve succeeded, the star states of its two sides
+    cfg, V, ID, phi = problems.shock_bubble(n=24)
+    s = Solver(cfg, FluidState(V, ID, phi))
+    s.ComputeResidual()
+    sol = s.RiemannSolutions()
+    n = cfg.nx
+    assert len(sol["ijkd"]) > 100
+    st = (1, n, n * n)
+    plus = np.array([(k * n + j) * n + i for i, j, k, d in sol["ijkd"]])
+    minus = plus - np.array([st[d] for d in sol["ijkd"][:, 3]])
+    np.testing.assert_array_equal(sol["ids"][:, 0], ID[minus])
+    np.testing.assert_array_equal(sol["ids"][:, 1], ID[plus])
+    assert np.all(ID[minus] != ID[plus])
+    dirs = np.zeros((len(plus), 3))
+    dirs[np.arange(len(plus)), sol["ijkd"][:, 3]] = 1.0
+    o = ob.riemann_batch(cfg, V[minus], ID[minus], V[plus], ID[plus], dirs)
+    assert np.all(o["err"] == 0)
+    np.testing.assert_allclose(sol["Vsm"], o["Vsm"], rtol=1e-12, atol=1e-300)
+    np.testing.assert_allclose(sol["Vsp"], o["Vsp"], rtol=1e-12, atol=1e-300)
+    # every interface face of the state is listed (no failures on this input)
+    I3 = ID.reshape(n, n, n)
+    n_if = sum(int((np.diff(I3, axis=a) != 0).sum()) for a in range(3))
+    assert len(plus) == n_if
+    s.close()
