@@ -64,7 +64,7 @@ FP64_PROFILE_FUSED = {
 # (profiles/reinit_graph_shock_bubble_128.txt) and fused
 # (profiles/step_graph_shock_bubble_128.txt).
 STEP_DRAM_BYTES_PER_CELL_STAGE = (2388.8e6 + 1971.9e6) / (128 ** 3 * 2)
-STEP_DRAM_BYTES_PER_CELL_STAGE_FUSED = None
+STEP_DRAM_BYTES_PER_CELL_STAGE_FUSED = (1305.2e6 + 956.4e6) / (128 ** 3 * 2)
 # Algorithmic bytes per cell-stage of the fused ideal (binary64 V and phi, int32
 # ID, ideal halo reuse): a first stage reads W = (V, phi) 48 B + ID 4 B and
 # writes 48 B = 100 B; a later stage also reads W^n = 148 B.  Mean over the
@@ -91,7 +91,7 @@ def parse():
     ap.add_argument("--reinit", type=int, default=0)
     # learned warm start: training / test problems of the study (0 disables it)
     ap.add_argument("--ws-train", type=int, default=1 << 20)
-    ap.add_argument("--ws-test", type=int, default=1 << 17)
+    ap.add_argument("--ws-test", type=int, default=1 << 16)
     ap.add_argument("--ws-epochs", type=int, default=60)
     # batched ensemble of uneven bubble-collapse domains (0 disables it): batched
     # steps, and steps of the per-domain-launch baseline
@@ -183,81 +183,110 @@ def cpu_model():
     return {"model": name or "unknown", "logical_cpus": os.cpu_count()}
 
 
-def oracle_leg(args, cfg, V, ID, phi, stages):
+class OracleLeg:
     """The CPU-baseline leg: the oracle (the CPU restatement of the reference
-    numerics, every host thread) advances the benchmarked workload itself from
-    the same initial state as a fresh GPU context, to each parity checkpoint.
-    Its wall time over all checkpoints is the all-core CPU rate; one step of a
-    64^3 sample on one thread gives the single-thread rate.  At every
-    checkpoint the GPU state is compared with the oracle's, and -- up to
-    --parity-fma-steps -- the oracle compiled with fused multiply-add
-    contraction is compared with the oracle too: how far the reference's own
-    numerics move under a contracting compiler, the yardstick for the GPU's
-    FMA-contracting kernels."""
-    from m2c_gb300 import problems
-    from m2c_gb300.solver import FluidState, Solver
-    from oracle import binding as ob
-    from oracle import parity
-    threads = os.cpu_count()
-    for fma in (False, True):
-        ob.lib(fma).orc_set_threads(threads)
-    used = ob.lib().orc_max_threads()
-    cells = cfg.nx * cfg.ny * cfg.nz
-    shape = (cfg.nz, cfg.ny, cfg.nx)
-    cps = sorted({int(x) for x in str(args.parity_steps).split(",") if x.strip()})
-    g = Solver(cfg, FluidState(V, ID, phi))
-    o = ob.OracleSim(cfg)
-    o.upload(V, ID, phi)
-    f = ob.OracleSim(cfg, fma=True) if args.parity_fma_steps > 0 else None
-    if f is not None:
-        f.upload(V, ID, phi)
-    t0g, t0o = g.conserved_totals(), o.conserved_totals()
-    out = {"workload": "the benchmarked workload, GPU (fresh context, graph-replayed steps) and oracle from the same "
-                       "initial state", "checkpoints": []}
-    done, t_orc = 0, 0.0
-    for c in cps:
-        g.run(c - done)
+    numerics) advances the benchmarked workload itself from the initial state
+    to each parity checkpoint, in a background thread (ctypes releases the
+    GIL) while the device-timed GPU legs run; it leaves one host core to the
+    GPU's host thread.  Its wall time over all checkpoints is the all-core CPU
+    rate; one step of a 64^3 sample on one thread, run before the thread
+    starts, gives the single-thread rate.  Up to --parity-fma-steps the oracle
+    compiled with fused multiply-add contraction runs too: how far the
+    reference's own numerics move under a contracting compiler, the yardstick
+    for the GPU's FMA-contracting kernels.  finish() then advances a fresh GPU
+    context to the same checkpoints and compares state, IDs, counters and
+    conserved totals."""
+
+    def __init__(self, args, cfg, V, ID, phi, stages):
+        import threading
+        from m2c_gb300 import problems
+        from oracle import binding as ob
+        self.args, self.cfg, self.V, self.ID, self.phi, self.stages = args, cfg, V, ID, phi, stages
+        self.cps = sorted({int(x) for x in str(args.parity_steps).split(",") if x.strip()})
+        self.threads = max(1, (os.cpu_count() or 1) - 1)
+        # one thread, one step of a 64^3 sample of the same problem
+        ob.lib().orc_set_threads(1)
+        c1, V1, I1, p1 = problems.shock_bubble(n=64)
+        o1 = ob.OracleSim(c1)
+        o1.upload(V1, I1, p1)
         t = time.perf_counter()
-        o.run(c - done)
-        t_orc += time.perf_counter() - t
-        if f is not None and c <= args.parity_fma_steps:
-            f.run(c - done)
-        done = c
-        gs = g.get_state()
-        Vo, IDo, pho = o.download()
-        cp = {"step": c}
-        cp.update(parity.compare(gs.V, gs.ID, gs.Phi, Vo, IDo, pho, shape))
-        cp["counters"] = parity.counters_pair(g.counters(), o.counters())
-        tg, to = g.conserved_totals(), o.conserved_totals()
-        cp["conserved_gpu"] = parity.totals_dict(t0g, tg, ref=to)
-        cp["conserved_oracle"] = parity.totals_dict(t0o, to)
-        if f is not None and c <= args.parity_fma_steps:
-            Vf, IDf, phf = f.download()
-            y = parity.compare(Vf, IDf, phf, Vo, IDo, pho, shape)
-            cf = f.counters()
-            y["riemann_errors"] = int(cf["riemann_errors"])
-            y["riemann_iterations"] = int(cf["riemann_iterations"])
-            cp["oracle_fma_vs_oracle"] = y
-        out["checkpoints"].append(cp)
-    g.close()
-    del o, f
-    rate = cells * stages * done / t_orc
-    # one thread, one step of a 64^3 sample of the same problem
-    ob.lib().orc_set_threads(1)
-    c1, V1, I1, p1 = problems.shock_bubble(n=64)
-    o1 = ob.OracleSim(c1)
-    o1.upload(V1, I1, p1)
-    t = time.perf_counter()
-    o1.run(1)
-    t1 = time.perf_counter() - t
-    ob.lib().orc_set_threads(threads)
-    cpu = {"value": rate, "unit": UNIT, "cores": used, "kind": "port",
-           "sample": f"oracle CPU restatement on the benchmarked workload itself ({cfg.nx}^3), {done} RK2 steps from "
-                     f"the initial state, {t_orc:.1f} s on {used} threads",
-           "single_thread": {"value": 64 ** 3 * stages / t1, "unit": UNIT, "cores": 1,
-                             "sample": f"shock-bubble 64^3, 1 RK2 step, {t1:.2f} s"},
-           "cpu": cpu_model()}
-    return cpu, out
+        o1.run(1)
+        self.t1 = time.perf_counter() - t
+        del o1
+        for fma in (False, True):
+            ob.lib(fma).orc_set_threads(self.threads)
+        self.used = ob.lib().orc_max_threads()
+        self.snap, self.snap_fma, self.error = {}, {}, None
+        self.t_orc = 0.0
+        self.thread = threading.Thread(target=self._run, daemon=True)
+        self.thread.start()
+
+    def _run(self):
+        from oracle import binding as ob
+        try:
+            for fma, store, last in ((False, self.snap, self.cps[-1]), (True, self.snap_fma, self.args.parity_fma_steps)):
+                if last <= 0:
+                    continue
+                o = ob.OracleSim(self.cfg, fma=fma)
+                o.upload(self.V, self.ID, self.phi)
+                store[0] = {"totals": o.conserved_totals()}
+                done = 0
+                for c in self.cps:
+                    if c > last:
+                        break
+                    t = time.perf_counter()
+                    o.run(c - done)
+                    if not fma:
+                        self.t_orc += time.perf_counter() - t
+                    done = c
+                    Vo, IDo, pho = o.download()
+                    store[c] = {"state": (Vo, IDo, pho), "counters": o.counters(), "totals": o.conserved_totals()}
+                del o
+        except Exception as e:   # reported in the bench line, never hidden
+            self.error = repr(e)
+
+    def finish(self):
+        from m2c_gb300.solver import FluidState, Solver
+        from oracle import parity
+        self.thread.join()
+        if self.error:
+            return {"error": self.error}, {"error": self.error}
+        cfg = self.cfg
+        cells = cfg.nx * cfg.ny * cfg.nz
+        shape = (cfg.nz, cfg.ny, cfg.nx)
+        g = Solver(cfg, FluidState(self.V, self.ID, self.phi))
+        t0g, t0o = g.conserved_totals(), self.snap[0]["totals"]
+        out = {"workload": "the benchmarked workload, GPU (fresh context, graph-replayed steps) and oracle from the "
+                           "same initial state", "checkpoints": []}
+        done = 0
+        for c in self.cps:
+            g.run(c - done)
+            done = c
+            gs = g.get_state()
+            Vo, IDo, pho = self.snap[c]["state"]
+            cp = {"step": c}
+            cp.update(parity.compare(gs.V, gs.ID, gs.Phi, Vo, IDo, pho, shape))
+            cp["counters"] = parity.counters_pair(g.counters(), self.snap[c]["counters"])
+            tg, to = g.conserved_totals(), self.snap[c]["totals"]
+            cp["conserved_gpu"] = parity.totals_dict(t0g, tg, ref=to)
+            cp["conserved_oracle"] = parity.totals_dict(t0o, to)
+            if c in self.snap_fma:
+                Vf, IDf, phf = self.snap_fma[c]["state"]
+                y = parity.compare(Vf, IDf, phf, Vo, IDo, pho, shape)
+                y["riemann_errors"] = int(self.snap_fma[c]["counters"]["riemann_errors"])
+                y["riemann_iterations"] = int(self.snap_fma[c]["counters"]["riemann_iterations"])
+                cp["oracle_fma_vs_oracle"] = y
+            out["checkpoints"].append(cp)
+        g.close()
+        rate = cells * self.stages * done / self.t_orc
+        cpu = {"value": rate, "unit": UNIT, "cores": self.used, "kind": "port",
+               "sample": f"oracle CPU restatement on the benchmarked workload itself ({cfg.nx}^3), {done} RK2 steps "
+                         f"from the initial state, {self.t_orc:.1f} s on {self.used} threads (beside the "
+                         f"device-timed GPU legs, one core left to their host thread)",
+               "single_thread": {"value": 64 ** 3 * self.stages / self.t1, "unit": UNIT, "cores": 1,
+                                 "sample": f"shock-bubble 64^3, 1 RK2 step, {self.t1:.2f} s"},
+               "cpu": cpu_model()}
+        return cpu, out
 
 
 def run_reference(args):
@@ -517,7 +546,8 @@ def run_gb300(args):
                      "dram_over_alg": step_dram / alg if step_dram else None,
                      "achieved_gbs": alg * cells * stages / (step_ms * 1e-3) / 1e9,
                      "frac": alg * cells * stages / (step_ms * 1e-3) / 1e9 / pk["hbm_gbs"],
-                     "dram_source": "ncu whole-graph capture of the 128^3 step (profiles/)"}}
+                     "dram_source": "ncu whole-graph capture of the 128^3 step (profiles/" +
+                                    ("step_graph_shock_bubble_128.txt)" if fused else "reinit_graph_shock_bubble_128.txt)")}}
     # the binding bound of the stage kernels: GB300's FP64 pipe.  Peak = binary64
     # FMAs/s of this GPU measured now (m2cg_fp64_peak); achieved = the kernel's
     # FP64-pipe instructions per launch (per-cell count from the ncu profile x
@@ -575,6 +605,15 @@ def run_gb300(args):
     for p in (hv, hi, hp):
         lib.m2cg_host_free(p)
 
+    # batched ensemble (its per-domain baseline is wall-timed: it runs before
+    # the oracle leg starts on the host cores)
+    ensres = None
+    if args.ens_domains > 0 and rank == 0:
+        ensres = ensemble_bench(args.ens_domains, args.ens_steps, args.ens_seq_steps)
+    # the oracle leg runs on the host cores from here on, beside the
+    # device-timed legs below
+    oleg = OracleLeg(args, cfg, V, ID, phi, stages) if (not args.no_cpu and rank == 0) else None
+
     # learned warm start: batch study (interface problems drawn from the
     # warm-start distribution) and the same step with the network in the loop
     wsres = None
@@ -607,9 +646,6 @@ def run_gb300(args):
         wsres = res
         ws_net = net
 
-    ensres = None
-    if args.ens_domains > 0 and rank == 0:
-        ensres = ensemble_bench(args.ens_domains, args.ens_steps, args.ens_seq_steps)
     largeres = None
     if args.large > 0 and rank == 0:
         s.close()  # the large run needs the device memory of the 256^3 context
@@ -620,10 +656,10 @@ def run_gb300(args):
     if rank != 0:
         return 0
     cpu, parity = None, None
-    if not args.no_cpu:
+    if oleg is not None:
         if largeres is None:
             s.close()   # the parity leg runs its own context from the initial state
-        cpu, parity = oracle_leg(args, cfg, V, ID, phi, stages)
+        cpu, parity = oleg.finish()
     out = {"metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world, "steps": args.steps,
            "warmup": args.warmup, "ms_per_step": t_ms / args.steps, "higher_is_better": True, "scaling": "weak",
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
