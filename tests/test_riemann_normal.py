@@ -11,6 +11,7 @@ import pytest
 from helpers import rel_linf
 from m2c_gb300 import abi, inputfile as inf, problems
 from oracle import binding as ob
+from oracle import parity
 
 
 def _oracle_step(cfg, V, ID, phi, nsteps=1):
@@ -68,11 +69,20 @@ def test_gpu_matches_oracle(normal, nsteps, tol):
     c = s.run(nsteps)
     g = s.get_state()
     np.testing.assert_array_equal(g.ID, IDo)
-    e = rel_linf(g.V, Vo)
-    vmax = np.sqrt((Vo[:, 1:4] ** 2).sum(1)).max()
-    e[1:4] = np.abs(g.V[:, 1:4] - Vo[:, 1:4]).max(0) / vmax
-    assert np.all(e < tol), e
-    assert rel_linf(g.Phi, po) < tol
+    shape = (cfg.nz, cfg.ny, cfg.nx)
+    cmp = parity.compare(g.V, g.ID, g.Phi, Vo, IDo, po, shape)
+    # the yardstick: the oracle compiled with FMA contraction against the
+    # oracle (near-trivial interface problems follow the last bits of their
+    # inputs, in the reference's own numerics too)
+    of = ob.OracleSim(cfg, fma=True)
+    of.upload(V, ID, phi)
+    of.run(nsteps)
+    Vf, IDf, pf = of.download()
+    y = parity.compare(Vf, IDf, pf, Vo, IDo, po, shape)
+    for name in parity.NAMES:
+        bar = max(tol, 4 * y["rel_linf_velocity_magnitude"][name])
+        assert cmp["rel_linf_velocity_magnitude"][name] < bar, (name, cmp, y)
+    assert cmp["phi_rel_linf"] < tol
     assert c["riemann_solves"] == co["riemann_solves"]
     # with RK3, gradient normals turn some near-trivial problems (equal pressures, normal velocities
     # equal to rounding) into solves reported as not converged: the oracle 59 of 792 after one step,
