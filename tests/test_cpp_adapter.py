@@ -1,7 +1,8 @@
 """The C++ adapter (include/m2cg.hpp): a reference-shaped driver in C++
 (tests/cpp/adapter_check.cpp) compiled with g++ against libm2cg.so.  On the
 CPU it must compile, link and surface the library's error as m2cg::Error; on
-the GPU its results must equal the Python binding's for the same inputs."""
+the GPU its results must equal the Python binding's for the same inputs, and
+match the oracle (the residual to 1e-10, three steps to 1e-8)."""
 import os
 import shutil
 import subprocess
@@ -70,3 +71,15 @@ def test_gpu_adapter_matches_python_binding(tmp_path):
     rs = np.fromfile(o + "riemann.bin")
     assert rs[15] in (10.0, 0.0, 11.0) and np.all(np.isfinite(rs[:15]))   # err 0, id 0 or 1
     assert np.all(np.isfinite(np.fromfile(o + "flux.bin")))
+    # and the C++ driver's results against the oracle directly
+    from oracle import binding as ob
+    from oracle import parity
+    orc = ob.OracleSim(c)
+    orc.upload(V, ID, phi)
+    dto, cflo = orc.compute_dt()
+    assert abs(np.fromfile(o + "dt.bin")[0] - dto) <= 1e-14 * dto
+    assert np.all(parity.velocity_normalized(np.fromfile(o + "R.bin").reshape(-1, 5), orc.residual()) < 1e-10)
+    orc.run(3)
+    Vo, IDo, pho = orc.download()
+    np.testing.assert_array_equal(np.fromfile(o + "ID.bin", np.int32), IDo)
+    assert np.all(parity.velocity_normalized(np.fromfile(o + "V.bin").reshape(-1, 5), Vo) < 1e-8)

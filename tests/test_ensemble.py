@@ -54,6 +54,18 @@ def test_ensemble_matches_members_run_alone(normal):
             assert ca[k] == cb[k], (i, k, ca[k], cb[k])
         assert cb["riemann_solves"] > 0
         solo.close()
+    # and every member against the oracle directly
+    from oracle import binding as ob
+    from oracle import parity
+    for i, (c, V, ID, phi) in enumerate(doms):
+        o = ob.OracleSim(c)
+        o.upload(V, ID, phi)
+        o.run(6)
+        Vo, IDo, po = o.download()
+        a = ens.member(i).get_state()
+        np.testing.assert_array_equal(a.ID, IDo)
+        assert np.all(parity.velocity_normalized(a.V, Vo) < 1e-8), i
+        assert parity.rel_linf(a.Phi, po) < 1e-8, i
     assert ens.kernel_launches() > 0
     ens.close()
     seq.close()
