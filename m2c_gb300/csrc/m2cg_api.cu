@@ -154,7 +154,12 @@ struct m2cg_ctx {
   cudaEvent_t ev[16] = {};
   int64_t launches = 0;
   int64_t launches_per_step = 0;
+  int64_t launches_per_adv = 0;
   cudaGraphExec_t graph_exec = nullptr;
+  // m2cg_advance's step with the caller's dt: captured once, the dt written to
+  // sc->dt_in from a pinned host slot before each replay
+  cudaGraphExec_t adv_exec = nullptr;
+  double* h_dt = nullptr;
   // level-set reinitialization: sub-stage states, backup, sign, first-layer
   // tags, device loop state and the two loop graphs (gated on the step
   // number for the stepping, ungated for m2cg_reinitialize)
@@ -681,6 +686,8 @@ void m2cg_destroy(m2cg_ctx* x) {
   if (!x) return;
   if (x->stream) cudaStreamSynchronize(x->stream);
   if (x->graph_exec) cudaGraphExecDestroy(x->graph_exec);
+  if (x->adv_exec) cudaGraphExecDestroy(x->adv_exec);
+  if (x->h_dt) cudaFreeHost(x->h_dt);
   if (x->ri_gated) cudaGraphExecDestroy(x->ri_gated);
   if (x->ri_now) cudaGraphExecDestroy(x->ri_now);
   if (x->ri_unres) cudaGraphExecDestroy(x->ri_unres);
@@ -871,7 +878,21 @@ m2cg_status m2cg_levelset_residual(m2cg_ctx* x, double* Rphi) {
 
 m2cg_status m2cg_advance(m2cg_ctx* x, double dt) {
   if (!x || !(dt > 0)) { set_err("bad argument"); return M2CG_ERR_INVALID_ARG; }
-  x->launches += enqueue_step(x, 2, dt);
+  cudaStream_t s = x->stream;
+  if (!x->adv_exec) {   // the step with the given dt, captured once and replayed like m2cg_run's
+    if (!x->h_dt) CK(cudaHostAlloc((void**)&x->h_dt, sizeof(double), cudaHostAllocDefault));
+    cudaGraph_t g;
+    CK(cudaStreamBeginCapture(s, cudaStreamCaptureModeThreadLocal));
+    x->launches_per_adv = enqueue_step(x, 3, 0.0);
+    CK(cudaStreamEndCapture(s, &g));
+    CK(cudaGraphInstantiate(&x->adv_exec, g, cudaGraphInstantiateFlagUseNodePriority));
+    cudaGraphDestroy(g);
+  }
+  CK(cudaStreamSynchronize(s));   // the pinned slot may still feed the previous call's copy
+  *x->h_dt = dt;
+  CK(cudaMemcpyAsync(&x->sc->dt_in, x->h_dt, sizeof(double), cudaMemcpyHostToDevice, s));
+  CK(cudaGraphLaunch(x->adv_exec, s));
+  x->launches += x->launches_per_adv;
   int64_t ri = 0;
   if (x->ri_gated) {   // the graph's gate checks the step number on the device
     CK(cudaGraphLaunch(x->ri_gated, x->stream));
@@ -1048,6 +1069,10 @@ m2cg_status m2cg_set_warm_start(m2cg_ctx* x, m2cg_mlp* m) {
   if (x->graph_exec) {  // the step graph is captured again on the next m2cg_run
     cudaGraphExecDestroy(x->graph_exec);
     x->graph_exec = nullptr;
+  }
+  if (x->adv_exec) {
+    cudaGraphExecDestroy(x->adv_exec);
+    x->adv_exec = nullptr;
   }
   return M2CG_OK;
 }
@@ -1342,6 +1367,7 @@ struct m2cg_ensemble {
   bool building = false;   // first pass: fill the tables; second pass (captured): launch
   cudaGraphExec_t graph = nullptr;
   int64_t launches_per_step = 0;
+  int64_t launches_per_adv = 0;
   int64_t launches = 0;
 
   template <class T>

@@ -87,6 +87,7 @@ struct DevScalars {
   int active;       // 0 once MaxTime has been reached
   int pad;
   long long steps;
+  double dt_in;     // the time step a caller gave m2cg_advance (its step graph reads it here)
 };
 
 struct Params {

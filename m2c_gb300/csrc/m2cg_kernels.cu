@@ -782,6 +782,7 @@ __device__ __forceinline__ void k_dt_finalize_body(const Params& P, DevScalars* 
   sc->min_dx_over_lambda = 0x7fefffffffffffffull;  // DBL_MAX for the next reduction
   double dt, cfl;
   if (mode == 2) { dt = fixed_dt; cfl = dt / m; }
+  else if (mode == 3) { dt = sc->dt_in; cfl = dt / m; }   // mode 2 with the step given on the device
   else if (P.timestep > 0) { dt = P.timestep; cfl = dt / m; }
   else { cfl = P.cfl; dt = cfl * m; }
   if (mode == 0) { sc->dt = dt; sc->cfl = cfl; return; }

@@ -159,7 +159,7 @@ class OracleSim:
         return t
 
 
-def riemann_batch(cfg, Vm, idm, Vp, idp, dirs, warm_p=None):
+def riemann_batch(cfg, Vm, idm, Vp, idp, dirs, warm_p=None, fma=False):
     n = len(idm)
     Vm = np.ascontiguousarray(Vm, np.float64); Vp = np.ascontiguousarray(Vp, np.float64)
     idm = np.ascontiguousarray(idm, np.int32); idp = np.ascontiguousarray(idp, np.int32)
@@ -167,7 +167,7 @@ def riemann_batch(cfg, Vm, idm, Vp, idp, dirs, warm_p=None):
     Vs, Vsm, Vsp = np.zeros((n, 5)), np.zeros((n, 5)), np.zeros((n, 5))
     oid, it, err = np.zeros(n, np.int32), np.zeros(n, np.int32), np.zeros(n, np.int32)
     w = None if warm_p is None else np.ascontiguousarray(warm_p, np.float64)
-    lib().orc_riemann_batch(C.byref(cfg), n, dptr(Vm), iptr(idm), dptr(Vp), iptr(idp), dptr(dirs), dptr(Vs), iptr(oid),
+    lib(fma).orc_riemann_batch(C.byref(cfg), n, dptr(Vm), iptr(idm), dptr(Vp), iptr(idp), dptr(dirs), dptr(Vs), iptr(oid),
                             dptr(Vsm), dptr(Vsp), iptr(it), iptr(err), dptr(w))
     return dict(Vs=Vs, id=oid, Vsm=Vsm, Vsp=Vsp, iters=it, err=err)
 

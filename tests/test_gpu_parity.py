@@ -67,17 +67,41 @@ def test_riemann_random_batch_matches_oracle():
     dirs[np.arange(n), rng.integers(0, 3, n)] = 1.0
     g = Solver(cfg).riemann_batch(Vm, idm, Vp, idp, dirs)
     o = ob.riemann_batch(cfg, Vm, idm, Vp, idp, dirs)
+    f = ob.riemann_batch(cfg, Vm, idm, Vp, idp, dirs, fma=True)
     np.testing.assert_array_equal(g["err"], o["err"])
     ok = o["err"] == 0
     assert ok.mean() > 0.95
     np.testing.assert_array_equal(g["id"][ok], o["id"][ok])
-    # same algorithm in binary64 without contraction on both sides: agreement
-    # is at rounding level except where a pow() ulp moves an adaptive step
-    for k in ("Vsm", "Vsp"):
-        r = np.abs(g[k][ok] - o[k][ok]) / np.maximum(np.abs(o[k][ok]), 1e-300)
-        assert np.quantile(r[:, 4], 0.99) < 1e-11
-        assert (r[:, [0, 4]] > 1e-10).mean() < 0.002
-    assert (np.abs(g["iters"][ok] - o["iters"][ok]) <= 2).mean() > 0.99
+    # Per problem, each star-state component is compared on the scale of the
+    # problem's inputs (rho and p: the larger input value; velocity: the
+    # largest input speed): a near-vacuum star state (p* ~ 1e-8 Pa between
+    # states at 1e5 Pa) is fixed only to that absolute scale.  Agreement is
+    # judged against the reference's own rounding sensitivity: the oracle
+    # compiled with fused multiply-adds.  The main loop stops at a 1e-10
+    # relative mismatch and the rarefaction integrator's adaptive steps follow
+    # pow() of their error estimates, so one rounding step (a pow() ulp, a
+    # contracted multiply-add) that moves a step or the stopping iteration
+    # moves the answer within the integrator's error bar.  At every threshold
+    # the GPU must have no more problems beyond it than that second
+    # compilation of the reference's arithmetic.
+    sc = np.maximum(np.abs(Vm), np.abs(Vp))
+    sc[:, 1:4] = sc[:, 1:4].max(1, keepdims=True)
+
+    def dist(a):
+        e = np.zeros(len(sc))
+        for k in ("Vsm", "Vsp"):
+            e = np.maximum(e, (np.abs(a[k] - o[k]) / sc).max(1))
+        return e[ok & (a["err"] == 0)]
+
+    eg, ef = dist(g), dist(f)
+    st = {"q99": (np.quantile(eg, 0.99), np.quantile(ef, 0.99)), "max": (eg.max(), ef.max()),
+          "iters differ": ((g["iters"][ok] != o["iters"][ok]).sum(), (f["iters"][ok] != o["iters"][ok]).sum())}
+    for t in (1e-14, 1e-12, 1e-10, 1e-8, 1e-6):
+        st[">%g" % t] = ((eg > t).sum(), (ef > t).sum())
+        assert st[">%g" % t][0] <= st[">%g" % t][1], st
+    assert st["q99"][0] <= max(st["q99"][1], 1e-12), st
+    assert st["max"][0] <= max(st["max"][1], 1e-10), st
+    assert st["iters differ"][0] <= st["iters differ"][1], st
 
 
 @pytest.mark.parametrize("flux", [abi.FLUX_HLLC, abi.FLUX_LLF, abi.FLUX_ROE])
