@@ -451,6 +451,17 @@ int64_t     m2cg_kernel_launches(m2cg_ctx* ctx);
  * ms (optional) receives the timed kernel's duration.  The FP64-pipe roofline's
  * denominator. */
 m2cg_status m2cg_fp64_peak(int32_t iters, double* dfma_per_s, float* ms);
+/* No reference counterpart (self-check of the device solver's arithmetic): the
+ * exact interface Riemann solver divides several numerators by one divisor
+ * through a shared, correctly rounded reciprocal (Markstein's method), which
+ * must give IEEE a / b bit for bit.  This runs that code on n (1 .. 2^36)
+ * operand pairs drawn from `seed` -- random bit patterns, wide and physical
+ * exponent ranges, all-ones significands, zeros, subnormals, infinities, NaNs,
+ * exponent-limit quotients, exact quotients -- and compares each quotient with
+ * a / b and each reciprocal it forms with 1 / b.  mismatches receives the number
+ * of differing results (0 expected); fast (optional) the number of quotients
+ * that took the shared-reciprocal path rather than the IEEE fallback. */
+m2cg_status m2cg_selftest_quotient(int64_t n, uint64_t seed, int64_t* mismatches, int64_t* fast);
 /* Page-locked host memory for fast upload / download (NULL on failure). */
 void*       m2cg_host_alloc(size_t bytes);
 void        m2cg_host_free(void* ptr);

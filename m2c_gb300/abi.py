@@ -200,6 +200,7 @@ def load(path=None):
         "m2cg_get_counters": (C.c_int, [_P, C.POINTER(Counters)]),
         "m2cg_reinitialize": (C.c_int, [_P, C.POINTER(ReinitStats)]),
         "m2cg_fp64_peak": (C.c_int, [C.c_int32, _D, C.POINTER(C.c_float)]),
+        "m2cg_selftest_quotient": (C.c_int, [C.c_int64, C.c_uint64, C.POINTER(C.c_int64), C.POINTER(C.c_int64)]),
         "m2cg_download_ghosted": (C.c_int, [_P, _D, _I, _D]),
         "m2cg_sample_points": (C.c_int, [_P, C.c_int32, _D, _D]),
         "m2cg_integrate": (C.c_int, [_P, _D, _D]),

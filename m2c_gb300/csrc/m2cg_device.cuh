@@ -64,6 +64,52 @@ M2CG_DEV double rsqrt_fast(double x) {
   return fma(y * e, fma(e, 0.375, 0.5), y);
 }
 
+// Correctly rounded quotients a / b for several numerators over one divisor,
+// after P. Markstein, "Computation of elementary functions on the IBM RISC
+// System/6000 processor", IBM J. Res. Dev. 34(1), 1990 (theorems restated in
+// Muller et al., Handbook of Floating-Point Arithmetic, ch. on division with
+// an FMA).  In round-to-nearest binary64 without underflow or overflow:
+//   (1) if y1 is within one ulp of 1/b and the significand of b is not all
+//       ones, y = y1 + y1 (1 - b y1) (two FMAs) is RN(1/b);
+//   (2) if y = RN(1/b) and q is within one ulp of a/b, the remainder
+//       a - b q is exact in one FMA and q + (a - b q) y rounds to RN(a/b).
+// q0 = RN(a y) can be 1.5 ulp off, so one remainder step brings it within
+// half an ulp first: five FP64 operations per quotient against the ~9 of a
+// full division, which pays from the second quotient of a divisor on
+// (measured on GB300, one dependent chain: 590 cycles for a / b, 321 for the
+// five operations, 372 for y).  Operands outside the range where the theorems
+// hold -- zero, subnormal, infinite or NaN operands, quotients near the
+// exponent limits, divisors with an all-ones significand -- take the IEEE
+// division instead, so every result equals a / b bit for bit
+// (m2cg_selftest_quotient checks that on random and edge-case operands).
+struct Quot {
+  double b, y;
+  bool fast;
+};
+M2CG_DEV int exp_field(double x) { return (int)((bits(x) >> 52) & 0x7ff); }
+M2CG_DEV Quot quot_of(double b) {
+  Quot q;
+  q.b = b;
+  const int eb = exp_field(b);
+  q.fast = (unsigned)(eb - 128) <= 1792u && (bits(b) & 0xfffffffffffffll) != 0xfffffffffffffll;
+  q.y = 0.0;
+  if (q.fast) {
+    const double y1 = rcp_fast(b);
+    q.y = fma(fma(-b, y1, 1.0), y1, y1);
+  }
+  return q;
+}
+// the IEEE division out of line: one copy of its code however many quotients
+// fall back, which keeps the solver's hot loops small in the instruction cache
+static __device__ __noinline__ double ieee_div(double a, double b) { return a / b; }
+M2CG_DEV double qdiv(double a, const Quot& d) {
+  const int ea = exp_field(a), eq = ea - exp_field(d.b) + 1023;
+  if (!d.fast || (unsigned)(ea - 128) > 1792u || (unsigned)(eq - 128) > 1792u) return ieee_div(a, d.b);
+  double q = __dmul_rn(a, d.y);
+  q = fma(fma(-d.b, q, a), d.y, q);
+  return fma(fma(-d.b, q, a), d.y, q);
+}
+
 // ---- equation of state ----------------------------------------------------
 M2CG_DEV double eos_p(const DevMat& M, double rho, double e) {
   if (M.type == M2CG_EOS_SG) return M.gam1 * rho * e - M.gam * M.Pstiff;
@@ -92,6 +138,10 @@ M2CG_DEV double eos_Gamma(const DevMat& M, double rho) {
 // VarFcnBase.h:219-223
 M2CG_DEV double eos_c2(const DevMat& M, double rho, double e) {
   return eos_dpdrho(M, rho, e) + eos_p(M, rho, e) / rho * eos_Gamma(M, rho);
+}
+// eos_c2 with its division by rho through a reciprocal the caller shares (same bits)
+M2CG_DEV double eos_c2_q(const DevMat& M, double rho, const Quot& R, double e) {
+  return eos_dpdrho(M, rho, e) + qdiv(eos_p(M, rho, e), R) * eos_Gamma(M, rho);
 }
 // CheckState: true = nonphysical (VarFcnSG.h:96-108, VarFcnNASG.h:73-85, VarFcnBase.h:120-140)
 M2CG_DEV bool eos_bad(const DevMat& M, double rho, double p) {
