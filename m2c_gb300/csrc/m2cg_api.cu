@@ -201,6 +201,18 @@ m2cg_status m2cg_fill_params(const m2cg_config& c, m2cg::Params& P) {
   g.px = c.nx + 2; g.py = c.ny + 2; g.pz = c.nz + 2;
   g.sy = g.px; g.sz = (int64_t)g.px * g.py; g.ntot = g.sz * g.pz;
   g.dx = (c.xmax - c.x0) / c.nx; g.dy = (c.ymax - c.y0) / c.ny; g.dz = (c.zmax - c.z0) / c.nz;
+  {
+    const int n[3] = {g.nx, g.ny, g.nz};
+    const double h[3] = {g.dx, g.dy, g.dz};
+    bool same = true;
+    g.h_common = 0.0;
+    for (int d = 0; d < 3; d++)
+      if (n[d] > 1) {
+        if (g.h_common == 0.0) g.h_common = h[d];
+        else same = same && h[d] == g.h_common;
+      }
+    if (!same) g.h_common = 0.0;
+  }
   P.n_mat = c.n_materials;
   for (int m = 0; m < c.n_materials; m++) {
     const m2cg_material& s = c.mat[m];

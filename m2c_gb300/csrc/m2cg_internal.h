@@ -16,6 +16,7 @@ struct Grid {
   int px, py, pz;
   int64_t sy, sz, ntot;  // sx = 1
   double dx, dy, dz;
+  double h_common;   // the spacing shared by every axis with more than one cell, 0 if they differ
   // Block shape of the cell and face kernels: tile[0] x tile[1] x tile[2] cells
   // per block of 128 threads (x fastest), or all zero: 128 consecutive cells of
   // the x-fastest order.  Set per ensemble member by the tile autotuner.

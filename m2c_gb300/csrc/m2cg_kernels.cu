@@ -747,9 +747,19 @@ __device__ __forceinline__ void k_dt_reduce_body(const Params& P, const StateSet
     Side sd;
     side_eos(M, V, 0, sd);
     double cc = sd.c;
-    if (g.nx > 1) m = fmin(m, g.dx * rcp_fast(fabs(V[1]) + cc));
-    if (g.ny > 1) m = fmin(m, g.dy * rcp_fast(fabs(V[2]) + cc));
-    if (g.nz > 1) m = fmin(m, g.dz * rcp_fast(fabs(V[3]) + cc));
+    if (g.h_common > 0.0) {
+      // one spacing on every active axis: min_d h / (|u_d| + c) = h / (max_d |u_d| + c),
+      // one reciprocal instead of three
+      double v = 0.0;
+      if (g.nx > 1) v = fabs(V[1]);
+      if (g.ny > 1) v = fmax(v, fabs(V[2]));
+      if (g.nz > 1) v = fmax(v, fabs(V[3]));
+      m = g.h_common * rcp_fast(v + cc);
+    } else {
+      if (g.nx > 1) m = fmin(m, g.dx * rcp_fast(fabs(V[1]) + cc));
+      if (g.ny > 1) m = fmin(m, g.dy * rcp_fast(fabs(V[2]) + cc));
+      if (g.nz > 1) m = fmin(m, g.dz * rcp_fast(fabs(V[3]) + cc));
+    }
   }
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) m = fmin(m, __shfl_xor_sync(0xffffffffu, m, o));
