@@ -109,6 +109,29 @@ M2CG_DEV double qdiv(double a, const Quot& d) {
   q = fma(fma(-d.b, q, a), d.y, q);
   return fma(fma(-d.b, q, a), d.y, q);
 }
+// 1 / b from the same divisor: y itself is RN(1/b)
+M2CG_DEV double qrcp(const Quot& d) { return d.fast ? d.y : ieee_div(1.0, d.b); }
+// The same calls with Shared = false are plain IEEE divisions.  The shared
+// reciprocal shortens a dependent chain (a lone solve on an otherwise idle
+// FP64 pipe) but issues a few more FP64-pipe slots per divisor than the
+// divisions it replaces, so code whose pipe is full (a warp of independent
+// solves per lane) keeps the divisions.  Both give the same bits.
+template <bool Shared> M2CG_DEV Quot quot_of_t(double b) {
+  if constexpr (Shared) return quot_of(b);
+  Quot q;
+  q.b = b;
+  q.y = 0.0;
+  q.fast = false;
+  return q;
+}
+template <bool Shared> M2CG_DEV double qdiv_t(double a, const Quot& d) {
+  if constexpr (Shared) return qdiv(a, d);
+  return a / d.b;
+}
+template <bool Shared> M2CG_DEV double qrcp_t(const Quot& d) {
+  if constexpr (Shared) return qrcp(d);
+  return 1.0 / d.b;
+}
 
 // ---- equation of state ----------------------------------------------------
 M2CG_DEV double eos_p(const DevMat& M, double rho, double e) {
@@ -140,8 +163,8 @@ M2CG_DEV double eos_c2(const DevMat& M, double rho, double e) {
   return eos_dpdrho(M, rho, e) + eos_p(M, rho, e) / rho * eos_Gamma(M, rho);
 }
 // eos_c2 with its division by rho through a reciprocal the caller shares (same bits)
-M2CG_DEV double eos_c2_q(const DevMat& M, double rho, const Quot& R, double e) {
-  return eos_dpdrho(M, rho, e) + qdiv(eos_p(M, rho, e), R) * eos_Gamma(M, rho);
+template <bool Shared> M2CG_DEV double eos_c2_q(const DevMat& M, double rho, const Quot& R, double e) {
+  return eos_dpdrho(M, rho, e) + qdiv_t<Shared>(eos_p(M, rho, e), R) * eos_Gamma(M, rho);
 }
 // CheckState: true = nonphysical (VarFcnSG.h:96-108, VarFcnNASG.h:73-85, VarFcnBase.h:120-140)
 M2CG_DEV bool eos_bad(const DevMat& M, double rho, double p) {

@@ -62,7 +62,11 @@ struct PathCache {
   }
 };
 
-struct ExactRiemannDev {
+// SharedDiv: the Cash-Karp and RK4 steps form each repeated divisor's
+// reciprocal once (qdiv), for the latency-bound solves of the finite-volume
+// step; false keeps the IEEE divisions (batched independent problems).
+template <bool SharedDiv>
+struct ExactRiemannDevT {
   const Mats* mats;
   RiemannPrm P;
   PathCache path1, path3;
@@ -100,59 +104,59 @@ struct ExactRiemannDev {
                      double& rho, double& u, double& p, double& xi, double& uErr, double& rhoErr) const {
     dp = -dp;
     double e_0 = eos_e(M, rho_0, p_0);
-    const Quot R0 = quot_of(rho_0);
-    double c_0_square = eos_c2_q(M, rho_0, R0, e_0);
+    const Quot R0 = quot_of_t<SharedDiv>(rho_0);
+    double c_0_square = eos_c2_q<SharedDiv>(M, rho_0, R0, e_0);
     if (rho_0 <= 0 || c_0_square < 0) return false;
     double c_0 = sqrt(c_0_square);
-    const Quot C0 = quot_of(c_0_square);
-    double rho_1 = rho_0 + qdiv(0.2 * dp, C0);
+    const Quot C0 = quot_of_t<SharedDiv>(c_0_square);
+    double rho_1 = rho_0 + qdiv_t<SharedDiv>(0.2 * dp, C0);
     double p_1 = p_0 + 0.2 * dp;
     double e_1 = eos_e(M, rho_1, p_1);
     double c_1_square = eos_c2(M, rho_1, e_1);
     if (rho_1 <= 0 || c_1_square < 0) return false;
-    const Quot C1 = quot_of(c_1_square);
-    double rho_2 = rho_0 + qdiv(3. / 40. * dp, C0) + qdiv(9. / 40. * dp, C1);
+    const Quot C1 = quot_of_t<SharedDiv>(c_1_square);
+    double rho_2 = rho_0 + qdiv_t<SharedDiv>(3. / 40. * dp, C0) + qdiv_t<SharedDiv>(9. / 40. * dp, C1);
     double p_2 = p_1 + 3. / 10. * dp;
     double e_2 = eos_e(M, rho_2, p_2);
-    const Quot R2 = quot_of(rho_2);
-    double c_2_square = eos_c2_q(M, rho_2, R2, e_2);
+    const Quot R2 = quot_of_t<SharedDiv>(rho_2);
+    double c_2_square = eos_c2_q<SharedDiv>(M, rho_2, R2, e_2);
     if (rho_2 <= 0 || c_2_square < 0) return false;
     double c_2 = sqrt(c_2_square);
-    const Quot C2 = quot_of(c_2_square);
-    double rho_3 = rho_0 + qdiv(3. / 10. * dp, C0) - qdiv(9. / 10. * dp, C1) + qdiv(6. / 5. * dp, C2);
+    const Quot C2 = quot_of_t<SharedDiv>(c_2_square);
+    double rho_3 = rho_0 + qdiv_t<SharedDiv>(3. / 10. * dp, C0) - qdiv_t<SharedDiv>(9. / 10. * dp, C1) + qdiv_t<SharedDiv>(6. / 5. * dp, C2);
     double p_3 = p_0 + 3. / 5. * dp;
     double e_3 = eos_e(M, rho_3, p_3);
-    const Quot R3 = quot_of(rho_3);
-    double c_3_square = eos_c2_q(M, rho_3, R3, e_3);
+    const Quot R3 = quot_of_t<SharedDiv>(rho_3);
+    double c_3_square = eos_c2_q<SharedDiv>(M, rho_3, R3, e_3);
     if (rho_3 <= 0 || c_3_square < 0) return false;
     double c_3 = sqrt(c_3_square);
-    const Quot C3 = quot_of(c_3_square);
-    double rho_4 = rho_0 - qdiv(11. / 54. * dp, C0) + qdiv(2.5 * dp, C1) - qdiv(70. / 27. * dp, C2) +
-                   qdiv(35. / 27. * dp, C3);
+    const Quot C3 = quot_of_t<SharedDiv>(c_3_square);
+    double rho_4 = rho_0 - qdiv_t<SharedDiv>(11. / 54. * dp, C0) + qdiv_t<SharedDiv>(2.5 * dp, C1) - qdiv_t<SharedDiv>(70. / 27. * dp, C2) +
+                   qdiv_t<SharedDiv>(35. / 27. * dp, C3);
     double p_4 = p_0 + dp;
     double e_4 = eos_e(M, rho_4, p_4);
-    const Quot R4 = quot_of(rho_4);
-    double c_4_square = eos_c2_q(M, rho_4, R4, e_4);
+    const Quot R4 = quot_of_t<SharedDiv>(rho_4);
+    double c_4_square = eos_c2_q<SharedDiv>(M, rho_4, R4, e_4);
     if (rho_4 <= 0 || c_4_square < 0) return false;
     double c_4 = sqrt(c_4_square);
-    const Quot C4 = quot_of(c_4_square);
-    double rho_5 = rho_0 + qdiv(1631. / 55296. * dp, C0) + qdiv(175. / 512. * dp, C1) +
-                   qdiv(575. / 13824. * dp, C2) + qdiv(44275. / 110592. * dp, C3) + qdiv(253. / 4096. * dp, C4);
+    const Quot C4 = quot_of_t<SharedDiv>(c_4_square);
+    double rho_5 = rho_0 + qdiv_t<SharedDiv>(1631. / 55296. * dp, C0) + qdiv_t<SharedDiv>(175. / 512. * dp, C1) +
+                   qdiv_t<SharedDiv>(575. / 13824. * dp, C2) + qdiv_t<SharedDiv>(44275. / 110592. * dp, C3) + qdiv_t<SharedDiv>(253. / 4096. * dp, C4);
     double p_5 = p_0 + 7. / 8. * dp;
     double e_5 = eos_e(M, rho_5, p_5);
-    const Quot R5 = quot_of(rho_5);
-    double c_5_square = eos_c2_q(M, rho_5, R5, e_5);
+    const Quot R5 = quot_of_t<SharedDiv>(rho_5);
+    double c_5_square = eos_c2_q<SharedDiv>(M, rho_5, R5, e_5);
     if (rho_5 <= 0 || c_5_square < 0) return false;
     double c_5 = sqrt(c_5_square);
-    const Quot C5 = quot_of(c_5_square);
-    double drho = (qdiv(37. / 378., C0) + qdiv(250. / 621., C2) + qdiv(125. / 594., C3) + qdiv(512. / 1771., C5)) * dp;
-    double drho_err = (qdiv(2825. / 27648., C0) + qdiv(18575. / 48384., C2) + qdiv(13525. / 55296., C3) +
-                       qdiv(277. / 14336., C4) + qdiv(0.25, C5)) * dp;
-    const Quot S0 = quot_of(c_0), S2 = quot_of(c_2), S3 = quot_of(c_3), S5 = quot_of(c_5);
-    double du = (qdiv(qdiv(37. / 378., S0), R0) + qdiv(qdiv(250. / 621., S2), R2) + qdiv(qdiv(125. / 594., S3), R3) +
-                 qdiv(qdiv(512. / 1771., S5), R5)) * dp;
-    double du_err = (qdiv(qdiv(2825. / 27648., S0), R0) + qdiv(qdiv(18575. / 48384., S2), R2) +
-                     qdiv(qdiv(13525. / 55296., S3), R3) + qdiv(277. / 14336. / c_4, R4) + qdiv(qdiv(0.25, S5), R5)) * dp;
+    const Quot C5 = quot_of_t<SharedDiv>(c_5_square);
+    double drho = (qdiv_t<SharedDiv>(37. / 378., C0) + qdiv_t<SharedDiv>(250. / 621., C2) + qdiv_t<SharedDiv>(125. / 594., C3) + qdiv_t<SharedDiv>(512. / 1771., C5)) * dp;
+    double drho_err = (qdiv_t<SharedDiv>(2825. / 27648., C0) + qdiv_t<SharedDiv>(18575. / 48384., C2) + qdiv_t<SharedDiv>(13525. / 55296., C3) +
+                       qdiv_t<SharedDiv>(277. / 14336., C4) + qdiv_t<SharedDiv>(0.25, C5)) * dp;
+    const Quot S0 = quot_of_t<SharedDiv>(c_0), S2 = quot_of_t<SharedDiv>(c_2), S3 = quot_of_t<SharedDiv>(c_3), S5 = quot_of_t<SharedDiv>(c_5);
+    double du = (qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(37. / 378., S0), R0) + qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(250. / 621., S2), R2) + qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(125. / 594., S3), R3) +
+                 qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(512. / 1771., S5), R5)) * dp;
+    double du_err = (qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(2825. / 27648., S0), R0) + qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(18575. / 48384., S2), R2) +
+                     qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(13525. / 55296., S3), R3) + qdiv_t<SharedDiv>(277. / 14336. / c_4, R4) + qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(0.25, S5), R5)) * dp;
     if (isnan(du) || isnan(du_err)) return false;
     rhoErr = fabs(drho_err - drho);
     uErr = fabs(du_err - du);
@@ -173,37 +177,37 @@ struct ExactRiemannDev {
                                    double& rho, double& u, double& p, double& xi) const {
     dp = -dp;
     double e_0 = eos_e(M, rho_0, p_0);
-    const Quot R0 = quot_of(rho_0);
-    double c_0_square = eos_c2_q(M, rho_0, R0, e_0);
+    const Quot R0 = quot_of_t<SharedDiv>(rho_0);
+    double c_0_square = eos_c2_q<SharedDiv>(M, rho_0, R0, e_0);
     if (rho_0 <= 0 || c_0_square < 0) return false;
     double c_0 = sqrt(c_0_square);
-    const Quot C0 = quot_of(c_0_square);
-    double rho_1 = rho_0 + qdiv(0.5 * dp, C0);
+    const Quot C0 = quot_of_t<SharedDiv>(c_0_square);
+    double rho_1 = rho_0 + qdiv_t<SharedDiv>(0.5 * dp, C0);
     double p_1 = p_0 + 0.5 * dp;
     double e_1 = eos_e(M, rho_1, p_1);
-    const Quot R1 = quot_of(rho_1);
-    double c_1_square = eos_c2_q(M, rho_1, R1, e_1);
+    const Quot R1 = quot_of_t<SharedDiv>(rho_1);
+    double c_1_square = eos_c2_q<SharedDiv>(M, rho_1, R1, e_1);
     if (rho_1 <= 0 || c_1_square < 0) return false;
     double c_1 = sqrt(c_1_square);
-    const Quot C1 = quot_of(c_1_square);
-    double rho_2 = rho_0 + qdiv(0.5 * dp, C1);
+    const Quot C1 = quot_of_t<SharedDiv>(c_1_square);
+    double rho_2 = rho_0 + qdiv_t<SharedDiv>(0.5 * dp, C1);
     double p_2 = p_1;
     double e_2 = eos_e(M, rho_2, p_2);
-    const Quot R2 = quot_of(rho_2);
-    double c_2_square = eos_c2_q(M, rho_2, R2, e_2);
+    const Quot R2 = quot_of_t<SharedDiv>(rho_2);
+    double c_2_square = eos_c2_q<SharedDiv>(M, rho_2, R2, e_2);
     if (rho_2 <= 0 || c_2_square < 0) return false;
     double c_2 = sqrt(c_2_square);
-    const Quot C2 = quot_of(c_2_square);
-    double rho_3 = rho_0 + qdiv(dp, C2);
+    const Quot C2 = quot_of_t<SharedDiv>(c_2_square);
+    double rho_3 = rho_0 + qdiv_t<SharedDiv>(dp, C2);
     double p_3 = p_0 + dp;
     double e_3 = eos_e(M, rho_3, p_3);
-    const Quot R3 = quot_of(rho_3);
-    double c_3_square = eos_c2_q(M, rho_3, R3, e_3);
+    const Quot R3 = quot_of_t<SharedDiv>(rho_3);
+    double c_3_square = eos_c2_q<SharedDiv>(M, rho_3, R3, e_3);
     if (rho_3 <= 0 || c_3_square < 0) return false;
     double c_3 = sqrt(c_3_square);
-    double drho = 1.0 / 6.0 * dp * (qdiv(1., C0) + 2.0 * (qdiv(1., C1) + qdiv(1., C2)) + 1. / c_3_square);
+    double drho = 1.0 / 6.0 * dp * (qrcp_t<SharedDiv>(C0) + 2.0 * (qrcp_t<SharedDiv>(C1) + qrcp_t<SharedDiv>(C2)) + 1. / c_3_square);
     double du = 1.0 / 6.0 * dp *
-                (qdiv(1. / c_0, R0) + 2.0 * (qdiv(1. / c_1, R1) + qdiv(1. / c_2, R2)) + qdiv(1. / c_3, R3));
+                (qdiv_t<SharedDiv>(1. / c_0, R0) + 2.0 * (qdiv_t<SharedDiv>(1. / c_1, R1) + qdiv_t<SharedDiv>(1. / c_2, R2)) + qdiv_t<SharedDiv>(1. / c_3, R3));
     if (isnan(du)) return false;
     rho = rho_0 + drho;
     p = p_0 + dp;
@@ -764,5 +768,7 @@ struct ExactRiemannDev {
     return (iter == P.maxIts_main) ? 1 : 0;
   }
 };
+using ExactRiemannDev = ExactRiemannDevT<false>;
+using ExactRiemannChainDev = ExactRiemannDevT<true>;
 
 }  // namespace m2cg

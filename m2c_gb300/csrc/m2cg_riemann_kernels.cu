@@ -64,7 +64,8 @@ __device__ __forceinline__ int iface_finish(const Params& P, const IfaceList& L,
   return bad;
 }
 
-__device__ __forceinline__ void init_solver(ExactRiemannDev& rs, const Mats* md, const RiemannPrm& rp, double* scratch,
+template <class Solver>
+__device__ __forceinline__ void init_solver(Solver& rs, const Mats* md, const RiemannPrm& rp, double* scratch,
                                             int path_cap, int64_t tid, int64_t T) {
   rs.mats = md;
   rs.P = rp;
@@ -145,7 +146,7 @@ __device__ __forceinline__ void riemann_normal_dir(const Params& P, int64_t c, i
 // anything when the solver's evaluation budget ran out.
 __device__ __forceinline__ int iface_solve(const Params& P, StateSet S, const int32_t* __restrict__ id,
                                            double* const* fs, const IfaceList& L, int store, const float* warm,
-                                           int64_t s, ExactRiemannDev& rs, unsigned long long (&acc)[6]) {
+                                           int64_t s, ExactRiemannChainDev& rs, unsigned long long (&acc)[6]) {
   int d, idm, idp;
   int64_t c;
   double Vm[5], Vp[5];
@@ -200,7 +201,7 @@ __global__ void k_riemann_interfaces(Params P, const Mats* __restrict__ md, Stat
   int64_t n = (int64_t)min((unsigned long long)L.cap, *L.count);
   int64_t T = (int64_t)gridDim.x * blockDim.x;
   int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  ExactRiemannDev rs;
+  ExactRiemannChainDev rs;
   init_solver(rs, md, P.rp, scratch, path_cap, tid, T);
   rs.eval_limit = eval_limit;
   if (tid == 0) atomicAdd(&cnt[CNT_IFACE], (unsigned long long)n);
@@ -254,7 +255,7 @@ __global__ void __launch_bounds__(128) k_riemann_stragglers(Params P, const Mats
   const int64_t lane = threadIdx.x & 31;
   int64_t T = (int64_t)gridDim.x * blockDim.x;
   int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  ExactRiemannDev rs;
+  ExactRiemannChainDev rs;
   init_solver(rs, md, P.rp, scratch, path_cap, tid, T);
   const size_t per_warp = (size_t)6 * path_cap;  // doubles: two waves x cap entries x {p, rho, u}
   if (lane == 0 && (size_t)(blockDim.x >> 5) * per_warp * sizeof(double) <= reserve_bytes) {
@@ -312,7 +313,7 @@ __global__ void k_riemann_interfaces_ens(const RiemannEnsArgs* __restrict__ a, i
   const int64_t n = off[D];
   int64_t T = (int64_t)gridDim.x * blockDim.x;
   int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  ExactRiemannDev rs;
+  ExactRiemannChainDev rs;
   init_solver(rs, a[0].md, a[0].P.rp, scratch, path_cap, tid, T);
   rs.eval_limit = eval_limit;
   unsigned long long acc[6] = {0, 0, 0, 0, 0, 0};
@@ -349,7 +350,7 @@ __global__ void __launch_bounds__(128) k_riemann_stragglers_ens(const RiemannEns
   const int64_t lane = threadIdx.x & 31;
   int64_t T = (int64_t)gridDim.x * blockDim.x;
   int64_t tid = (int64_t)blockIdx.x * blockDim.x + threadIdx.x;
-  ExactRiemannDev rs;
+  ExactRiemannChainDev rs;
   init_solver(rs, a[0].md, a[0].P.rp, scratch, path_cap, tid, T);
   const size_t per_warp = (size_t)6 * path_cap;
   if (lane == 0 && (size_t)(blockDim.x >> 5) * per_warp * sizeof(double) <= reserve_bytes) {
