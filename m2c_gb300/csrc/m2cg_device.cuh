@@ -135,13 +135,13 @@ template <bool Shared> M2CG_DEV double qrcp_t(const Quot& d) {
 
 // ---- equation of state ----------------------------------------------------
 M2CG_DEV double eos_p(const DevMat& M, double rho, double e) {
-  if (M.type == M2CG_EOS_SG) return M.gam1 * rho * e - M.gam * M.Pstiff;
+  if (M.type == M2CG_EOS_SG) return M.gam1 * rho * e - M.gamPs;   // gamPs = RN(gamma * pc), the same product
   if (M.type == M2CG_EOS_NASG) return M.gam1 * (e - M.q) / (1.0 / rho - M.b) - M.gamPs;
   double eta = 1.0 - M.rho0 / rho;
   return M.rho0_c0_c0 * eta * (1.0 - M.G0_half * eta) / ((1.0 - M.s * eta) * (1.0 - M.s * eta)) + M.G0_rho0 * (e - M.e0);
 }
 M2CG_DEV double eos_e(const DevMat& M, double rho, double p) {
-  if (M.type == M2CG_EOS_SG) return (p + M.gam * M.Pstiff) / (M.gam1 * rho);
+  if (M.type == M2CG_EOS_SG) return (p + M.gamPs) / (M.gam1 * rho);
   if (M.type == M2CG_EOS_NASG) return M.invgam1 * (p + M.gamPs) * (1.0 / rho - M.b) + M.q;
   double eta = 1.0 - M.rho0 / rho;
   return (p - M.rho0_c0_c0 * eta * (1.0 - M.G0_half * eta) / ((1.0 - M.s * eta) * (1.0 - M.s * eta))) / M.G0_rho0 + M.e0;
@@ -227,7 +227,7 @@ M2CG_DEV void cons_to_prim_fast(const DevMat& M, const double* U, double* V) {
   double ir = rcp_fast(U[0]);
   V[1] = U[1] * ir; V[2] = U[2] * ir; V[3] = U[3] * ir;
   double rhoe = U[4] - 0.5 * V[0] * (V[1] * V[1] + V[2] * V[2] + V[3] * V[3]);
-  if (M.type == M2CG_EOS_SG) V[4] = fma(M.gam1, rhoe, -M.gam * M.Pstiff);
+  if (M.type == M2CG_EOS_SG) V[4] = fma(M.gam1, rhoe, -M.gamPs);
   else V[4] = eos_p(M, V[0], rhoe * ir);
 }
 // VarFcnBase.h:173-186

@@ -141,6 +141,27 @@ def _residual_case(cfg, V, ID, phi):
     assert s.counters()["interface_faces"] == o.counters()["interface_faces"]
 
 
+@pytest.mark.parametrize("shape,extent", [
+    ((16, 16, 16), (1.0, 0.5, 2.0)),      # three spacings: one reciprocal per axis
+    ((64, 4, 1), (1.0, 0.0625, 0.01)),    # planar, the two active axes share a spacing
+    ((64, 4, 1), (1.0, 0.5, 0.01)),       # planar, different spacings
+])
+def test_dt_on_uneven_spacings(shape, extent):
+    """ComputeTimeStepSize's min over axes of h_d / (|u_d| + c) (SpaceOperator.cpp:1298-1330):
+    the kernel takes one reciprocal when every axis with more than one cell has
+    the same spacing, one per axis otherwise; axes of one cell do not count."""
+    cfg, V, ID, phi = (problems.shock_bubble(n=16) if shape[2] > 1 else problems.riemann1d(*shape))
+    cfg.nx, cfg.ny, cfg.nz = shape
+    cfg.xmax, cfg.ymax, cfg.zmax = cfg.x0 + extent[0], cfg.y0 + extent[1], cfg.z0 + extent[2]
+    rng = np.random.default_rng(11)
+    V = V.copy()
+    V[:, 1:4] += rng.uniform(-50, 50, (len(V), 3))   # a different fastest axis from cell to cell
+    s, o = _pair(cfg, V, ID, phi)
+    dt, cfl = s.ComputeTimeStepSize()
+    dto, cflo = o.compute_dt()
+    assert abs(dt - dto) <= 1e-14 * dto and abs(cfl - cflo) <= 1e-14
+
+
 def test_residual_riemann1d():
     _residual_case(*problems.riemann1d())
 
