@@ -96,6 +96,29 @@ struct ExactRiemannDevT {
 
   M2CG_DEV const DevMat& mat(int id) const { return mats->m[id]; }
 
+  // The sound speed of the state a Runge-Kutta step starts from.  The next
+  // step of an integration starts where the last one ended (an accepted step)
+  // or where it started (a rejected one), and the same state and material give
+  // the same bits, so the step keeps those two evaluations and reuses them:
+  // a fixed-step non-adaptive rarefaction runs thousands of RK4 steps in a
+  // stalled solve, each of whose first stage is an evaluation already made.
+  struct EosMemo {
+    const DevMat* M;
+    double rho, p, c2, c;
+  };
+  mutable EosMemo memo_start, memo_end;
+  M2CG_DEV void memo_clear() const { memo_start.M = nullptr; memo_end.M = nullptr; }
+  M2CG_DEV static bool memo_hit(const EosMemo& m, const DevMat& M, double rho, double p) {
+    return m.M == &M && __double_as_longlong(m.rho) == __double_as_longlong(rho) &&
+           __double_as_longlong(m.p) == __double_as_longlong(p);
+  }
+  // c^2 and c of (rho, p) from a kept evaluation; false if there is none
+  M2CG_DEV bool memo_get(const DevMat& M, double rho, double p, double& c2, double& c) const {
+    if (memo_hit(memo_end, M, rho, p)) { c2 = memo_end.c2; c = memo_end.c; return true; }
+    if (memo_hit(memo_start, M, rho, p)) { c2 = memo_start.c2; c = memo_start.c; return true; }
+    return false;
+  }
+
   // Cash-Karp step, ExactRiemannSolverBase.cpp:1771-1896.  The same
   // operations in the same order; a divisor that serves several quotients
   // (c_k^2, c_k, rho_k) takes its correctly rounded reciprocal once and each
@@ -103,11 +126,15 @@ struct ExactRiemannDevT {
   __device__ __noinline__ bool rk45(int wave, const DevMat& M, double rho_0, double u_0, double p_0, double dp,
                      double& rho, double& u, double& p, double& xi, double& uErr, double& rhoErr) const {
     dp = -dp;
-    double e_0 = eos_e(M, rho_0, p_0);
     const Quot R0 = quot_of_t<SharedDiv>(rho_0);
-    double c_0_square = eos_c2_q<SharedDiv>(M, rho_0, R0, e_0);
-    if (rho_0 <= 0 || c_0_square < 0) return false;
-    double c_0 = sqrt(c_0_square);
+    double c_0_square, c_0;
+    if (!memo_get(M, rho_0, p_0, c_0_square, c_0)) {
+      double e_0 = eos_e(M, rho_0, p_0);
+      c_0_square = eos_c2_q<SharedDiv>(M, rho_0, R0, e_0);
+      if (rho_0 <= 0 || c_0_square < 0) return false;
+      c_0 = sqrt(c_0_square);
+      memo_start = EosMemo{&M, rho_0, p_0, c_0_square, c_0};
+    }
     const Quot C0 = quot_of_t<SharedDiv>(c_0_square);
     double rho_1 = rho_0 + qdiv_t<SharedDiv>(0.2 * dp, C0);
     double p_1 = p_0 + 0.2 * dp;
@@ -166,7 +193,9 @@ struct ExactRiemannDevT {
     double e = eos_e(M, rho, p);
     double c = eos_c2(M, rho, e);
     if (rho <= 0 || c < 0) return false;
+    const double c2 = c;
     c = sqrt(c);
+    memo_end = EosMemo{&M, rho, p, c2, c};
     xi = (wave == 1) ? u - c : u + c;
     return true;
   }
@@ -176,11 +205,15 @@ struct ExactRiemannDevT {
   __device__ __noinline__ bool rk4(int wave, const DevMat& M, double rho_0, double u_0, double p_0, double dp,
                                    double& rho, double& u, double& p, double& xi) const {
     dp = -dp;
-    double e_0 = eos_e(M, rho_0, p_0);
     const Quot R0 = quot_of_t<SharedDiv>(rho_0);
-    double c_0_square = eos_c2_q<SharedDiv>(M, rho_0, R0, e_0);
-    if (rho_0 <= 0 || c_0_square < 0) return false;
-    double c_0 = sqrt(c_0_square);
+    double c_0_square, c_0;
+    if (!memo_get(M, rho_0, p_0, c_0_square, c_0)) {
+      double e_0 = eos_e(M, rho_0, p_0);
+      c_0_square = eos_c2_q<SharedDiv>(M, rho_0, R0, e_0);
+      if (rho_0 <= 0 || c_0_square < 0) return false;
+      c_0 = sqrt(c_0_square);
+      memo_start = EosMemo{&M, rho_0, p_0, c_0_square, c_0};
+    }
     const Quot C0 = quot_of_t<SharedDiv>(c_0_square);
     double rho_1 = rho_0 + qdiv_t<SharedDiv>(0.5 * dp, C0);
     double p_1 = p_0 + 0.5 * dp;
@@ -215,7 +248,9 @@ struct ExactRiemannDevT {
     double e = eos_e(M, rho, p);
     double c = eos_c2(M, rho, e);
     if (rho <= 0 || c < 0) return false;
+    const double c2 = c;
     c = sqrt(c);
+    memo_end = EosMemo{&M, rho, p, c2, c};
     xi = (wave == 1) ? u - c : u + c;
     return true;
   }
@@ -680,6 +715,7 @@ struct ExactRiemannDevT {
   __device__ __noinline__ int solve_once(const double* dir, const double* Vm, int idl, const double* Vp, int idr,
                                          double* Vs, int& id, double* Vsm, double* Vsp) {
     evals = 0;
+    memo_clear();
     double rhol = Vm[0], ul = Vm[1] * dir[0] + Vm[2] * dir[1] + Vm[3] * dir[2], pl = Vm[4];
     double rhor = Vp[0], ur = Vp[1] * dir[0] + Vp[2] * dir[1] + Vp[3] * dir[2], pr = Vp[4];
     path1.reset(pl, rhol, ul);
