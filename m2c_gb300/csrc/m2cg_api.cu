@@ -126,7 +126,7 @@ struct m2cg_ctx {
   // evaluation budget, then k_riemann_stragglers for the faces that outlast
   // it) on stream2, which has the highest priority so that the straggler
   // blocks are placed on empty SMs before the reconstruction kernel's.
-  int eval_limit = 16;
+  int eval_limit = 24;
   int sblocks = 0;             // straggler blocks of 128 threads (one SM each; idle ones exit at once)
   int strag_lanes = 1;         // straggler faces packed per warp (1: one face per warp)
   // Fused reconstruction + face flux (m2cg_tile.cu) for each state set, when
