@@ -665,7 +665,8 @@ def run_gb300(args):
            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
            "config": {"workload": f"shock-bubble {args.size}^3, SG/SG, MUSCL-van Albada, HLLC, exact interface "
                                   f"Riemann @1e-10, RK2, CFL 0.4", "cells": cells, "stages_per_step": stages,
-                      "l2": "inputs larger than L2 (state 52 B/cell x 16.8M cells = 0.87 GB per copy)",
+                      "l2": "inputs %s than L2 (state 52 B/cell x %.1fM cells = %.2f GB per copy)" %
+                            ("larger" if 52 * cells > 129e6 else "smaller", cells / 1e6, 52 * cells / 1e9),
                       "reinit_frequency": args.reinit if args.reinit > 0 else None,
                       "parallelism": "replicas" if world > 1 else "single"},
            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": nb_v + nb_i + nb_p,
