@@ -353,11 +353,11 @@ def ensemble_bench(n_domains, steps, seq_steps):
 
     reset()
     t0 = time.perf_counter()
-    budget, tuned_ms = ens.autotune(steps=1, budgets=(8, 16, 24, 32, 64))
+    budget, tuned_ms = ens.autotune(steps=1, budgets=(16, 24, 32, 64))
     shapes = ((0, 0, 0), (32, 4, 1), (16, 8, 1), (16, 4, 2))
     chosen, tile_ms = ens.autotune_tiles(steps=1, shapes=shapes)
     out["autotune"] = {"first_pass_eval_budget": budget, "budget_ms_per_step": tuned_ms,
-                       "budget_candidates": [8, 16, 24, 32, 64],
+                       "budget_candidates": [16, 24, 32, 64],
                        "block_shape_by_nx": {str(k): list(v) for k, v in sorted(chosen.items())},
                        "shape_candidates": [list(x) for x in shapes], "tuning_s": time.perf_counter() - t0}
     for mode, n in (("batched", steps), ("sequential", seq_steps)):
