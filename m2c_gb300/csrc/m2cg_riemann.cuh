@@ -107,7 +107,53 @@ struct ExactRiemannDevT {
     double rho, p, c2, c;
   };
   mutable EosMemo memo_start, memo_end;
-  M2CG_DEV void memo_clear() const { memo_start.M = nullptr; memo_end.M = nullptr; }
+  // The states a solve starts from are the same at every evaluation, so their
+  // internal energy, sound speed, dp/drho and 1/rho are kept from the first
+  // evaluation that needs each of them (keyed on the exact state and material).
+  struct SideMemo {
+    const DevMat* M;
+    double rho, p, e, c2, c, dpdrho, oor;
+    unsigned have;   // bits: 1 e, 2 c2, 4 c, 8 dpdrho, 16 oor
+  };
+  mutable SideMemo side_memo[2];
+  M2CG_DEV void memo_clear() const {
+    memo_start.M = nullptr;
+    memo_end.M = nullptr;
+    side_memo[0].M = nullptr;
+    side_memo[1].M = nullptr;
+  }
+  M2CG_DEV SideMemo& side(int wave, const DevMat& M, double rho, double p) const {
+    SideMemo& m = side_memo[wave == 1 ? 0 : 1];
+    if (!(m.M == &M && __double_as_longlong(m.rho) == __double_as_longlong(rho) &&
+          __double_as_longlong(m.p) == __double_as_longlong(p))) {
+      m.M = &M;
+      m.rho = rho;
+      m.p = p;
+      m.have = 0;
+    }
+    return m;
+  }
+  M2CG_DEV static double side_e(SideMemo& m) {
+    if (!(m.have & 1u)) { m.e = eos_e(*m.M, m.rho, m.p); m.have |= 1u; }
+    return m.e;
+  }
+  M2CG_DEV static double side_c2(SideMemo& m) {
+    if (!(m.have & 2u)) { m.c2 = eos_c2(*m.M, m.rho, side_e(m)); m.have |= 2u; }
+    return m.c2;
+  }
+  // only after the caller has checked c^2 >= 0
+  M2CG_DEV static double side_c(SideMemo& m) {
+    if (!(m.have & 4u)) { m.c = sqrt(side_c2(m)); m.have |= 4u; }
+    return m.c;
+  }
+  M2CG_DEV static double side_dpdrho(SideMemo& m) {
+    if (!(m.have & 8u)) { m.dpdrho = eos_dpdrho(*m.M, m.rho, side_e(m)); m.have |= 8u; }
+    return m.dpdrho;
+  }
+  M2CG_DEV static double side_oor(SideMemo& m) {
+    if (!(m.have & 16u)) { m.oor = 1.0 / m.rho; m.have |= 16u; }
+    return m.oor;
+  }
   M2CG_DEV static bool memo_hit(const EosMemo& m, const DevMat& M, double rho, double p) {
     return m.M == &M && __double_as_longlong(m.rho) == __double_as_longlong(rho) &&
            __double_as_longlong(m.p) == __double_as_longlong(p);
@@ -262,16 +308,16 @@ struct ExactRiemannDevT {
     double rhos_0 = rho, us_0 = u, ps_0 = p, xi_0;
     double rhos_1 = rho, us_1 = u, ps_1 = p, xi_1 = 0;
     double dp_target = (p - ps) / P.numSteps;
-    double e = eos_e(M, rho, p);
-    double dpdrho = eos_dpdrho(M, rho, e);
+    SideMemo& sm = side(wave, M, rho, p);
+    double dpdrho = side_dpdrho(sm);
     double drho_op1 = (p - ps) / dpdrho / P.numSteps;
     double drho_op2 = rho / (2.5 * P.numSteps);
     double drho_target = fmin(drho_op1, drho_op2);
     double dp = fmin(dp_target, drho_target * dpdrho);
     double tol_end = P.tol_rare * fmax(1.0, fabs(p));
-    double c = eos_c2(M, rho, e);
+    double c = side_c2(sm);
     if (rho <= 0 || c < 0) return false;
-    c = sqrt(c);
+    c = side_c(sm);
     if (path.n > 1) {
       int index0 = path.last_above(ps);
       ps_0 = path.get(index0, 0);
@@ -329,10 +375,10 @@ struct ExactRiemannDevT {
       double dp = (p - ps) / P.numSteps;
       double dp_min = dp / 2.5;
       double tol_end = P.tol_rare * fmax(1.0, fabs(p));
-      double e = eos_e(M, rho, p);
-      double c = eos_c2(M, rho, e);
+      SideMemo& sm = side(wave, M, rho, p);
+      double c = side_c2(sm);
       if (rho <= 0 || c < 0) return false;
-      c = sqrt(c);
+      c = side_c(sm);
       int index0 = 0;
       if (path.n > 1) {
         index0 = path.last_above(ps);
@@ -400,9 +446,10 @@ struct ExactRiemannDevT {
       }
       if (!done) return false;
     } else {
-      double e = eos_e(M, rho, p);
+      SideMemo& sm = side(wave, M, rho, p);
+      double e = side_e(sm);
       double pavg = 0.5 * (p + ps);
-      double oor = 1.0 / rho;
+      double oor = side_oor(sm);
       double f0, f1;
       double drho = fmax(fabs(rhos0 - rhos1), 0.001 * rhos0);
       bool found0 = false, found1 = false;
