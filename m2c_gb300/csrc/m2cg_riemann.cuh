@@ -809,6 +809,9 @@ struct ExactRiemannDevT {
     double f0 = ul0 - ur0, f1 = ul1 - ur1, f2;
     p2 = p1;
     f2 = f1;
+    // the stopping rule's two denominators do not change during the loop
+    const Quot Qp = quot_of_t<SharedDiv>(fmax(fabs(pl + 0.5 * rhol * ul * ul), fabs(pr + 0.5 * rhor * ur * ur)));
+    const Quot Qc = quot_of_t<SharedDiv>(fmax(cl, cr));
     int iter;
     for (iter = 0; iter < P.maxIts_main; iter++) {
       double denom = f1 - f0;
@@ -841,8 +844,8 @@ struct ExactRiemannDevT {
       f2 = ul2 - ur2;
       if (f0 * f2 < 0.0) { p1 = p2; f1 = f2; rhol1 = rhol2; rhor1 = rhor2; }
       else { p0 = p2; f0 = f2; rhol0 = rhol2; rhor0 = rhor2; }
-      double err_p = fabs(p1 - p0) / fmax(fabs(pl + 0.5 * rhol * ul * ul), fabs(pr + 0.5 * rhor * ur * ur));
-      double err_u = fabs(f2) / fmax(cl, cr);
+      double err_p = qdiv_t<SharedDiv>(fabs(p1 - p0), Qp);
+      double err_u = qdiv_t<SharedDiv>(fabs(f2), Qc);
       if ((err_p < P.tol_main && err_u < P.tol_main) || (err_p < P.tol_main * 1e-3) || (err_u < P.tol_main * 1e-3)) break;
       trans_rare = false;
     }
