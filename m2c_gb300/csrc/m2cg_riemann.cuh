@@ -95,6 +95,10 @@ struct ExactRiemannDevT {
   }
 
   M2CG_DEV const DevMat& mat(int id) const { return mats->m[id]; }
+  // the division policy (shared reciprocals or IEEE divisions, same bits)
+  M2CG_DEV static Quot qof(double b) { return quot_of_t<SharedDiv>(b); }
+  M2CG_DEV static double qd(double a, const Quot& d) { return qdiv_t<SharedDiv>(a, d); }
+  M2CG_DEV static double qr(const Quot& d) { return qrcp_t<SharedDiv>(d); }
 
   // The sound speed of the state a Runge-Kutta step starts from.  The next
   // step of an integration starts where the last one ended (an accepted step)
@@ -172,7 +176,7 @@ struct ExactRiemannDevT {
   __device__ __noinline__ bool rk45(int wave, const DevMat& M, double rho_0, double u_0, double p_0, double dp,
                      double& rho, double& u, double& p, double& xi, double& uErr, double& rhoErr) const {
     dp = -dp;
-    const Quot R0 = quot_of_t<SharedDiv>(rho_0);
+    const Quot R0 = qof(rho_0);
     double c_0_square, c_0;
     if (!memo_get(M, rho_0, p_0, c_0_square, c_0)) {
       double e_0 = eos_e(M, rho_0, p_0);
@@ -181,55 +185,55 @@ struct ExactRiemannDevT {
       c_0 = sqrt(c_0_square);
       memo_start = EosMemo{&M, rho_0, p_0, c_0_square, c_0};
     }
-    const Quot C0 = quot_of_t<SharedDiv>(c_0_square);
-    double rho_1 = rho_0 + qdiv_t<SharedDiv>(0.2 * dp, C0);
+    const Quot C0 = qof(c_0_square);
+    double rho_1 = rho_0 + qd(0.2 * dp, C0);
     double p_1 = p_0 + 0.2 * dp;
     double e_1 = eos_e(M, rho_1, p_1);
     double c_1_square = eos_c2(M, rho_1, e_1);
     if (rho_1 <= 0 || c_1_square < 0) return false;
-    const Quot C1 = quot_of_t<SharedDiv>(c_1_square);
-    double rho_2 = rho_0 + qdiv_t<SharedDiv>(3. / 40. * dp, C0) + qdiv_t<SharedDiv>(9. / 40. * dp, C1);
+    const Quot C1 = qof(c_1_square);
+    double rho_2 = rho_0 + qd(3. / 40. * dp, C0) + qd(9. / 40. * dp, C1);
     double p_2 = p_1 + 3. / 10. * dp;
     double e_2 = eos_e(M, rho_2, p_2);
-    const Quot R2 = quot_of_t<SharedDiv>(rho_2);
+    const Quot R2 = qof(rho_2);
     double c_2_square = eos_c2_q<SharedDiv>(M, rho_2, R2, e_2);
     if (rho_2 <= 0 || c_2_square < 0) return false;
     double c_2 = sqrt(c_2_square);
-    const Quot C2 = quot_of_t<SharedDiv>(c_2_square);
-    double rho_3 = rho_0 + qdiv_t<SharedDiv>(3. / 10. * dp, C0) - qdiv_t<SharedDiv>(9. / 10. * dp, C1) + qdiv_t<SharedDiv>(6. / 5. * dp, C2);
+    const Quot C2 = qof(c_2_square);
+    double rho_3 = rho_0 + qd(3. / 10. * dp, C0) - qd(9. / 10. * dp, C1) + qd(6. / 5. * dp, C2);
     double p_3 = p_0 + 3. / 5. * dp;
     double e_3 = eos_e(M, rho_3, p_3);
-    const Quot R3 = quot_of_t<SharedDiv>(rho_3);
+    const Quot R3 = qof(rho_3);
     double c_3_square = eos_c2_q<SharedDiv>(M, rho_3, R3, e_3);
     if (rho_3 <= 0 || c_3_square < 0) return false;
     double c_3 = sqrt(c_3_square);
-    const Quot C3 = quot_of_t<SharedDiv>(c_3_square);
-    double rho_4 = rho_0 - qdiv_t<SharedDiv>(11. / 54. * dp, C0) + qdiv_t<SharedDiv>(2.5 * dp, C1) - qdiv_t<SharedDiv>(70. / 27. * dp, C2) +
-                   qdiv_t<SharedDiv>(35. / 27. * dp, C3);
+    const Quot C3 = qof(c_3_square);
+    double rho_4 = rho_0 - qd(11. / 54. * dp, C0) + qd(2.5 * dp, C1) - qd(70. / 27. * dp, C2) +
+                   qd(35. / 27. * dp, C3);
     double p_4 = p_0 + dp;
     double e_4 = eos_e(M, rho_4, p_4);
-    const Quot R4 = quot_of_t<SharedDiv>(rho_4);
+    const Quot R4 = qof(rho_4);
     double c_4_square = eos_c2_q<SharedDiv>(M, rho_4, R4, e_4);
     if (rho_4 <= 0 || c_4_square < 0) return false;
     double c_4 = sqrt(c_4_square);
-    const Quot C4 = quot_of_t<SharedDiv>(c_4_square);
-    double rho_5 = rho_0 + qdiv_t<SharedDiv>(1631. / 55296. * dp, C0) + qdiv_t<SharedDiv>(175. / 512. * dp, C1) +
-                   qdiv_t<SharedDiv>(575. / 13824. * dp, C2) + qdiv_t<SharedDiv>(44275. / 110592. * dp, C3) + qdiv_t<SharedDiv>(253. / 4096. * dp, C4);
+    const Quot C4 = qof(c_4_square);
+    double rho_5 = rho_0 + qd(1631. / 55296. * dp, C0) + qd(175. / 512. * dp, C1) +
+                   qd(575. / 13824. * dp, C2) + qd(44275. / 110592. * dp, C3) + qd(253. / 4096. * dp, C4);
     double p_5 = p_0 + 7. / 8. * dp;
     double e_5 = eos_e(M, rho_5, p_5);
-    const Quot R5 = quot_of_t<SharedDiv>(rho_5);
+    const Quot R5 = qof(rho_5);
     double c_5_square = eos_c2_q<SharedDiv>(M, rho_5, R5, e_5);
     if (rho_5 <= 0 || c_5_square < 0) return false;
     double c_5 = sqrt(c_5_square);
-    const Quot C5 = quot_of_t<SharedDiv>(c_5_square);
-    double drho = (qdiv_t<SharedDiv>(37. / 378., C0) + qdiv_t<SharedDiv>(250. / 621., C2) + qdiv_t<SharedDiv>(125. / 594., C3) + qdiv_t<SharedDiv>(512. / 1771., C5)) * dp;
-    double drho_err = (qdiv_t<SharedDiv>(2825. / 27648., C0) + qdiv_t<SharedDiv>(18575. / 48384., C2) + qdiv_t<SharedDiv>(13525. / 55296., C3) +
-                       qdiv_t<SharedDiv>(277. / 14336., C4) + qdiv_t<SharedDiv>(0.25, C5)) * dp;
-    const Quot S0 = quot_of_t<SharedDiv>(c_0), S2 = quot_of_t<SharedDiv>(c_2), S3 = quot_of_t<SharedDiv>(c_3), S5 = quot_of_t<SharedDiv>(c_5);
-    double du = (qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(37. / 378., S0), R0) + qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(250. / 621., S2), R2) + qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(125. / 594., S3), R3) +
-                 qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(512. / 1771., S5), R5)) * dp;
-    double du_err = (qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(2825. / 27648., S0), R0) + qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(18575. / 48384., S2), R2) +
-                     qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(13525. / 55296., S3), R3) + qdiv_t<SharedDiv>(277. / 14336. / c_4, R4) + qdiv_t<SharedDiv>(qdiv_t<SharedDiv>(0.25, S5), R5)) * dp;
+    const Quot C5 = qof(c_5_square);
+    double drho = (qd(37. / 378., C0) + qd(250. / 621., C2) + qd(125. / 594., C3) + qd(512. / 1771., C5)) * dp;
+    double drho_err = (qd(2825. / 27648., C0) + qd(18575. / 48384., C2) + qd(13525. / 55296., C3) +
+                       qd(277. / 14336., C4) + qd(0.25, C5)) * dp;
+    const Quot S0 = qof(c_0), S2 = qof(c_2), S3 = qof(c_3), S5 = qof(c_5);
+    double du = (qd(qd(37. / 378., S0), R0) + qd(qd(250. / 621., S2), R2) + qd(qd(125. / 594., S3), R3) +
+                 qd(qd(512. / 1771., S5), R5)) * dp;
+    double du_err = (qd(qd(2825. / 27648., S0), R0) + qd(qd(18575. / 48384., S2), R2) +
+                     qd(qd(13525. / 55296., S3), R3) + qd(277. / 14336. / c_4, R4) + qd(qd(0.25, S5), R5)) * dp;
     if (isnan(du) || isnan(du_err)) return false;
     rhoErr = fabs(drho_err - drho);
     uErr = fabs(du_err - du);
@@ -251,7 +255,7 @@ struct ExactRiemannDevT {
   __device__ __noinline__ bool rk4(int wave, const DevMat& M, double rho_0, double u_0, double p_0, double dp,
                                    double& rho, double& u, double& p, double& xi) const {
     dp = -dp;
-    const Quot R0 = quot_of_t<SharedDiv>(rho_0);
+    const Quot R0 = qof(rho_0);
     double c_0_square, c_0;
     if (!memo_get(M, rho_0, p_0, c_0_square, c_0)) {
       double e_0 = eos_e(M, rho_0, p_0);
@@ -260,33 +264,33 @@ struct ExactRiemannDevT {
       c_0 = sqrt(c_0_square);
       memo_start = EosMemo{&M, rho_0, p_0, c_0_square, c_0};
     }
-    const Quot C0 = quot_of_t<SharedDiv>(c_0_square);
-    double rho_1 = rho_0 + qdiv_t<SharedDiv>(0.5 * dp, C0);
+    const Quot C0 = qof(c_0_square);
+    double rho_1 = rho_0 + qd(0.5 * dp, C0);
     double p_1 = p_0 + 0.5 * dp;
     double e_1 = eos_e(M, rho_1, p_1);
-    const Quot R1 = quot_of_t<SharedDiv>(rho_1);
+    const Quot R1 = qof(rho_1);
     double c_1_square = eos_c2_q<SharedDiv>(M, rho_1, R1, e_1);
     if (rho_1 <= 0 || c_1_square < 0) return false;
     double c_1 = sqrt(c_1_square);
-    const Quot C1 = quot_of_t<SharedDiv>(c_1_square);
-    double rho_2 = rho_0 + qdiv_t<SharedDiv>(0.5 * dp, C1);
+    const Quot C1 = qof(c_1_square);
+    double rho_2 = rho_0 + qd(0.5 * dp, C1);
     double p_2 = p_1;
     double e_2 = eos_e(M, rho_2, p_2);
-    const Quot R2 = quot_of_t<SharedDiv>(rho_2);
+    const Quot R2 = qof(rho_2);
     double c_2_square = eos_c2_q<SharedDiv>(M, rho_2, R2, e_2);
     if (rho_2 <= 0 || c_2_square < 0) return false;
     double c_2 = sqrt(c_2_square);
-    const Quot C2 = quot_of_t<SharedDiv>(c_2_square);
-    double rho_3 = rho_0 + qdiv_t<SharedDiv>(dp, C2);
+    const Quot C2 = qof(c_2_square);
+    double rho_3 = rho_0 + qd(dp, C2);
     double p_3 = p_0 + dp;
     double e_3 = eos_e(M, rho_3, p_3);
-    const Quot R3 = quot_of_t<SharedDiv>(rho_3);
+    const Quot R3 = qof(rho_3);
     double c_3_square = eos_c2_q<SharedDiv>(M, rho_3, R3, e_3);
     if (rho_3 <= 0 || c_3_square < 0) return false;
     double c_3 = sqrt(c_3_square);
-    double drho = 1.0 / 6.0 * dp * (qrcp_t<SharedDiv>(C0) + 2.0 * (qrcp_t<SharedDiv>(C1) + qrcp_t<SharedDiv>(C2)) + 1. / c_3_square);
+    double drho = 1.0 / 6.0 * dp * (qr(C0) + 2.0 * (qr(C1) + qr(C2)) + 1. / c_3_square);
     double du = 1.0 / 6.0 * dp *
-                (qdiv_t<SharedDiv>(1. / c_0, R0) + 2.0 * (qdiv_t<SharedDiv>(1. / c_1, R1) + qdiv_t<SharedDiv>(1. / c_2, R2)) + qdiv_t<SharedDiv>(1. / c_3, R3));
+                (qd(1. / c_0, R0) + 2.0 * (qd(1. / c_1, R1) + qd(1. / c_2, R2)) + qd(1. / c_3, R3));
     if (isnan(du)) return false;
     rho = rho_0 + drho;
     p = p_0 + dp;
@@ -810,8 +814,8 @@ struct ExactRiemannDevT {
     p2 = p1;
     f2 = f1;
     // the stopping rule's two denominators do not change during the loop
-    const Quot Qp = quot_of_t<SharedDiv>(fmax(fabs(pl + 0.5 * rhol * ul * ul), fabs(pr + 0.5 * rhor * ur * ur)));
-    const Quot Qc = quot_of_t<SharedDiv>(fmax(cl, cr));
+    const Quot Qp = qof(fmax(fabs(pl + 0.5 * rhol * ul * ul), fabs(pr + 0.5 * rhor * ur * ur)));
+    const Quot Qc = qof(fmax(cl, cr));
     int iter;
     for (iter = 0; iter < P.maxIts_main; iter++) {
       double denom = f1 - f0;
@@ -844,8 +848,8 @@ struct ExactRiemannDevT {
       f2 = ul2 - ur2;
       if (f0 * f2 < 0.0) { p1 = p2; f1 = f2; rhol1 = rhol2; rhor1 = rhor2; }
       else { p0 = p2; f0 = f2; rhol0 = rhol2; rhor0 = rhor2; }
-      double err_p = qdiv_t<SharedDiv>(fabs(p1 - p0), Qp);
-      double err_u = qdiv_t<SharedDiv>(fabs(f2), Qc);
+      double err_p = qd(fabs(p1 - p0), Qp);
+      double err_u = qd(fabs(f2), Qc);
       if ((err_p < P.tol_main && err_u < P.tol_main) || (err_p < P.tol_main * 1e-3) || (err_u < P.tol_main * 1e-3)) break;
       trans_rare = false;
     }
